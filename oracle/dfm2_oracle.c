@@ -1,0 +1,641 @@
+/*
+ * CPU oracle for DelFEM2's 3x3 block-CSR assembly -> ILU(0) -> PCG path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product): a plain-C
+ * restatement of the reference's serial algorithms. Each function names the
+ * reference file:line it follows (paths relative to the DelFEM2 source tree).
+ * Its results are pinned against the reference itself (oracle/ref_driver.cpp,
+ * built from the unmodified reference headers) by tests/test_oracle_*.py and
+ * by the committed fixtures under tests/golden/.
+ */
+#include "dfm2_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_UNSET 0xFFFFFFFFu
+
+/* ---------------------------------------------------------------------- */
+/* Mesh: include/delfem2/gridvoxel.cpp:194-271 (MeshTet3D_VoxelGrid with   */
+/* every voxel active). Lattice node (ix,iy,iz) has id                      */
+/* ix*(ny+1)*(nz+1) + iy*(nz+1) + iz and integer coordinates; `scale`       */
+/* multiplies them (1/n maps the lattice onto the unit cube). Each voxel is */
+/* split into six tets around its 0-6 diagonal, in the reference's order.   */
+void orc_voxel_tet_mesh(uint32_t nx, uint32_t ny, uint32_t nz, double scale,
+                        double *xyz, uint32_t *tet) {
+  const uint32_t my = ny + 1, mz = nz + 1;
+  size_t ip = 0;
+  for (uint32_t ix = 0; ix <= nx; ++ix)
+    for (uint32_t iy = 0; iy <= ny; ++iy)
+      for (uint32_t iz = 0; iz <= nz; ++iz) {
+        xyz[ip * 3 + 0] = (double)ix * scale;
+        xyz[ip * 3 + 1] = (double)iy * scale;
+        xyz[ip * 3 + 2] = (double)iz * scale;
+        ++ip;
+      }
+  /* corner k of the voxel -> (dx,dy,dz) */
+  static const uint32_t corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                        {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  static const int split[6][4] = {{0, 1, 2, 6}, {0, 1, 6, 5}, {0, 4, 5, 6},
+                                  {0, 2, 3, 6}, {0, 3, 7, 6}, {0, 4, 6, 7}};
+  size_t it = 0;
+  for (uint32_t vx = 0; vx < nx; ++vx)
+    for (uint32_t vy = 0; vy < ny; ++vy)
+      for (uint32_t vz = 0; vz < nz; ++vz) {
+        uint32_t id[8];
+        for (int k = 0; k < 8; ++k)
+          id[k] = (vx + corner[k][0]) * my * mz + (vy + corner[k][1]) * mz + (vz + corner[k][2]);
+        for (int s = 0; s < 6; ++s) {
+          for (int k = 0; k < 4; ++k) tet[it * 4 + k] = id[split[s][k]];
+          ++it;
+        }
+      }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Pattern: node-to-node adjacency excluding self,                          */
+/* include/delfem2/msh_topology_uniform.cpp:19-51 (elements around a point), */
+/* 250-299 (one-ring with a marker array, self marked first at 262) and     */
+/* 301-316 (the composition); rows then sorted ascending as                 */
+/* include/delfem2/jagarray.cpp:72-92 does (its bubble sort and the         */
+/* insertion sort here give the same order: the ids in a row are distinct). */
+static void orc_elsup(const uint32_t *elem, size_t nelem, uint32_t nnoel, size_t np,
+                      uint32_t **ind_out, uint32_t **elsup_out) {
+  uint32_t *ind = (uint32_t *)calloc(np + 1, sizeof(uint32_t));
+  for (size_t e = 0; e < nelem; ++e)
+    for (uint32_t k = 0; k < nnoel; ++k) ind[elem[e * nnoel + k] + 1] += 1;
+  for (size_t p = 0; p < np; ++p) ind[p + 1] += ind[p];
+  uint32_t *cursor = (uint32_t *)malloc((np + 1) * sizeof(uint32_t));
+  memcpy(cursor, ind, (np + 1) * sizeof(uint32_t));
+  uint32_t *elsup = (uint32_t *)malloc((size_t)ind[np] * sizeof(uint32_t) + 1);
+  for (size_t e = 0; e < nelem; ++e)
+    for (uint32_t k = 0; k < nnoel; ++k) elsup[cursor[elem[e * nnoel + k]]++] = (uint32_t)e;
+  free(cursor);
+  *ind_out = ind;
+  *elsup_out = elsup;
+}
+
+size_t orc_psup_count(const uint32_t *elem, size_t nelem, uint32_t nnoel, size_t np,
+                      uint32_t *psup_ind) {
+  uint32_t *eind, *elsup;
+  orc_elsup(elem, nelem, nnoel, np, &eind, &elsup);
+  uint32_t *mark = (uint32_t *)malloc(np * sizeof(uint32_t));
+  for (size_t p = 0; p < np; ++p) mark[p] = ORC_UNSET;
+  psup_ind[0] = 0;
+  for (size_t p = 0; p < np; ++p) {
+    uint32_t cnt = 0;
+    mark[p] = (uint32_t)p;
+    for (uint32_t q = eind[p]; q < eind[p + 1]; ++q) {
+      const uint32_t e = elsup[q];
+      for (uint32_t k = 0; k < nnoel; ++k) {
+        const uint32_t n = elem[(size_t)e * nnoel + k];
+        if (mark[n] != p) { mark[n] = (uint32_t)p; ++cnt; }
+      }
+    }
+    psup_ind[p + 1] = psup_ind[p] + cnt;
+  }
+  free(mark);
+  free(eind);
+  free(elsup);
+  return psup_ind[np];
+}
+
+void orc_psup_fill(const uint32_t *elem, size_t nelem, uint32_t nnoel, size_t np,
+                   const uint32_t *psup_ind, uint32_t *psup) {
+  uint32_t *eind, *elsup;
+  orc_elsup(elem, nelem, nnoel, np, &eind, &elsup);
+  uint32_t *mark = (uint32_t *)malloc(np * sizeof(uint32_t));
+  for (size_t p = 0; p < np; ++p) mark[p] = ORC_UNSET;
+  for (size_t p = 0; p < np; ++p) {
+    uint32_t w = psup_ind[p];
+    mark[p] = (uint32_t)p;
+    for (uint32_t q = eind[p]; q < eind[p + 1]; ++q) {
+      const uint32_t e = elsup[q];
+      for (uint32_t k = 0; k < nnoel; ++k) {
+        const uint32_t n = elem[(size_t)e * nnoel + k];
+        if (mark[n] != p) { mark[n] = (uint32_t)p; psup[w++] = n; }
+      }
+    }
+    /* ascending order inside the row (jagarray.cpp:72-92) */
+    for (uint32_t a = psup_ind[p] + 1; a < psup_ind[p + 1]; ++a) {
+      const uint32_t v = psup[a];
+      uint32_t b = a;
+      while (b > psup_ind[p] && psup[b - 1] > v) { psup[b] = psup[b - 1]; --b; }
+      psup[b] = v;
+    }
+  }
+  free(mark);
+  free(eind);
+  free(elsup);
+}
+
+/* ---------------------------------------------------------------------- */
+/* y = alpha*K*x + beta*y, include/delfem2/ls_block_sparse.cpp:215-223 (y is */
+/* scaled by beta first, even for beta == 0, so a NaN in y survives) and    */
+/* the 3x3 kernel at 103-133 (off-diagonal blocks, then the diagonal).       */
+void orc_bsr_matvec(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                    const double *vcrs, const double *vdia,
+                    double *y, double alpha, const double *x, double beta) {
+  for (size_t i = 0; i < (size_t)nblk * 3; ++i) y[i] *= beta;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    double *yi = y + (size_t)i * 3;
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const double *a = vcrs + (size_t)s * 9;
+      const double *xj = x + (size_t)col[s] * 3;
+      for (int r = 0; r < 3; ++r)
+        yi[r] += alpha * (a[r * 3 + 0] * xj[0] + a[r * 3 + 1] * xj[1] + a[r * 3 + 2] * xj[2]);
+    }
+    const double *d = vdia + (size_t)i * 9;
+    const double *xi = x + (size_t)i * 3;
+    for (int r = 0; r < 3; ++r)
+      yi[r] += alpha * (d[r * 3 + 0] * xi[0] + d[r * 3 + 1] * xi[1] + d[r * 3 + 2] * xi[2]);
+  }
+}
+
+/* CMatrixSparse<float>::MatVec, the same loops in single precision         */
+/* (explicit float instantiation at ls_block_sparse.cpp:274-282).           */
+void orc_bsr_matvec_f32(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                        const float *vcrs, const float *vdia,
+                        float *y, float alpha, const float *x, float beta) {
+  for (size_t i = 0; i < (size_t)nblk * 3; ++i) y[i] *= beta;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    float *yi = y + (size_t)i * 3;
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const float *a = vcrs + (size_t)s * 9;
+      const float *xj = x + (size_t)col[s] * 3;
+      for (int r = 0; r < 3; ++r)
+        yi[r] += alpha * (a[r * 3 + 0] * xj[0] + a[r * 3 + 1] * xj[1] + a[r * 3 + 2] * xj[2]);
+    }
+    const float *d = vdia + (size_t)i * 9;
+    const float *xi = x + (size_t)i * 3;
+    for (int r = 0; r < 3; ++r)
+      yi[r] += alpha * (d[r * 3 + 0] * xi[0] + d[r * 3 + 1] * xi[1] + d[r * 3 + 2] * xi[2]);
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Merge<nno,nno,3,3,double>, include/delfem2/ls_block_sparse.h:260-310:    */
+/* for each element row, mark the row's columns with their slots in          */
+/* merge_buffer, add the (irow,jcol) 3x3 block to the diagonal (same node)  */
+/* or to the marked slot, then reset the marks. Returns 0, or 1 on a         */
+/* missing slot (the reference returns false there).                         */
+int orc_merge(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+              double *vcrs, double *vdia, uint32_t nnoel, const uint32_t *nodes,
+              const double *emat, uint32_t *merge_buffer) {
+  (void)nblk;
+  for (uint32_t a = 0; a < nnoel; ++a) {
+    const uint32_t i = nodes[a];
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) merge_buffer[col[s]] = s;
+    for (uint32_t b = 0; b < nnoel; ++b) {
+      const uint32_t j = nodes[b];
+      const double *src = emat + ((size_t)a * nnoel + b) * 9;
+      double *dst;
+      if (i == j) {
+        dst = vdia + (size_t)i * 9;
+      } else {
+        if (merge_buffer[j] == ORC_UNSET) return 1;
+        dst = vcrs + (size_t)merge_buffer[j] * 9;
+      }
+      for (int k = 0; k < 9; ++k) dst[k] += src[k];
+    }
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) merge_buffer[col[s]] = ORC_UNSET;
+  }
+  return 0;
+}
+
+/* SetFixedBC = Dia(1) + Row + Col, include/delfem2/ls_block_sparse.h:147-151 */
+/* and ls_block_sparse.cpp:397-472: for every fixed DOF zero its row and     */
+/* column (keeping the matrix symmetric) and put 1 on the diagonal.          */
+void orc_set_fixed_bc(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                      double *vcrs, double *vdia, const int *bc) {
+  for (uint32_t i = 0; i < nblk; ++i) {
+    double *d = vdia + (size_t)i * 9;
+    for (int a = 0; a < 3; ++a) {
+      if (bc[(size_t)i * 3 + a] == 0) continue;
+      for (int b = 0; b < 3; ++b) { d[a * 3 + b] = 0.0; d[b * 3 + a] = 0.0; }
+      d[a * 3 + a] = 1.0;
+    }
+  }
+  for (uint32_t i = 0; i < nblk; ++i)
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s)
+      for (int a = 0; a < 3; ++a) {
+        if (bc[(size_t)i * 3 + a] == 0) continue;
+        for (int b = 0; b < 3; ++b) vcrs[(size_t)s * 9 + a * 3 + b] = 0.0;
+      }
+  for (uint32_t i = 0; i < nblk; ++i)
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const uint32_t j = col[s];
+      for (int b = 0; b < 3; ++b) {
+        if (bc[(size_t)j * 3 + b] == 0) continue;
+        for (int a = 0; a < 3; ++a) vcrs[(size_t)s * 9 + a * 3 + b] = 0.0;
+      }
+    }
+}
+
+/* setRHS_Zero, include/delfem2/vecxitrsol.cpp:286-296 (offset 0). */
+void orc_rhs_zero(double *b, const int *bc, size_t ndof) {
+  for (size_t i = 0; i < ndof; ++i)
+    if (bc[i] != 0) b[i] = 0.0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Linear tet element: TetVolume3D include/delfem2/femutil.cpp:202-212,     */
+/* TetDlDx femutil.cpp:215-258 (gradients of the barycentric coordinates),  */
+/* AddEmat_LinearSolid3<4> include/delfem2/fem_solidlinear.cpp:55-79:       */
+/*   K_e[i][j][a][b] = vol*(lambda dN_i[a] dN_j[b] + myu dN_j[a] dN_i[b]    */
+/*                          + myu (dN_i . dN_j) delta_ab)                    */
+static double orc_tet_volume(const double *p0, const double *p1, const double *p2,
+                             const double *p3) {
+  const double ax = p1[0] - p0[0], ay = p1[1] - p0[1], az = p1[2] - p0[2];
+  const double bx = p2[0] - p0[0], by = p2[1] - p0[1], bz = p2[2] - p0[2];
+  const double cx = p3[0] - p0[0], cy = p3[1] - p0[1], cz = p3[2] - p0[2];
+  return (ax * (by * cz - cy * bz) - ay * (bx * cz - cx * bz) + az * (bx * cy - cx * by)) / 6.0;
+}
+
+/* gradient of barycentric coordinate k: (face opposite k) normal / (6 vol)  */
+static void orc_tet_grad(const double P[4][3], double vol, double dN[4][3]) {
+  const double inv6v = 1.0 / (6.0 * vol);
+  for (int k = 0; k < 4; ++k) {
+    /* the other three vertices, ordered so that the sign matches a 0->1->2->3 */
+    /* positive orientation: N_k = 1 at P[k] and 0 on the opposite face.        */
+    const double *a = P[(k + 1) % 4], *b = P[(k + 2) % 4], *c = P[(k + 3) % 4];
+    const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+    const double wx = c[0] - a[0], wy = c[1] - a[1], wz = c[2] - a[2];
+    const double nx = uy * wz - uz * wy, ny = uz * wx - ux * wz, nz = ux * wy - uy * wx;
+    /* for odd k the cyclic triple has opposite orientation */
+    const double sgn = (k % 2 == 0) ? -1.0 : 1.0;
+    dN[k][0] = sgn * nx * inv6v;
+    dN[k][1] = sgn * ny * inv6v;
+    dN[k][2] = sgn * nz * inv6v;
+  }
+}
+
+void orc_emat_tet_linear(const double P[4][3], double myu, double lambda,
+                         double emat[4][4][3][3], double *vol_out) {
+  const double vol = orc_tet_volume(P[0], P[1], P[2], P[3]);
+  double dN[4][3];
+  orc_tet_grad(P, vol, dN);
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      const double dd = dN[i][0] * dN[j][0] + dN[i][1] * dN[j][1] + dN[i][2] * dN[j][2];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          emat[i][j][a][b] = vol * (lambda * dN[i][a] * dN[j][b] + myu * dN[j][a] * dN[i][b] +
+                                    (a == b ? myu * dd : 0.0));
+    }
+  if (vol_out) *vol_out = vol;
+}
+
+/* Per-tet-E assembly: the caller loop over EMat_SolidLinear_Static_Tet +   */
+/* Merge that MergeLinSys_SolidLinear_Static_MeshTet3D                      */
+/* (include/delfem2/fem_solidlinear.h:192-237) performs for scalar moduli.   */
+/* Residual per node: body force rho*g*vol/4 (213-221) minus K_e u_e        */
+/* (fem_solidlinear.cpp:430-434 with scale -1); b += residual; K += K_e.     */
+/* Lame parameters from (E, nu): lambda = E nu/((1+nu)(1-2nu)),             */
+/* myu = E/(2(1+nu)).                                                        */
+int orc_assemble_tet_linear(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                            double *vcrs, double *vdia, double *b,
+                            const double *xyz, const uint32_t *tet, size_t ntet,
+                            const double *young, double nu, double rho,
+                            const double g[3], const double *disp) {
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t));
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  double emat[4][4][3][3];
+  int status = 0;
+  for (size_t e = 0; e < ntet && status == 0; ++e) {
+    const uint32_t *n = tet + e * 4;
+    double P[4][3], U[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) {
+        P[k][d] = xyz[(size_t)n[k] * 3 + d];
+        U[k][d] = disp ? disp[(size_t)n[k] * 3 + d] : 0.0;
+      }
+    const double E = young[e];
+    const double lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    const double myu = E / (2.0 * (1.0 + nu));
+    double vol;
+    orc_emat_tet_linear(P, myu, lambda, emat, &vol);
+    for (int i = 0; i < 4; ++i) {
+      double res[3];
+      for (int a = 0; a < 3; ++a) res[a] = vol * rho * g[a] * 0.25;
+      for (int j = 0; j < 4; ++j)
+        for (int a = 0; a < 3; ++a)
+          res[a] -= emat[i][j][a][0] * U[j][0] + emat[i][j][a][1] * U[j][1] + emat[i][j][a][2] * U[j][2];
+      for (int a = 0; a < 3; ++a) b[(size_t)n[i] * 3 + a] += res[a];
+    }
+    status = orc_merge(nblk, row_start, col, vcrs, vdia, 4, n, &emat[0][0][0][0], buf);
+  }
+  free(buf);
+  return status;
+}
+
+/* Adjoint element term dL/dE_e = -lam_e^T (dK_e/dE_e) u_e. K_e is linear in */
+/* E (lambda and myu both scale with E), so dK_e/dE_e = K_e / E_e.           */
+void orc_tet_dLdE(const double *xyz, const uint32_t *tet, size_t ntet,
+                  const double *young, double nu, const double *u,
+                  const double *lam, double *dLdE) {
+  double emat[4][4][3][3];
+  const double lam1 = nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  const double myu1 = 1.0 / (2.0 * (1.0 + nu));
+  (void)young;
+  for (size_t e = 0; e < ntet; ++e) {
+    const uint32_t *n = tet + e * 4;
+    double P[4][3];
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) P[k][d] = xyz[(size_t)n[k] * 3 + d];
+    orc_emat_tet_linear(P, myu1, lam1, emat, NULL);
+    double s = 0.0;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j)
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c)
+            s += lam[(size_t)n[i] * 3 + a] * emat[i][j][a][c] * u[(size_t)n[j] * 3 + c];
+    dLdE[e] = -s;
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* SetPattern0, include/delfem2/ls_ilu_block_sparse.cpp:1057-1090: copy the */
+/* pattern, sort each row ascending, dia_ind[i] = first slot with col > i   */
+/* (row end if none).                                                        */
+void orc_ilu_pattern0(uint32_t nblk, const uint32_t *row_start, const uint32_t *col_in,
+                      uint32_t *col_out, uint32_t *dia_ind) {
+  memcpy(col_out, col_in, (size_t)row_start[nblk] * sizeof(uint32_t));
+  for (uint32_t i = 0; i < nblk; ++i) {
+    for (uint32_t a = row_start[i] + 1; a < row_start[i + 1]; ++a) {
+      const uint32_t v = col_out[a];
+      uint32_t b = a;
+      while (b > row_start[i] && col_out[b - 1] > v) { col_out[b] = col_out[b - 1]; --b; }
+      col_out[b] = v;
+    }
+    dia_ind[i] = row_start[i + 1];
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s)
+      if (col_out[s] > i) { dia_ind[i] = s; break; }
+  }
+}
+
+/* CopyValue, ls_ilu_block_sparse.cpp:1009-1047: zero the factor storage,  */
+/* scatter each matrix block into the ILU slot with the same column, copy   */
+/* the diagonal.                                                            */
+void orc_ilu_copy_value(uint32_t nblk, const uint32_t *row_start, const uint32_t *col_ilu,
+                        double *ilu_vcrs, double *ilu_vdia,
+                        const uint32_t *col_mat, const double *mat_vcrs,
+                        const double *mat_vdia) {
+  memset(ilu_vcrs, 0, (size_t)row_start[nblk] * 9 * sizeof(double));
+  int64_t *slot_of = (int64_t *)malloc((size_t)nblk * sizeof(int64_t));
+  for (uint32_t i = 0; i < nblk; ++i) slot_of[i] = -1;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) slot_of[col_ilu[s]] = s;
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const int64_t t = slot_of[col_mat[s]];
+      if (t < 0) continue;
+      memcpy(ilu_vcrs + (size_t)t * 9, mat_vcrs + (size_t)s * 9, 9 * sizeof(double));
+    }
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) slot_of[col_ilu[s]] = -1;
+  }
+  free(slot_of);
+  memcpy(ilu_vdia, mat_vdia, (size_t)nblk * 9 * sizeof(double));
+}
+
+/* 3x3 determinant and adjugate inverse (the cofactor formula used by       */
+/* ls_ilu_block_sparse.cpp:84-103).                                          */
+static double orc_det3(const double *m) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+static void orc_inv3(double *m) {
+  const double t[9] = {m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8]};
+  const double s = 1.0 / orc_det3(t);
+  m[0] = s * (t[4] * t[8] - t[5] * t[7]);
+  m[1] = s * (t[2] * t[7] - t[1] * t[8]);
+  m[2] = s * (t[1] * t[5] - t[2] * t[4]);
+  m[3] = s * (t[5] * t[6] - t[3] * t[8]);
+  m[4] = s * (t[0] * t[8] - t[2] * t[6]);
+  m[5] = s * (t[2] * t[3] - t[0] * t[5]);
+  m[6] = s * (t[3] * t[7] - t[4] * t[6]);
+  m[7] = s * (t[1] * t[6] - t[0] * t[7]);
+  m[8] = s * (t[0] * t[4] - t[1] * t[3]);
+}
+
+/* Decompose (double, 3x3 branch), ls_ilu_block_sparse.cpp:152-160,286-356: */
+/* rows in ascending order; for every k < i in row i (ascending) and every  */
+/* j > k in row k: A_ij -= A_ik A_kj when (i,j) is in the pattern (A_ii when */
+/* j == i). Then D_i <- inverse(D_i) unless |det| <= 1e-30 (counted as a    */
+/* singular pivot and left as is; more than 10 stops with failure), then    */
+/* U_ij <- D_i^-1 U_ij. Returns 0 on success, 1 on failure.                  */
+int orc_ilu_decompose(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                      const uint32_t *dia_ind, double *vcrs, double *vdia,
+                      int *n_singular) {
+  int64_t *slot_of = (int64_t *)malloc((size_t)nblk * sizeof(int64_t));
+  for (uint32_t i = 0; i < nblk; ++i) slot_of[i] = -1;
+  int nsing = 0, status = 0;
+  for (uint32_t i = 0; i < nblk && status == 0; ++i) {
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) slot_of[col[s]] = s;
+    for (uint32_t sk = row_start[i]; sk < dia_ind[i]; ++sk) {
+      const uint32_t k = col[sk];
+      const double *aik = vcrs + (size_t)sk * 9;
+      for (uint32_t sj = dia_ind[k]; sj < row_start[k + 1]; ++sj) {
+        const uint32_t j = col[sj];
+        double *aij;
+        if (j == i) {
+          aij = vdia + (size_t)i * 9;
+        } else {
+          if (slot_of[j] < 0) continue;
+          aij = vcrs + (size_t)slot_of[j] * 9;
+        }
+        const double *akj = vcrs + (size_t)sj * 9;
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c)
+            aij[r * 3 + c] -= aik[r * 3 + 0] * akj[0 * 3 + c] + aik[r * 3 + 1] * akj[1 * 3 + c] +
+                              aik[r * 3 + 2] * akj[2 * 3 + c];
+      }
+    }
+    double *dii = vdia + (size_t)i * 9;
+    if (fabs(orc_det3(dii)) > 1.0e-30) {
+      orc_inv3(dii);
+    } else {
+      ++nsing;
+      if (nsing > 10) status = 1;
+    }
+    if (status == 0) {
+      for (uint32_t s = dia_ind[i]; s < row_start[i + 1]; ++s) {
+        double *u = vcrs + (size_t)s * 9;
+        const double t[9] = {u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]};
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c)
+            u[r * 3 + c] = dii[r * 3 + 0] * t[0 * 3 + c] + dii[r * 3 + 1] * t[1 * 3 + c] +
+                           dii[r * 3 + 2] * t[2 * 3 + c];
+      }
+    }
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) slot_of[col[s]] = -1;
+  }
+  free(slot_of);
+  if (n_singular) *n_singular = nsing;
+  return status;
+}
+
+/* ForwardSubstitution 3x3, ls_ilu_block_sparse.cpp:544-573:                */
+/* v_i <- D_i^-1 (v_i - sum_{j<i} L_ij v_j), ascending rows, in place.      */
+void orc_ilu_forward(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                     const uint32_t *dia_ind, const double *vcrs, const double *vdia,
+                     double *vec) {
+  for (uint32_t i = 0; i < nblk; ++i) {
+    double t[3] = {vec[(size_t)i * 3], vec[(size_t)i * 3 + 1], vec[(size_t)i * 3 + 2]};
+    for (uint32_t s = row_start[i]; s < dia_ind[i]; ++s) {
+      const double *a = vcrs + (size_t)s * 9;
+      const double *vj = vec + (size_t)col[s] * 3;
+      for (int r = 0; r < 3; ++r) t[r] -= a[r * 3] * vj[0] + a[r * 3 + 1] * vj[1] + a[r * 3 + 2] * vj[2];
+    }
+    const double *d = vdia + (size_t)i * 9;
+    for (int r = 0; r < 3; ++r)
+      vec[(size_t)i * 3 + r] = d[r * 3] * t[0] + d[r * 3 + 1] * t[1] + d[r * 3 + 2] * t[2];
+  }
+}
+
+/* BackwardSubstitution 3x3, ls_ilu_block_sparse.cpp:721-749:               */
+/* v_i <- v_i - sum_{j>i} U'_ij v_j, descending rows, in place.             */
+void orc_ilu_backward(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                      const uint32_t *dia_ind, const double *vcrs, double *vec) {
+  for (uint32_t ii = nblk; ii-- > 0;) {
+    double t[3] = {vec[(size_t)ii * 3], vec[(size_t)ii * 3 + 1], vec[(size_t)ii * 3 + 2]};
+    for (uint32_t s = dia_ind[ii]; s < row_start[ii + 1]; ++s) {
+      const double *a = vcrs + (size_t)s * 9;
+      const double *vj = vec + (size_t)col[s] * 3;
+      for (int r = 0; r < 3; ++r) t[r] -= a[r * 3] * vj[0] + a[r * 3 + 1] * vj[1] + a[r * 3 + 2] * vj[2];
+    }
+    for (int r = 0; r < 3; ++r) vec[(size_t)ii * 3 + r] = t[r];
+  }
+}
+
+/* Level sets of the triangular sweeps (no reference counterpart: the       */
+/* reference sweeps rows serially). Forward: level(i) = 0 when row i has no */
+/* column j < i, else 1 + max level(j) over its columns j < i. Backward:    */
+/* the same over columns j > i. `order` lists the rows by (level, row id)   */
+/* ascending; level_start[l] is the first position of level l. Returns the  */
+/* number of levels.                                                         */
+uint32_t orc_ilu_levels(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                        const uint32_t *dia_ind, int backward, uint32_t *level,
+                        uint32_t *order, uint32_t *level_start) {
+  uint32_t nlev = 0;
+  for (uint32_t n = 0; n < nblk; ++n) {
+    const uint32_t i = backward ? nblk - 1 - n : n;
+    const uint32_t s0 = backward ? dia_ind[i] : row_start[i];
+    const uint32_t s1 = backward ? row_start[i + 1] : dia_ind[i];
+    uint32_t lv = 0;
+    for (uint32_t s = s0; s < s1; ++s) {
+      const uint32_t j = col[s];
+      if (j == i) continue;
+      if (level[j] + 1 > lv) lv = level[j] + 1;
+    }
+    level[i] = lv;
+    if (lv + 1 > nlev) nlev = lv + 1;
+  }
+  for (uint32_t l = 0; l <= nlev; ++l) level_start[l] = 0;
+  for (uint32_t i = 0; i < nblk; ++i) level_start[level[i] + 1] += 1;
+  for (uint32_t l = 0; l < nlev; ++l) level_start[l + 1] += level_start[l];
+  uint32_t *cursor = (uint32_t *)malloc(((size_t)nlev + 1) * sizeof(uint32_t));
+  memcpy(cursor, level_start, ((size_t)nlev + 1) * sizeof(uint32_t));
+  for (uint32_t i = 0; i < nblk; ++i) order[cursor[level[i]]++] = i;
+  free(cursor);
+  return nlev;
+}
+
+/* ---------------------------------------------------------------------- */
+double orc_dot(const double *a, const double *b, size_t n) {
+  double s = 0.0;
+  for (size_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+/* Solve_PCG, include/delfem2/lsitrsol.h:80-148 with the vector primitives  */
+/* of include/delfem2/view_vectorx.h:61-109. x starts at 0; history holds   */
+/* absolute residual norms [|r0|, |r1|, ...]; stops when                     */
+/* sqrt(|r|^2/|r0|^2) < tol; early return when |r0|^2 < 1e-30; one extra    */
+/* final entry when max_iter is exhausted. r is overwritten with the final   */
+/* residual. Returns the history length (entries past hist_cap are counted  */
+/* but not stored).                                                          */
+uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                       const double *vcrs, const double *vdia,
+                       const uint32_t *ilu_col, const uint32_t *dia_ind,
+                       const double *ilu_vcrs, const double *ilu_vdia,
+                       double *r, double *x, double tol, uint32_t max_iter,
+                       double *hist, uint32_t hist_cap) {
+  const size_t n = (size_t)nblk * 3;
+  uint32_t nh = 0;
+#define ORC_PUSH(v)                          \
+  do {                                       \
+    if (nh < hist_cap) hist[nh] = (v);       \
+    ++nh;                                    \
+  } while (0)
+  for (size_t k = 0; k < n; ++k) x[k] = 0.0;
+  const double sq0 = orc_dot(r, r, n);
+  ORC_PUSH(sqrt(sq0));
+  if (sq0 < 1.0e-30) return nh;
+  const double inv_sq0 = 1.0 / sq0;
+  double *Pr = (double *)malloc(n * sizeof(double));
+  double *p = (double *)malloc(n * sizeof(double));
+  memcpy(Pr, r, n * sizeof(double));
+  orc_ilu_forward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
+  orc_ilu_backward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
+  memcpy(p, Pr, n * sizeof(double));
+  double rPr = orc_dot(r, Pr, n);
+  int converged = 0;
+  for (uint32_t it = 0; it < max_iter; ++it) {
+    double *Ap = Pr; /* the reference reuses Pr's storage for Ap */
+    orc_bsr_matvec(nblk, row_start, col, vcrs, vdia, Ap, 1.0, p, 0.0);
+    const double pAp = orc_dot(p, Ap, n);
+    const double alpha = rPr / pAp;
+    for (size_t k = 0; k < n; ++k) r[k] += -alpha * Ap[k];
+    for (size_t k = 0; k < n; ++k) x[k] += alpha * p[k];
+    const double sq = orc_dot(r, r, n);
+    ORC_PUSH(sqrt(sq));
+    if (sqrt(sq * inv_sq0) < tol) { converged = 1; break; }
+    memcpy(Pr, r, n * sizeof(double));
+    orc_ilu_forward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
+    orc_ilu_backward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
+    const double rPr1 = orc_dot(r, Pr, n);
+    const double beta = rPr1 / rPr;
+    rPr = rPr1;
+    for (size_t k = 0; k < n; ++k) p[k] = beta * p[k] + Pr[k];
+  }
+  if (!converged) ORC_PUSH(sqrt(orc_dot(r, r, n)));
+#undef ORC_PUSH
+  free(Pr);
+  free(p);
+  return nh;
+}
+
+/* Solve_CG, include/delfem2/lsitrsol.h:35-74: history holds the relative   */
+/* ratio sqrt(|r|^2/|r0|^2) per iteration (no initial or final extra entry). */
+uint32_t orc_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                      const double *vcrs, const double *vdia, double *r, double *x,
+                      double tol, uint32_t max_iter, double *hist, uint32_t hist_cap) {
+  const size_t n = (size_t)nblk * 3;
+  uint32_t nh = 0;
+  for (size_t k = 0; k < n; ++k) x[k] = 0.0;
+  double sq = orc_dot(r, r, n);
+  if (sq < 1.0e-30) return 0;
+  const double inv_sq0 = 1.0 / sq;
+  double *p = (double *)malloc(n * sizeof(double));
+  double *Ap = (double *)malloc(n * sizeof(double));
+  memcpy(p, r, n * sizeof(double));
+  for (uint32_t it = 0; it < max_iter; ++it) {
+    orc_bsr_matvec(nblk, row_start, col, vcrs, vdia, Ap, 1.0, p, 0.0);
+    const double alpha = sq / orc_dot(p, Ap, n);
+    for (size_t k = 0; k < n; ++k) x[k] += alpha * p[k];
+    for (size_t k = 0; k < n; ++k) r[k] += -alpha * Ap[k];
+    const double sq1 = orc_dot(r, r, n);
+    const double ratio = sqrt(sq1 * inv_sq0);
+    if (nh < hist_cap) hist[nh] = ratio;
+    ++nh;
+    if (ratio < tol) break;
+    const double beta = sq1 / sq;
+    sq = sq1;
+    for (size_t k = 0; k < n; ++k) p[k] = beta * p[k] + r[k];
+  }
+  free(p);
+  free(Ap);
+  return nh;
+}

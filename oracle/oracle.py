@@ -1,0 +1,254 @@
+"""numpy front-end over the two CPU oracles (TEST INFRASTRUCTURE ONLY).
+
+* ``port()``: the plain-C restatement ``dfm2_oracle.c`` (builds anywhere).
+* ``reference()``: ``ref_driver.cpp`` over the unmodified DelFEM2 headers
+  (built only where the reference source tree exists).
+
+Both expose the same functions; arrays are numpy, indices uint32, values f64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libdfm2ref.so")
+
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def build(reference_tree: str | None = None, quiet: bool = True) -> None:
+    """Compile the restatement, and the reference driver when its tree exists."""
+    env = dict(os.environ)
+    if reference_tree:
+        env["REF"] = reference_tree
+    out = subprocess.run(["make", "-C", HERE, "all"], env=env, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def _optr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """One of the two CPU implementations, selected by symbol prefix."""
+
+    def __init__(self, so_path: str, prefix: str):
+        self.lib = C.CDLL(so_path)
+        self.prefix = prefix
+        self.kind = "reference" if prefix == "ref_" else "port"
+
+    def _f(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    # ---- mesh + pattern -------------------------------------------------
+    def voxel_tet_mesh(self, nx, ny, nz, scale=1.0):
+        np_ = (nx + 1) * (ny + 1) * (nz + 1)
+        nt = nx * ny * nz * 6
+        xyz = np.zeros(np_ * 3, np.float64)
+        tet = np.zeros(nt * 4, np.uint32)
+        f = self._f("voxel_tet_mesh")
+        f.argtypes = [C.c_uint32] * 3 + [C.c_double, _f64p, _u32p]
+        f(nx, ny, nz, scale, xyz, tet)
+        return xyz, tet
+
+    def psup(self, elem, nnoel, np_):
+        elem = np.ascontiguousarray(elem, np.uint32)
+        nelem = elem.size // nnoel
+        ind = np.zeros(np_ + 1, np.uint32)
+        fc = self._f("psup_count")
+        fc.argtypes = [_u32p, C.c_size_t, C.c_uint32, C.c_size_t, _u32p]
+        fc.restype = C.c_size_t
+        n = fc(elem, nelem, nnoel, np_, ind)
+        psup = np.zeros(max(n, 1), np.uint32)
+        ff = self._f("psup_fill")
+        ff.argtypes = [_u32p, C.c_size_t, C.c_uint32, C.c_size_t, _u32p, _u32p]
+        ff(elem, nelem, nnoel, np_, ind, psup)
+        return ind, psup[:n]
+
+    # ---- matrix ----------------------------------------------------------
+    def matvec(self, row_start, col, vcrs, vdia, y, alpha, x, beta):
+        nblk = row_start.size - 1
+        if vcrs.dtype == np.float32:
+            f = self._f("bsr_matvec_f32")
+            f.argtypes = [C.c_uint32, _u32p, _u32p, _f32p, _f32p, _f32p, C.c_float, _f32p, C.c_float]
+        else:
+            f = self._f("bsr_matvec")
+            f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, C.c_double, _f64p, C.c_double]
+        y = y.copy()
+        f(nblk, row_start, _nz(col), _nz(vcrs), vdia, y, alpha, x, beta)
+        return y
+
+    def merge(self, row_start, col, vcrs, vdia, nodes, emat):
+        nblk = row_start.size - 1
+        f = self._f("merge")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, C.c_uint32, _u32p, _f64p, _u32p]
+        f.restype = C.c_int
+        buf = np.full(nblk, 0xFFFFFFFF, np.uint32)
+        nodes = np.ascontiguousarray(nodes, np.uint32)
+        return f(nblk, row_start, _nz(col), _nz(vcrs), vdia, nodes.size, nodes,
+                 np.ascontiguousarray(emat, np.float64).ravel(), buf)
+
+    def set_fixed_bc(self, row_start, col, vcrs, vdia, bc):
+        nblk = row_start.size - 1
+        f = self._f("set_fixed_bc")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _i32p]
+        f(nblk, row_start, _nz(col), _nz(vcrs), vdia, np.ascontiguousarray(bc, np.int32))
+
+    def rhs_zero(self, b, bc):
+        f = self._f("rhs_zero")
+        f.argtypes = [_f64p, _i32p, C.c_size_t]
+        f(b, np.ascontiguousarray(bc, np.int32), b.size)
+
+    def emat_tet_linear(self, P, myu, lam):
+        f = self._f("emat_tet_linear")
+        f.argtypes = [_f64p, C.c_double, C.c_double, _f64p, _f64p]
+        emat = np.zeros(144, np.float64)
+        vol = np.zeros(1, np.float64)
+        f(np.ascontiguousarray(P, np.float64).ravel(), myu, lam, emat, vol)
+        return emat.reshape(4, 4, 3, 3), float(vol[0])
+
+    def assemble_tet_linear(self, row_start, col, vcrs, vdia, b, xyz, tet, young, nu, rho, g,
+                            disp=None):
+        nblk = row_start.size - 1
+        f = self._f("assemble_tet_linear")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, _f64p, _u32p, C.c_size_t,
+                      _f64p, C.c_double, C.c_double, _f64p, C.c_void_p]
+        f.restype = C.c_int
+        g = np.ascontiguousarray(g, np.float64)
+        return f(nblk, row_start, _nz(col), _nz(vcrs), vdia, b, xyz, tet, tet.size // 4,
+                 np.ascontiguousarray(young, np.float64), nu, rho, g, _optr(disp))
+
+    def tet_dLdE(self, xyz, tet, young, nu, u, lam):
+        f = self.lib.orc_tet_dLdE  # restatement only (the reference has no adjoint)
+        f.argtypes = [_f64p, _u32p, C.c_size_t, _f64p, C.c_double, _f64p, _f64p, _f64p]
+        out = np.zeros(tet.size // 4, np.float64)
+        f(xyz, tet, tet.size // 4, np.ascontiguousarray(young, np.float64), nu, u, lam, out)
+        return out
+
+    # ---- ILU -------------------------------------------------------------
+    def ilu_pattern0(self, row_start, col):
+        nblk = row_start.size - 1
+        f = self._f("ilu_pattern0")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, _u32p]
+        col_out = np.zeros(max(col.size, 1), np.uint32)
+        dia = np.zeros(nblk, np.uint32)
+        f(nblk, row_start, _nz(col), col_out, dia)
+        return col_out[: col.size], dia
+
+    def ilu_copy_value(self, row_start, col_ilu, col_mat, mat_vcrs, mat_vdia):
+        nblk = row_start.size - 1
+        f = self._f("ilu_copy_value")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _u32p, _f64p, _f64p]
+        vcrs = np.zeros(max(mat_vcrs.size, 9), np.float64)
+        vdia = np.zeros(nblk * 9, np.float64)
+        f(nblk, row_start, _nz(col_ilu), vcrs, vdia, _nz(col_mat), _nz(mat_vcrs), mat_vdia)
+        return vcrs[: mat_vcrs.size], vdia
+
+    def ilu_decompose(self, row_start, col, dia, vcrs, vdia):
+        """In place; returns (status, n_singular) with status 0 on success."""
+        nblk = row_start.size - 1
+        f = self._f("ilu_decompose")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p, _i32p]
+        f.restype = C.c_int
+        ns = np.zeros(1, np.int32)
+        st = f(nblk, row_start, _nz(col), dia, _nz(vcrs), vdia, ns)
+        return st, int(ns[0])
+
+    def ilu_forward(self, row_start, col, dia, vcrs, vdia, vec):
+        f = self._f("ilu_forward")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p]
+        v = np.array(vec, np.float64)
+        f(row_start.size - 1, row_start, _nz(col), dia, _nz(vcrs), vdia, v)
+        return v
+
+    def ilu_backward(self, row_start, col, dia, vcrs, vec):
+        f = self._f("ilu_backward")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p]
+        v = np.array(vec, np.float64)
+        f(row_start.size - 1, row_start, _nz(col), dia, _nz(vcrs), v)
+        return v
+
+    def ilu_levels(self, row_start, col, dia, backward=False):
+        """Level sets (restatement only; the reference sweeps serially)."""
+        nblk = row_start.size - 1
+        f = self.lib.orc_ilu_levels
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _u32p, C.c_int, _u32p, _u32p, _u32p]
+        f.restype = C.c_uint32
+        level = np.zeros(nblk, np.uint32)
+        order = np.zeros(nblk, np.uint32)
+        lstart = np.zeros(nblk + 1, np.uint32)
+        nlev = f(nblk, row_start, _nz(col), dia, int(backward), level, order, lstart)
+        return level, order, lstart[: nlev + 1]
+
+    # ---- Krylov ------------------------------------------------------------
+    def solve_pcg(self, row_start, col, vcrs, vdia, ilu_col, dia, ilu_vcrs, ilu_vdia, r, tol,
+                  max_iter):
+        """Returns (x, r_final, hist) for Solve_PCG on a copy of r."""
+        nblk = row_start.size - 1
+        f = self._f("solve_pcg")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _u32p, _u32p, _f64p, _f64p, _f64p,
+                      _f64p, C.c_double, C.c_uint32, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        r = np.array(r, np.float64)
+        x = np.zeros_like(r)
+        cap = max_iter + 2
+        hist = np.zeros(cap, np.float64)
+        nh = f(nblk, row_start, _nz(col), _nz(vcrs), vdia, _nz(ilu_col), dia, _nz(ilu_vcrs),
+               ilu_vdia, r, x, tol, max_iter, hist, cap)
+        return x, r, hist[:nh]
+
+    def solve_cg(self, row_start, col, vcrs, vdia, r, tol, max_iter):
+        nblk = row_start.size - 1
+        f = self._f("solve_cg")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, _f64p, C.c_double,
+                      C.c_uint32, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        r = np.array(r, np.float64)
+        x = np.zeros_like(r)
+        hist = np.zeros(max_iter + 2, np.float64)
+        nh = f(nblk, row_start, _nz(col), _nz(vcrs), vdia, r, x, tol, max_iter, hist, hist.size)
+        return x, r, hist[:nh]
+
+
+def _nz(a):
+    """Never hand a zero-length array to C (its data pointer may be NULL)."""
+    if a.size == 0:
+        return np.zeros(1, a.dtype)
+    return a
+
+
+_PORT = None
+_REF = None
+
+
+def port() -> Oracle:
+    global _PORT
+    if _PORT is None:
+        if not os.path.exists(PORT_SO):
+            build()
+        _PORT = Oracle(PORT_SO, "orc_")
+    return _PORT
+
+
+def HAVE_REFERENCE_BUILD() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def reference() -> Oracle:
+    global _REF
+    if _REF is None:
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError("reference driver not built (needs the DelFEM2 source tree)")
+        _REF = Oracle(REF_SO, "ref_")
+    return _REF
