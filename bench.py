@@ -1,0 +1,430 @@
+#!/usr/bin/env python
+"""Benchmark: PCG solve time at 3.24M DOF (128x128x64 voxel block, 6 tets per
+voxel, per-tet E log-uniform in [0.1, 10]), FP32-inner / FP64-refinement ILU(0)
+PCG to |b - K u| / |b| < 1e-10, next to the plain FP64 GPU Solve_PCG and the
+reference's CPU Solve_PCG.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one solve of K u = b from b resident in HBM (value), or through the
+C ABI with host buffers (e2e). Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PCG solve ms @3.2M DOF: FP32+FP64-refine vs FP64 to 1e-10; adjoint/forward"
+WORKLOAD = dict(nx=128, ny=128, nz=64, h=1.0 / 128, e_lo=0.1, e_hi=10.0, seed=3, nu=0.3, rho=1.0,
+                g=(0.0, 0.0, -1e-3), tol=1e-10, inner_tol=1e-4)
+SMALL = dict(WORKLOAD, nx=32, ny=32, nz=16, h=1.0 / 32)
+FALLBACK_HBM_GBS = 6800.0
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+
+        sm = [num(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.nanmedian(sm)), "sm_max_mhz": float(np.nanmax([num(r[2]) for r in rows])),
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": float(np.nanmax([num(r[3]) for r in rows]))}
+
+
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(kind: str, nb: int, nz: int, s: int) -> float:
+    """Bytes one launch of a kernel class must move (each array once per pass).
+
+    nb block rows, nz off-diagonal blocks, s = bytes per value; index arrays u32.
+    nz/2 blocks lie in each triangle (the pattern is symmetric)."""
+    v3 = 3 * s * nb
+    if kind == "spmv":      # K values + col + row_start, p read, Ap written
+        return 9 * s * (nz + nb) + 4 * nz + 4 * (nb + 1) + 2 * v3
+    if kind == "fwd":       # L blocks + D^-1 + col/row_start/dia_ind/order, in read, out written
+        return 9 * s * (nz / 2 + nb) + 4 * nz / 2 + 4 * (3 * nb + 1) + 2 * v3
+    if kind == "bwd":       # U' blocks + col/row_start/dia_ind/order, in read, out written
+        return 9 * s * (nz / 2) + 4 * nz / 2 + 4 * (3 * nb + 1) + 2 * v3
+    if kind == "update":    # r, x, p, Ap read; r, x written
+        return 6 * v3
+    if kind == "dot":       # r, z read
+        return 2 * v3
+    if kind == "pupdate":   # p, z read; p written
+        return 3 * v3
+    if kind == "fill":      # two output vectors written (two launches)
+        return v3
+    return float("nan")
+
+
+def traffic_from_profiles(kind: str):
+    """DRAM bytes per launch recorded from an ncu capture (profiles/ncu_traffic.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            t = json.load(f)
+        return t.get(kind)
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local, dist
+
+
+def reduce_max(dist, value: float, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_problem(w):
+    import delfem2_gb300 as D
+    t0 = time.perf_counter()
+    arrays = D.voxel_problem_arrays(w["nx"], w["ny"], w["nz"], w["h"], seed=w["seed"],
+                                    e_range=(w["e_lo"], w["e_hi"]))
+    t1 = time.perf_counter()
+    P = D.StaticElasticProblem(arrays, nu=w["nu"], rho=w["rho"], g=w["g"])
+    t2 = time.perf_counter()
+    return P, arrays, {"host_mesh_pattern_s": t1 - t0, "device_pattern_levels_s": t2 - t1}
+
+
+def iterations_to(hist, tol):
+    h = np.asarray(hist)
+    k = np.nonzero(h / h[0] < tol)[0]
+    return int(k[0]) if k.size else len(h) - 1
+
+
+def cpu_port_ms_per_iter(P, b_host, iters: int):
+    """Time `iters` Solve_PCG iterations of the C port on the device-assembled system."""
+    from oracle import port
+    O = port()
+    a = P.a
+    vc, vd = P.K.get_values()
+    col, dia = P.ilu.pattern()
+    ivc, ivd = P.ilu.values()
+    t = time.perf_counter()
+    O.solve_pcg(a["psup_ind"], a["psup"], vc, vd, col, dia, ivc, ivd, b_host, 1e-300, iters)
+    return (time.perf_counter() - t) * 1e3 / iters
+
+
+def run_ours(args):
+    import torch
+    import delfem2_gb300 as D
+    from delfem2_gb300 import _native as N
+
+    world, rank, local, dist = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = SMALL if args.small else WORKLOAD
+    P, arrays, setup = build_problem(w)
+    ndof = P.ndof
+    nz = int(arrays["psup"].size)
+    nb = int(arrays["np"])
+    lib = N.load()
+
+    t0 = time.perf_counter()
+    b = P.assemble(b=torch.zeros(ndof, dtype=torch.float64, device=dev))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    assert P.factor()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    setup.update(assemble_s=t1 - t0, ilu_s=t2 - t1)
+
+    def solve_mixed():
+        x = torch.zeros_like(b)
+        st = D.Solve_PCG_Mixed(b, x, w["tol"], P.K, P.ilu, inner_tol=w["inner_tol"])
+        return x, st
+
+    for _ in range(args.warmup):
+        x, st = solve_mixed()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    c0 = D._native.C.c_ulonglong(0)
+    lib.dfm2g_launch_count(D._native.C.byref(c0))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    stats = []
+    for _ in range(args.steps):
+        x, st = solve_mixed()
+        stats.append((st.iterations, st.outer, st.rel_residual, st.ms))
+    ev1.record()
+    torch.cuda.synchronize()
+    c1 = D._native.C.c_ulonglong(0)
+    lib.dfm2g_launch_count(D._native.C.byref(c1))
+    clk = clocks.stop()
+    if dist is not None:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = reduce_max(dist, ms, dev)
+    launches = int(c1.value - c0.value)
+
+    # plain FP64 GPU Solve_PCG on the same system (same metric, FP64 path)
+    xf = torch.zeros_like(b)
+    r = b.clone()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    hist64 = D.Solve_PCG(r, xf, w["tol"], 20000, P.K, P.ilu)
+    e1.record()
+    torch.cuda.synchronize()
+    fp64_ms = e0.elapsed_time(e1)
+    it64 = len(hist64) - 1
+
+    # accuracy: vs the FP64 GPU solution, and vs the reference's golden sample when present
+    xn = x.double().cpu().numpy()
+    err_fp64 = float(np.linalg.norm(xn - xf.cpu().numpy()) / np.linalg.norm(xf.cpu().numpy()))
+    err_oracle = None
+    gpath = os.path.join(ROOT, "tests", "golden", "cfg3.npz")
+    if not args.small and os.path.exists(gpath):
+        g = np.load(gpath)
+        err_oracle = float(np.abs(xn[g["idx"]] - g["x_sample"]).max() / np.abs(g["x_sample"]).max())
+
+    # adjoint / forward: forward = assemble + factor + solve; adjoint = solve
+    # K lam = dL/du on the same factors + the dL/dE element kernel
+    g_u = (x - 0.9 * x).contiguous()
+    ef0, ef1, ea1 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    ef0.record()
+    P.assemble(b=b)
+    P.factor()
+    xx, _ = solve_mixed()
+    ef1.record()
+    lam = torch.zeros_like(b)
+    D.Solve_PCG_Mixed(g_u, lam, w["tol"], P.K, P.ilu, inner_tol=w["inner_tol"])
+    dLdE = torch.zeros(arrays["ntet"], dtype=torch.float64, device=dev)
+    P.mesh.dLdE(w["nu"], xx, lam, dLdE)
+    ea1.record()
+    torch.cuda.synchronize()
+    fwd_ms, adj_ms = ef0.elapsed_time(ef1), ef1.elapsed_time(ea1)
+
+    # e2e: the public C-ABI call with HOST buffers (H2D of b and D2H of x inside)
+    bh = b.cpu().numpy().copy()
+    xh = np.zeros_like(bh)
+    D.Solve_PCG_Mixed(bh, xh, w["tol"], P.K, P.ilu, inner_tol=w["inner_tol"])
+    if dist is not None:
+        dist.barrier()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        D.Solve_PCG_Mixed(bh, xh, w["tol"], P.K, P.ilu, inner_tol=w["inner_tol"])
+    torch.cuda.synchronize()
+    e2e_ms = reduce_max(dist, (time.perf_counter() - t) * 1e3 / args.steps, dev)
+
+    # per-kernel device time (CUDA events around every launch, one extra solve)
+    lib.dfm2g_profile_reset()
+    lib.dfm2g_profile_enable(1)
+    solve_mixed()
+    lib.dfm2g_profile_enable(0)
+    prof = {}
+    for k, name in enumerate(N.PROF_KINDS):
+        cnt, tot = D._native.C.c_uint(0), D._native.C.c_double(0)
+        lib.dfm2g_profile_read(k, D._native.C.byref(cnt), D._native.C.byref(tot))
+        if cnt.value:
+            prof[name] = {"launches": cnt.value, "ms_total": tot.value, "ms_avg": tot.value / cnt.value}
+    hbm, peak_kind = peaks()
+    dom = max((k for k in prof if k in ("spmv", "fwd", "bwd", "update", "dot", "pupdate")),
+              key=lambda k: prof[k]["ms_total"])
+    alg = algorithmic_bytes(dom, nb, nz, 4)
+    achieved = alg / (prof[dom]["ms_avg"] * 1e-3) / 1e9
+    per_kernel = {k: dict(v, gbs=(algorithmic_bytes(k, nb, nz, 4) / (v["ms_avg"] * 1e-3) / 1e9
+                                  if k != "outer" else None)) for k, v in prof.items()}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        it_sample = args.cpu_iters
+        ms_it = cpu_port_ms_per_iter(P, b.cpu().numpy(), it_sample)
+        cpu = {"value": ms_it * it64, "unit": "ms", "cores": 1, "kind": "port",
+               "sample": f"{it_sample} Solve_PCG iterations of the C restatement on the same "
+                         f"{ndof}-DOF system ({ms_it:.1f} ms/iteration), scaled to the {it64} "
+                         f"iterations the FP64 solve takes to 1e-10",
+               "host_cores_available": os.cpu_count()}
+
+    its = [s[0] for s in stats]
+    out = {
+        "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic: voxel tet mesh, seeded log-uniform per-tet E, body force, z=0 clamped",
+        "config": {"workload": f"static linear elasticity, {w['nx']}x{w['ny']}x{w['nz']} voxels x 6 tets, "
+                               f"{ndof} DOF, ILU(0)-PCG FP32 inner (rel {w['inner_tol']}) + FP64 refinement "
+                               f"to {w['tol']}",
+                   "dof": ndof, "nblk": nb, "nnz_blocks": nz, "tets": arrays["ntet"],
+                   "l2": "inputs larger than L2 (FP32 K 0.57 GB, FP64 K 1.15 GB, factors 1.7 GB)",
+                   "parallelism": f"replicas x{world}"},
+        "iterations_inner": int(np.median(its)), "outer_steps": int(stats[-1][1]),
+        "rel_residual": stats[-1][2], "err_vs_fp64_gpu": err_fp64, "err_vs_reference_sample": err_oracle,
+        "fp64_ms": round(fp64_ms, 3), "fp64_iterations": it64,
+        "speedup_vs_fp64": round(fp64_ms / ms, 3),
+        "dof_iter_per_s": ndof * float(np.median(its)) / (ms * 1e-3),
+        "adjoint_over_forward": round(adj_ms / fwd_ms, 3), "forward_ms": round(fwd_ms, 3),
+        "adjoint_ms": round(adj_ms, 3),
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": 8 * ndof,
+                "d2h_bytes_per_step": 8 * ndof},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "algorithmic_bytes_per_launch": alg, "traffic": traffic_from_profiles(dom)},
+        "kernels": per_kernel,
+        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "setup": setup,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference's CPU Solve_PCG (oracle/_ref where it was built here, else
+    the C restatement), timed on this host; each step is a bounded sample of
+    PCG iterations on the same system, scaled to the full solve."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    w = SMALL if args.small else WORKLOAD
+    try:
+        O = oracle.reference()
+        kind = "reference"
+    except Exception:
+        O = oracle.port()
+        kind = "port"
+    t0 = time.perf_counter()
+    xyz, tet = O.voxel_tet_mesh(w["nx"], w["ny"], w["nz"], w["h"])
+    np_ = xyz.size // 3
+    ind, psup = O.psup(tet, 4, np_)
+    rng = np.random.default_rng(w["seed"])
+    young = np.exp(rng.uniform(np.log(w["e_lo"]), np.log(w["e_hi"]), tet.size // 4))
+    vc, vd, b = np.zeros(psup.size * 9), np.zeros(np_ * 9), np.zeros(np_ * 3)
+    O.assemble_tet_linear(ind, psup, vc, vd, b, xyz, tet, young, w["nu"], w["rho"], list(w["g"]))
+    bc = np.zeros(np_ * 3, np.int32)
+    bc[np.repeat(xyz[2::3] == 0.0, 3)] = 1
+    O.set_fixed_bc(ind, psup, vc, vd, bc)
+    O.rhs_zero(b, bc)
+    col, dia = O.ilu_pattern0(ind, psup)
+    ivc, ivd = O.ilu_copy_value(ind, col, psup, vc, vd)
+    O.ilu_decompose(ind, col, dia, ivc, ivd)
+    setup_s = time.perf_counter() - t0
+    gpath = os.path.join(ROOT, "tests", "golden", "cfg3.npz")
+    n_full = None
+    if not args.small and os.path.exists(gpath):
+        n_full = iterations_to(np.load(gpath)["hist"], w["tol"])
+    if n_full is None:  # run the full solve once to know the count (small workload)
+        _, _, h = O.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, w["tol"], 100000)
+        n_full = len(h) - 1
+    per = args.cpu_iters
+    for _ in range(args.warmup):
+        O.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, 1e-300, 1)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        O.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, 1e-300, per)
+    ms_it = (time.perf_counter() - t) * 1e3 / (args.steps * per)
+    value = ms_it * n_full
+    sample = (f"{per} Solve_PCG iterations per step ({ms_it:.1f} ms/iteration, 1 core, serial by construction) "
+              f"scaled to the {n_full} iterations FP64 ILU(0)-PCG needs to {w['tol']}")
+    out = {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "ms", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1), "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (same as ours)",
+           "config": {"workload": f"{w['nx']}x{w['ny']}x{w['nz']} voxels x 6 tets, {np_ * 3} DOF, FP64 "
+                                  f"ILU(0)-PCG to {w['tol']}", "dof": np_ * 3},
+           "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": 1, "kind": kind, "sample": sample,
+                            "host_cores_available": os.cpu_count(), "setup_s": round(setup_s, 2)},
+           "e2e": {"value": round(value, 1), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--small", action="store_true", help="32x32x16 voxels instead of 128x128x64")
+    ap.add_argument("--cpu-iters", type=int, default=6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

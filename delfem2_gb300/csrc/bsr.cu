@@ -1,0 +1,456 @@
+// CMatrixSparse<double> (3x3 blocks) on the device: pattern, values, fixed
+// boundary conditions, MatVec, and the colour-scheduled Merge.
+//
+// Device layout: row_start[nblk+1] and col[nnz] (u32, the reference's
+// col_ind_ / row_ptr_), vcrs[9*nnz] and vdia[9*nblk] (f64, row-major 3x3), plus
+// an FP32 mirror vcrs32/vdia32 used by the mixed-precision solver.
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace dfm2g {
+
+// ---------------------------------------------------------------------------
+// SpMV y = alpha*K*x + beta*y. One warp per block row (grid-stride). The row's
+// off-diagonal values are one contiguous run of 9*(s1-s0) scalars: lane l
+// reads scalars l, l+32, ... (coalesced), each scalar's block column comes from
+// a per-lane register of col[] via a shuffle, and the three row sums are
+// reduced with xor shuffles. The 3x3 diagonal block is handled by lanes 0-8.
+template <typename T>
+__global__ void __launch_bounds__(256) k_bsr_spmv(unsigned nblk, const unsigned *__restrict__ row_start,
+                                                  const unsigned *__restrict__ col,
+                                                  const T *__restrict__ vcrs, const T *__restrict__ vdia,
+                                                  T *__restrict__ y, T alpha, const T *__restrict__ x, T beta) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nblk; row += nwarp) {
+    const unsigned s0 = row_start[row], s1 = row_start[row + 1];
+    T a0 = 0, a1 = 0, a2 = 0;
+    for (unsigned cb = s0; cb < s1; cb += 32) {
+      const unsigned nb = min(32u, s1 - cb);
+      const unsigned my_col = lane < nb ? col[cb + lane] : 0u;
+      const size_t e_begin = (size_t)cb * 9, e_end = e_begin + (size_t)nb * 9;
+      for (size_t base = e_begin; base < e_end; base += 32) {
+        const size_t e = base + lane;
+        const bool ok = e < e_end;
+        const unsigned loc = ok ? (unsigned)(e - e_begin) : 0u;
+        const unsigned b = loc / 9u, rem = loc - b * 9u, r = rem / 3u, c = rem - r * 3u;
+        const unsigned j = __shfl_sync(0xffffffffu, my_col, b);
+        if (ok) {
+          const T v = vcrs[e] * x[(size_t)j * 3 + c];
+          a0 += (r == 0) ? v : T(0);
+          a1 += (r == 1) ? v : T(0);
+          a2 += (r == 2) ? v : T(0);
+        }
+      }
+    }
+    if (lane < 9) {
+      const unsigned r = lane / 3u, c = lane - r * 3u;
+      const T v = vdia[(size_t)row * 9 + lane] * x[(size_t)row * 3 + c];
+      a0 += (r == 0) ? v : T(0);
+      a1 += (r == 1) ? v : T(0);
+      a2 += (r == 2) ? v : T(0);
+    }
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    a2 = warp_sum(a2);
+    if (lane < 3) {
+      const T s = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
+      T *py = y + (size_t)row * 3 + lane;
+      *py = beta * *py + alpha * s;
+    }
+  }
+}
+
+int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta) {
+  const unsigned blocks = blocks_for((size_t)m->nblk * 32, 256, (unsigned)ctx().num_sms * 16);
+  if (prec == DFM2G_F64) {
+    k_bsr_spmv<double><<<blocks, 256, 0, stream()>>>(m->nblk, m->row_start.p, m->col.p, m->vcrs.p,
+                                                    m->vdia.p, (double *)y, alpha, (const double *)x, beta);
+  } else if (prec == DFM2G_F32) {
+    DFM2G_TRY(bsr_ensure_f32(m));
+    k_bsr_spmv<float><<<blocks, 256, 0, stream()>>>(m->nblk, m->row_start.p, m->col.p, m->vcrs32.p,
+                                                   m->vdia32.p, (float *)y, (float)alpha,
+                                                   (const float *)x, (float)beta);
+  } else {
+    return fail(DFM2G_ERR_ARG, "matvec: prec must be DFM2G_F64 or DFM2G_F32");
+  }
+  note_launches(1);
+  DFM2G_LAUNCH_CHECK();
+  return DFM2G_OK;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_to_f32(size_t n, const double *__restrict__ in, float *__restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+void to_f32(size_t n, const double *in, float *out) {
+  if (n) k_to_f32<<<blocks_for(n, 256, ctx().num_sms * 8), 256, 0, stream()>>>(n, in, out);
+}
+
+int bsr_ensure_f32(dfm2g_bsr_s *m) {
+  if (m->f32_valid) return DFM2G_OK;
+  DFM2G_TRY(m->vcrs32.ensure(m->nnz * 9 + 1));
+  DFM2G_TRY(m->vdia32.ensure((size_t)m->nblk * 9 + 1));
+  const unsigned cap = (unsigned)ctx().num_sms * 8;
+  if (m->nnz)
+    k_to_f32<<<blocks_for(m->nnz * 9, 256, cap), 256, 0, stream()>>>(m->nnz * 9, m->vcrs.p, m->vcrs32.p);
+  if (m->nblk)
+    k_to_f32<<<blocks_for((size_t)m->nblk * 9, 256, cap), 256, 0, stream()>>>((size_t)m->nblk * 9, m->vdia.p,
+                                                                            m->vdia32.p);
+  DFM2G_LAUNCH_CHECK();
+  m->f32_valid = true;
+  return DFM2G_OK;
+}
+
+// ---------------------------------------------------------------------------
+// SetFixedBC: for each fixed DOF zero its row and column, diagonal entry 1.
+__global__ void k_bsr_fixed_bc(unsigned nblk, const unsigned *__restrict__ row_start,
+                               const unsigned *__restrict__ col, double *__restrict__ vcrs,
+                               double *__restrict__ vdia, const int *__restrict__ bc) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nblk; row += nwarp) {
+    const bool f0 = bc[row * 3 + 0] != 0, f1 = bc[row * 3 + 1] != 0, f2 = bc[row * 3 + 2] != 0;
+    const unsigned s0 = row_start[row], s1 = row_start[row + 1];
+    for (unsigned s = s0 + lane; s < s1; s += 32) {
+      const unsigned j = col[s];
+      const bool g[3] = {bc[j * 3 + 0] != 0, bc[j * 3 + 1] != 0, bc[j * 3 + 2] != 0};
+      const bool f[3] = {f0, f1, f2};
+      double *a = vcrs + (size_t)s * 9;
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (f[r] || g[c]) a[r * 3 + c] = 0.0;
+    }
+    if (lane < 9) {
+      const unsigned r = lane / 3, c = lane % 3;
+      const bool f[3] = {f0, f1, f2};
+      double *d = vdia + (size_t)row * 9;
+      if (f[r] || f[c]) d[lane] = (r == c) ? 1.0 : 0.0;
+    }
+  }
+}
+
+__global__ void k_add_dia(unsigned nblk, double *vdia, double eps) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
+    vdia[(size_t)i * 9 + 0] += eps;
+    vdia[(size_t)i * 9 + 4] += eps;
+    vdia[(size_t)i * 9 + 8] += eps;
+  }
+}
+
+__global__ void k_zero_bc(size_t n, double *__restrict__ b, const int *__restrict__ bc) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (bc[i] != 0) b[i] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Colour-scheduled Merge. slot[(e*nno + a)*nno + b] is the val_crs_ slot of
+// block (elem[e][a], elem[e][b]) or kDiag when both nodes coincide.
+constexpr unsigned kDiag = 0xFFFFFFFFu;
+constexpr unsigned kMissing = 0xFFFFFFFEu;
+
+__global__ void k_slot_map(size_t nelem, unsigned nno, const unsigned *__restrict__ elem,
+                           const unsigned *__restrict__ row_start, const unsigned *__restrict__ col,
+                           unsigned *__restrict__ slot, int *__restrict__ missing) {
+  const size_t total = nelem * nno * nno;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = t / (nno * nno);
+    const unsigned ab = (unsigned)(t - e * nno * nno), a = ab / nno, b = ab - a * nno;
+    const unsigned i = elem[e * nno + a], j = elem[e * nno + b];
+    unsigned s = kDiag;
+    if (i != j) {
+      s = kMissing;
+      for (unsigned q = row_start[i]; q < row_start[i + 1]; ++q)
+        if (col[q] == j) { s = q; break; }
+      if (s == kMissing) atomicExch(missing, 1);
+    }
+    slot[t] = s;
+  }
+}
+
+__global__ void k_merge_color(unsigned n, const unsigned *__restrict__ list, unsigned nno,
+                              const unsigned *__restrict__ elem, const unsigned *__restrict__ slot,
+                              const double *__restrict__ emat, double *__restrict__ vcrs,
+                              double *__restrict__ vdia) {
+  const size_t total = (size_t)n * nno;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = list[t / nno];
+    const unsigned a = (unsigned)(t % nno);
+    const unsigned i = elem[e * nno + a];
+    for (unsigned b = 0; b < nno; ++b) {
+      const size_t k = (e * nno + a) * nno + b;
+      const unsigned s = slot[k];
+      double *dst = (s == kDiag) ? vdia + (size_t)i * 9 : vcrs + (size_t)s * 9;
+      const double *src = emat + k * 9;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) dst[q] += src[q];
+    }
+  }
+}
+
+int build_slot_map(const unsigned *d_elem, size_t nelem, unsigned nno, const dfm2g_bsr_s *m, unsigned *d_slot) {
+  DevBuf<int> d_missing;
+  DFM2G_TRY(d_missing.resize(1));
+  DFM2G_CUDA(cudaMemsetAsync(d_missing.p, 0, sizeof(int), stream()));
+  const size_t nslot = nelem * nno * nno;
+  if (nslot)
+    k_slot_map<<<blocks_for(nslot, 256, ctx().num_sms * 16), 256, 0, stream()>>>(nelem, nno, d_elem, m->row_start.p,
+                                                                                m->col.p, d_slot, d_missing.p);
+  DFM2G_LAUNCH_CHECK();
+  int missing = 0;
+  DFM2G_CUDA(cudaMemcpyAsync(&missing, d_missing.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (missing) return fail(DFM2G_ERR_MISSING_SLOT, "an element block is not in the sparsity pattern");
+  return DFM2G_OK;
+}
+
+// Greedy colouring: element e takes the lowest colour not yet used by any
+// element sharing one of its nodes. Deterministic (elements in index order).
+int color_elements(const unsigned *elem, size_t nelem, unsigned nno, size_t np,
+                   std::vector<unsigned> &by_color, std::vector<unsigned> &color_start) {
+  constexpr int kWords = 4;  // up to 256 colours
+  std::vector<uint64_t> used(np * kWords, 0);
+  std::vector<unsigned short> color(nelem);
+  unsigned ncolor = 0;
+  for (size_t e = 0; e < nelem; ++e) {
+    uint64_t m[kWords] = {0, 0, 0, 0};
+    for (unsigned a = 0; a < nno; ++a) {
+      const unsigned n = elem[e * nno + a];
+      if (n >= np) return fail(DFM2G_ERR_ARG, "element %zu names node %u >= %zu", e, n, np);
+      for (int w = 0; w < kWords; ++w) m[w] |= used[(size_t)n * kWords + w];
+    }
+    int c = -1;
+    for (int w = 0; w < kWords && c < 0; ++w)
+      if (~m[w]) c = w * 64 + __builtin_ctzll(~m[w]);
+    if (c < 0) return fail(DFM2G_ERR_UNSUPPORTED, "element colouring needs more than 256 colours");
+    color[e] = (unsigned short)c;
+    ncolor = std::max(ncolor, (unsigned)c + 1);
+    for (unsigned a = 0; a < nno; ++a) used[(size_t)elem[e * nno + a] * kWords + c / 64] |= 1ull << (c % 64);
+  }
+  color_start.assign(ncolor + 1, 0);
+  for (size_t e = 0; e < nelem; ++e) color_start[color[e] + 1]++;
+  for (unsigned c = 0; c < ncolor; ++c) color_start[c + 1] += color_start[c];
+  by_color.resize(nelem);
+  std::vector<unsigned> cur(color_start.begin(), color_start.end() - 1);
+  for (size_t e = 0; e < nelem; ++e) by_color[cur[color[e]]++] = (unsigned)e;
+  return DFM2G_OK;
+}
+
+}  // namespace dfm2g
+
+using namespace dfm2g;
+
+static int check_bsr(dfm2g_bsr m, bool need_pattern = true) {
+  if (!m) return fail(DFM2G_ERR_ARG, "null matrix handle");
+  if (need_pattern && !m->has_pattern) return fail(DFM2G_ERR_STATE, "matrix has no pattern (call set_pattern)");
+  return DFM2G_OK;
+}
+
+extern "C" {
+
+int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim) {
+  if (!out) return fail(DFM2G_ERR_ARG, "bsr_create: null out");
+  if (ndim != 3) return fail(DFM2G_ERR_UNSUPPORTED, "only 3x3 blocks are supported (ndim=%u)", ndim);
+  DFM2G_TRY(ensure_context());
+  auto *m = new dfm2g_bsr_s();
+  m->nblk = nblk;
+  *out = m;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_destroy(dfm2g_bsr m) {
+  if (m) {
+    cudaStreamSynchronize(stream());
+    delete m;
+  }
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_start, const unsigned *col,
+                          size_t ncol) {
+  DFM2G_TRY(check_bsr(m, false));
+  if (!row_start || n_row_start != (size_t)m->nblk + 1)
+    return fail(DFM2G_ERR_ARG, "set_pattern: row_start must have nblk+1 = %u entries", m->nblk + 1);
+  if (row_start[0] != 0 || row_start[m->nblk] != ncol)
+    return fail(DFM2G_ERR_PATTERN, "set_pattern: row_start[0] must be 0 and row_start[nblk] == ncol");
+  if (ncol && !col) return fail(DFM2G_ERR_ARG, "set_pattern: null col");
+  std::vector<unsigned> mark(m->nblk, 0xFFFFFFFFu);
+  for (unsigned i = 0; i < m->nblk; ++i) {
+    if (row_start[i + 1] < row_start[i]) return fail(DFM2G_ERR_PATTERN, "set_pattern: row_start decreases at %u", i);
+    for (unsigned s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const unsigned j = col[s];
+      if (j >= m->nblk) return fail(DFM2G_ERR_PATTERN, "set_pattern: column %u out of range in row %u", j, i);
+      if (j == i) return fail(DFM2G_ERR_PATTERN, "set_pattern: row %u lists its own diagonal block", i);
+      if (mark[j] == i) return fail(DFM2G_ERR_PATTERN, "set_pattern: duplicate column %u in row %u", j, i);
+      mark[j] = i;
+    }
+  }
+  DFM2G_TRY(ensure_context());
+  m->nnz = ncol;
+  m->h_row_start.assign(row_start, row_start + m->nblk + 1);
+  m->h_col.assign(col, col + ncol);
+  DFM2G_TRY(m->row_start.resize(m->nblk + 1));
+  DFM2G_TRY(m->col.resize(ncol + 1));
+  DFM2G_TRY(m->vcrs.resize(ncol * 9 + 1));
+  DFM2G_TRY(m->vdia.resize((size_t)m->nblk * 9 + 1));
+  DFM2G_CUDA(cudaMemcpyAsync(m->row_start.p, row_start, sizeof(unsigned) * (m->nblk + 1), cudaMemcpyHostToDevice,
+                             stream()));
+  if (ncol) DFM2G_CUDA(cudaMemcpyAsync(m->col.p, col, sizeof(unsigned) * ncol, cudaMemcpyHostToDevice, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * (ncol * 9 + 1), stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * ((size_t)m->nblk * 9 + 1), stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  m->has_pattern = true;
+  m->f32_valid = false;
+  m->pattern_version++;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_info(dfm2g_bsr m, unsigned *nblk, size_t *nnz) {
+  DFM2G_TRY(check_bsr(m, false));
+  if (nblk) *nblk = m->nblk;
+  if (nnz) *nnz = m->nnz;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_set_zero(dfm2g_bsr m) {
+  DFM2G_TRY(check_bsr(m));
+  DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * m->nnz * 9, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * m->nblk * 9, stream()));
+  m->f32_valid = false;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, int mem) {
+  DFM2G_TRY(check_bsr(m));
+  const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  if (vcrs && m->nnz) DFM2G_CUDA(cudaMemcpyAsync(m->vcrs.p, vcrs, sizeof(double) * 9 * m->nnz, k, stream()));
+  if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(m->vdia.p, vdia, sizeof(double) * 9 * m->nblk, k, stream()));
+  if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  m->f32_valid = false;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem) {
+  DFM2G_TRY(check_bsr(m));
+  const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (vcrs && m->nnz) DFM2G_CUDA(cudaMemcpyAsync(vcrs, m->vcrs.p, sizeof(double) * 9 * m->nnz, k, stream()));
+  if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, m->vdia.p, sizeof(double) * 9 * m->nblk, k, stream()));
+  if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem) {
+  DFM2G_TRY(check_bsr(m));
+  if (!bc) return fail(DFM2G_ERR_ARG, "set_fixed_bc: null bc");
+  VecArg<int> a;
+  DFM2G_TRY(a.in(bc, (size_t)m->nblk * 3, mem, true));
+  k_bsr_fixed_bc<<<blocks_for((size_t)m->nblk * 32, 256, ctx().num_sms * 16), 256, 0, stream()>>>(
+      m->nblk, m->row_start.p, m->col.p, m->vcrs.p, m->vdia.p, a.dev());
+  DFM2G_LAUNCH_CHECK();
+  if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  m->f32_valid = false;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_add_dia(dfm2g_bsr m, double eps) {
+  DFM2G_TRY(check_bsr(m));
+  k_add_dia<<<blocks_for(m->nblk, 256, ctx().num_sms * 8), 256, 0, stream()>>>(m->nblk, m->vdia.p, eps);
+  DFM2G_LAUNCH_CHECK();
+  m->f32_valid = false;
+  return DFM2G_OK;
+}
+
+int dfm2g_bsr_update_f32(dfm2g_bsr m) {
+  DFM2G_TRY(check_bsr(m));
+  m->f32_valid = false;
+  return bsr_ensure_f32(m);
+}
+
+int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x, double beta, int mem) {
+  DFM2G_TRY(check_bsr(m));
+  if (!y || !x) return fail(DFM2G_ERR_ARG, "matvec: null vector");
+  const size_t n = (size_t)m->nblk * 3;
+  if (prec == DFM2G_F64) {
+    VecArg<double> ay, ax;
+    DFM2G_TRY(ay.in((double *)y, n, mem, true));
+    DFM2G_TRY(ax.in((const double *)x, n, mem, true));
+    DFM2G_TRY(bsr_spmv(m, prec, ay.dev(), alpha, ax.dev(), beta));
+    return ay.copy_back();
+  }
+  if (prec == DFM2G_F32) {
+    VecArg<float> ay, ax;
+    DFM2G_TRY(ay.in((float *)y, n, mem, true));
+    DFM2G_TRY(ax.in((const float *)x, n, mem, true));
+    DFM2G_TRY(bsr_spmv(m, prec, ay.dev(), alpha, ax.dev(), beta));
+    return ay.copy_back();
+  }
+  return fail(DFM2G_ERR_ARG, "matvec: prec must be DFM2G_F64 or DFM2G_F32");
+}
+
+int dfm2g_vec_zero_bc(double *b, const int *bc, size_t ndof, int mem) {
+  if (!b || !bc) return fail(DFM2G_ERR_ARG, "vec_zero_bc: null argument");
+  DFM2G_TRY(ensure_context());
+  VecArg<double> ab;
+  VecArg<int> af;
+  DFM2G_TRY(ab.in(b, ndof, mem, true));
+  DFM2G_TRY(af.in(bc, ndof, mem, true));
+  k_zero_bc<<<blocks_for(ndof, 256, ctx().num_sms * 8), 256, 0, stream()>>>(ndof, ab.dev(), af.dev());
+  DFM2G_LAUNCH_CHECK();
+  return ab.copy_back();
+}
+
+int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned *elem, const double *emat,
+                    int mem) {
+  DFM2G_TRY(check_bsr(m));
+  if (nelem == 0) return DFM2G_OK;
+  if (!elem || !emat || nnoel == 0) return fail(DFM2G_ERR_ARG, "merge: null argument");
+  // Colouring needs the connectivity on the host.
+  std::vector<unsigned> h_elem((size_t)nelem * nnoel);
+  if (mem == DFM2G_MEM_HOST) {
+    std::memcpy(h_elem.data(), elem, h_elem.size() * sizeof(unsigned));
+  } else {
+    DFM2G_CUDA(cudaMemcpyAsync(h_elem.data(), elem, h_elem.size() * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                               stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  }
+  std::vector<unsigned> by_color, color_start;
+  DFM2G_TRY(color_elements(h_elem.data(), nelem, nnoel, m->nblk, by_color, color_start));
+  DevBuf<unsigned> d_elem, d_list, d_slot;
+  DevBuf<int> d_missing;
+  DFM2G_TRY(d_elem.resize(h_elem.size()));
+  DFM2G_TRY(d_list.resize(nelem));
+  DFM2G_TRY(d_slot.resize((size_t)nelem * nnoel * nnoel));
+  DFM2G_TRY(d_missing.resize(1));
+  DFM2G_CUDA(cudaMemcpyAsync(d_elem.p, h_elem.data(), h_elem.size() * sizeof(unsigned), cudaMemcpyHostToDevice,
+                             stream()));
+  DFM2G_CUDA(cudaMemcpyAsync(d_list.p, by_color.data(), nelem * sizeof(unsigned), cudaMemcpyHostToDevice,
+                             stream()));
+  DFM2G_CUDA(cudaMemsetAsync(d_missing.p, 0, sizeof(int), stream()));
+  VecArg<double> a_emat;
+  DFM2G_TRY(a_emat.in(emat, (size_t)nelem * nnoel * nnoel * 9, mem, true));
+  const size_t nslot = (size_t)nelem * nnoel * nnoel;
+  k_slot_map<<<blocks_for(nslot, 256, ctx().num_sms * 16), 256, 0, stream()>>>(
+      nelem, nnoel, d_elem.p, m->row_start.p, m->col.p, d_slot.p, d_missing.p);
+  DFM2G_LAUNCH_CHECK();
+  int missing = 0;
+  DFM2G_CUDA(cudaMemcpyAsync(&missing, d_missing.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (missing) return fail(DFM2G_ERR_MISSING_SLOT, "merge: an element block is not in the sparsity pattern");
+  for (size_t c = 0; c + 1 < color_start.size(); ++c) {
+    const unsigned n = color_start[c + 1] - color_start[c];
+    k_merge_color<<<blocks_for((size_t)n * nnoel, 128, ctx().num_sms * 16), 128, 0, stream()>>>(
+        n, d_list.p + color_start[c], nnoel, d_elem.p, d_slot.p, a_emat.dev(), m->vcrs.p, m->vdia.p);
+    DFM2G_LAUNCH_CHECK();
+  }
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  m->f32_valid = false;
+  return DFM2G_OK;
+}
+
+}  // extern "C"

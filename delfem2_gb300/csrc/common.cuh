@@ -1,0 +1,273 @@
+// Shared internals of libdfm2g: error plumbing, the library stream, handle
+// layouts and small device helpers. Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/dfm2g.h"
+
+namespace dfm2g {
+
+// ---- errors ----------------------------------------------------------------
+void set_error(const char *fmt, ...);
+int fail(int status, const char *fmt, ...);
+
+#define DFM2G_CUDA(call)                                                              \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return ::dfm2g::fail(DFM2G_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, \
+                           cudaGetErrorString(e_));                                   \
+  } while (0)
+
+#define DFM2G_TRY(call)            \
+  do {                             \
+    int s_ = (call);               \
+    if (s_ != DFM2G_OK) return s_; \
+  } while (0)
+
+#define DFM2G_LAUNCH_CHECK() DFM2G_CUDA(cudaGetLastError())
+
+// ---- instrumentation -----------------------------------------------------------
+void note_launches(unsigned n);
+// Times the launches between construction and destruction as one `kind`
+// sample when profiling is on; counts them always.
+struct ProfScope {
+  int kind;
+  unsigned n;
+  bool on;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(int kind, unsigned launches);
+  ~ProfScope();
+};
+
+// ---- context ---------------------------------------------------------------
+struct Context {
+  cudaStream_t stream = nullptr;
+  cudaStream_t own = nullptr;
+  int device = -1;
+  int num_sms = 0;
+};
+Context &ctx();
+int ensure_context();
+inline cudaStream_t stream() { return ctx().stream; }
+
+// ---- device buffers ----------------------------------------------------------
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  int resize(size_t count) {
+    if (count == n && p) return DFM2G_OK;
+    release();
+    if (count == 0) return DFM2G_OK;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(DFM2G_ERR_CUDA, "cudaMalloc(%zu bytes): %s", count * sizeof(T),
+                  cudaGetErrorString(e));
+    }
+    n = count;
+    return DFM2G_OK;
+  }
+  int ensure(size_t count) { return (n >= count && p) ? DFM2G_OK : resize(count); }
+};
+
+// Stage a host or device vector argument: `dev()` is a device pointer holding
+// the caller's data; copy_back() returns results to a host caller.
+template <typename T>
+struct VecArg {
+  T *user = nullptr;
+  size_t n = 0;
+  int mem = DFM2G_MEM_DEVICE;
+  DevBuf<T> tmp;
+  int in(const T *u, size_t count, int m, bool copy_in) {
+    user = const_cast<T *>(u);
+    n = count;
+    mem = m;
+    if (m == DFM2G_MEM_DEVICE) return DFM2G_OK;
+    if (m != DFM2G_MEM_HOST) return fail(DFM2G_ERR_ARG, "mem flag must be 0 (host) or 1 (device)");
+    DFM2G_TRY(tmp.resize(count));
+    if (copy_in && count)
+      DFM2G_CUDA(cudaMemcpyAsync(tmp.p, u, count * sizeof(T), cudaMemcpyHostToDevice, stream()));
+    return DFM2G_OK;
+  }
+  T *dev() const { return mem == DFM2G_MEM_DEVICE ? user : tmp.p; }
+  int copy_back() {
+    if (mem == DFM2G_MEM_HOST && n) {
+      DFM2G_CUDA(cudaMemcpyAsync(user, tmp.p, n * sizeof(T), cudaMemcpyDeviceToHost, stream()));
+      DFM2G_CUDA(cudaStreamSynchronize(stream()));
+    }
+    return DFM2G_OK;
+  }
+};
+
+// ---- grid sizing -------------------------------------------------------------
+inline unsigned blocks_for(size_t work, unsigned per_block, unsigned cap = 0xFFFFFFFFu) {
+  size_t b = (work + per_block - 1) / per_block;
+  if (b == 0) b = 1;
+  if (b > cap) b = cap;
+  return (unsigned)b;
+}
+
+// ---- device helpers ------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float ld_relaxed(const float *p) {
+  float v;
+  asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_relaxed(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_relaxed(const int *p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(float *p, float v) {
+  asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(double *p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// "Not yet written" marker for values produced by the sync-free sweeps: an
+// all-ones NaN. Arithmetic on the GPU only produces the canonical NaN
+// (0x7fffffff / 0x7fffffffffffffff), so a computed value never equals it.
+__device__ __forceinline__ bool is_pending(float v) { return __float_as_uint(v) == 0xffffffffu; }
+__device__ __forceinline__ bool is_pending(double v) {
+  return __double_as_longlong(v) == (long long)-1;
+}
+
+// Default bound on every device-side wait.
+constexpr unsigned long long kWaitTimeoutNs = 1000000000ull;  // 1 s
+
+// Block-wide FP64 sum; valid in thread 0. `sh` holds >= blockDim.x/32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? sh[lane] : 0.0;
+    v = warp_sum(v);
+  }
+  return v;
+}
+
+// Deterministic grid reduction: every block writes its partial sum, the last
+// block to arrive (ticket) adds the partials in block order. Returns true in
+// thread 0 of the last block, with *total set; the ticket is reset there.
+__device__ __forceinline__ bool grid_sum_last(double partial, double *partials,
+                                              unsigned *ticket, double *sh, double *total) {
+  __shared__ bool am_last;
+  double v = block_sum(partial, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = v;
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double s = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += ld_relaxed(partials + b);
+  // fixed-order combination: per-thread strided sums then a fixed tree
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) {
+    *total = s;
+    *ticket = 0;
+  }
+  return threadIdx.x == 0;
+}
+
+}  // namespace dfm2g
+
+// ---- handle layouts -----------------------------------------------------------------
+struct dfm2g_bsr_s {
+  unsigned nblk = 0;
+  size_t nnz = 0;
+  bool has_pattern = false;
+  std::vector<unsigned> h_row_start, h_col;  // host copy of the pattern
+  dfm2g::DevBuf<unsigned> row_start, col;
+  dfm2g::DevBuf<double> vcrs, vdia;
+  dfm2g::DevBuf<float> vcrs32, vdia32;
+  bool f32_valid = false;
+  unsigned pattern_version = 0;
+};
+
+struct dfm2g_ilu_s {
+  unsigned nblk = 0;
+  size_t nnz = 0;
+  bool has_pattern = false, has_factor = false, f32_valid = false;
+  int sweep_mode = DFM2G_SWEEP_SYNCFREE;
+  dfm2g::DevBuf<unsigned> row_start, col, dia_ind;
+  dfm2g::DevBuf<double> vcrs, vdia;
+  dfm2g::DevBuf<float> vcrs32, vdia32;
+  // level sets: level[i], order (rows by (level,row)), level_start (nlev+1)
+  dfm2g::DevBuf<unsigned> level_f, order_f, lstart_f, level_b, order_b, lstart_b;
+  unsigned nlev_f = 0, nlev_b = 0;
+  std::vector<unsigned> h_lstart_f, h_lstart_b;
+  // scratch for the sweeps (sentinel-filled outputs) and the device error word
+  dfm2g::DevBuf<double> tmp64a, tmp64b;
+  dfm2g::DevBuf<float> tmp32a, tmp32b;
+  dfm2g::DevBuf<int> err;
+  dfm2g::DevBuf<int> nsing;
+  int coop_blocks64 = 0, coop_blocks32 = 0, coop_blocks64b = 0, coop_blocks32b = 0;
+};
+
+struct dfm2g_tetmesh_s {
+  size_t np = 0, ntet = 0;
+  unsigned nblk = 0;
+  unsigned pattern_version = 0;
+  const dfm2g_bsr_s *bsr = nullptr;
+  dfm2g::DevBuf<double> xyz;
+  dfm2g::DevBuf<unsigned> tet;        // ntet*4, original order
+  dfm2g::DevBuf<unsigned> slot;       // ntet*16 slot ids (diagonal: 0xffffffff)
+  dfm2g::DevBuf<unsigned> by_color;   // tets sorted by colour (stable)
+  std::vector<unsigned> color_start;  // ncolor+1
+};
+
+namespace dfm2g {
+// cross-file internals
+int ilu_sweep(dfm2g_ilu_s *p, int prec, bool forward, const void *in, void *out);
+int ilu_sweep_guarded(dfm2g_ilu_s *p, int prec, bool forward, const void *in, void *out, const int *skip);
+int color_elements(const unsigned *elem, size_t nelem, unsigned nno, size_t np, std::vector<unsigned> &by_color,
+                   std::vector<unsigned> &color_start);
+void to_f32(size_t n, const double *in, float *out);
+int build_slot_map(const unsigned *d_elem, size_t nelem, unsigned nno, const dfm2g_bsr_s *m, unsigned *d_slot);
+int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta);
+int ilu_ensure_f32(dfm2g_ilu_s *p);
+int bsr_ensure_f32(dfm2g_bsr_s *m);
+}  // namespace dfm2g

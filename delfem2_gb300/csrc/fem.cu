@@ -1,0 +1,232 @@
+// Linear-tet elasticity on the device: colour-scheduled, atomic-free assembly
+// of K and b (per-tet Young's modulus) and the adjoint element term dL/dE.
+//
+// Layout: tet[4*ntet] node ids, slot[16*ntet] with slot[16e + 4a + b] the
+// val_crs_ slot of block (tet[e][a], tet[e][b]) (0xffffffff on the diagonal),
+// by_color = tets grouped by colour. Within one colour no two tets share a
+// node, so each thread (tet, node a) owns block row a of its tet exclusively.
+#include <cstring>
+
+#include "common.cuh"
+
+namespace dfm2g {
+
+constexpr unsigned kDiagSlot = 0xFFFFFFFFu;
+
+// Volume and barycentric-coordinate gradients of a tet (the quantities of
+// TetVolume3D / TetDlDx, include/delfem2/femutil.cpp:202-258): dN_k is the
+// normal of the face opposite vertex k, scaled by 1/(6 vol), pointing to k.
+__device__ __forceinline__ double tet_geometry(const double P[4][3], double dN[4][3]) {
+  const double ax = P[1][0] - P[0][0], ay = P[1][1] - P[0][1], az = P[1][2] - P[0][2];
+  const double bx = P[2][0] - P[0][0], by = P[2][1] - P[0][1], bz = P[2][2] - P[0][2];
+  const double cx = P[3][0] - P[0][0], cy = P[3][1] - P[0][1], cz = P[3][2] - P[0][2];
+  const double vol = (ax * (by * cz - cy * bz) - ay * (bx * cz - cx * bz) + az * (bx * cy - cx * by)) / 6.0;
+  const double inv6v = 1.0 / (6.0 * vol);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double *a = P[(k + 1) & 3], *b = P[(k + 2) & 3], *c = P[(k + 3) & 3];
+    const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+    const double wx = c[0] - a[0], wy = c[1] - a[1], wz = c[2] - a[2];
+    const double s = ((k & 1) ? 1.0 : -1.0) * inv6v;
+    dN[k][0] = s * (uy * wz - uz * wy);
+    dN[k][1] = s * (uz * wx - ux * wz);
+    dN[k][2] = s * (ux * wy - uy * wx);
+  }
+  return vol;
+}
+
+// One thread per (tet of this colour, local node a): block row a of K_e,
+// K_e[a][b][r][c] = vol (lambda dN_a[r] dN_b[c] + myu dN_b[r] dN_a[c]
+//                        + myu (dN_a . dN_b) delta_rc)
+// (AddEmat_LinearSolid3, include/delfem2/fem_solidlinear.cpp:55-79), added into
+// the diagonal block or the mapped slot; b_i += rho g vol/4 - sum_b K_ab u_b.
+__global__ void __launch_bounds__(128) k_tet_assemble(unsigned n, const unsigned *__restrict__ list,
+                                                      const unsigned *__restrict__ tet,
+                                                      const unsigned *__restrict__ slot,
+                                                      const double *__restrict__ xyz, const double *__restrict__ young,
+                                                      double nu, double rho, double gx, double gy, double gz,
+                                                      const double *__restrict__ disp, double *vcrs, double *vdia,
+                                                      double *rhs) {
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * 4u) return;
+  const unsigned e = list[t >> 2], a = t & 3u;
+  unsigned nd[4];
+  double P[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    nd[k] = tet[(size_t)e * 4 + k];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) P[k][d] = xyz[(size_t)nd[k] * 3 + d];
+  }
+  double dN[4][3];
+  const double vol = tet_geometry(P, dN);
+  const double E = young[e];
+  const double lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  const double myu = E / (2.0 * (1.0 + nu));
+  const unsigned i = nd[a];
+  double res[3] = {vol * rho * gx * 0.25, vol * rho * gy * 0.25, vol * rho * gz * 0.25};
+  double da[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) da[d] = (a == 0) ? dN[0][d] : (a == 1) ? dN[1][d] : (a == 2) ? dN[2][d] : dN[3][d];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const double dd = da[0] * dN[b][0] + da[1] * dN[b][1] + da[2] * dN[b][2];
+    double k[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        k[r * 3 + c] = vol * (lam * da[r] * dN[b][c] + myu * dN[b][r] * da[c] + (r == c ? myu * dd : 0.0));
+    if (disp) {
+      const double *u = disp + (size_t)nd[b] * 3;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) res[r] -= k[r * 3 + 0] * u[0] + k[r * 3 + 1] * u[1] + k[r * 3 + 2] * u[2];
+    }
+    const unsigned s = slot[(size_t)e * 16 + a * 4 + b];
+    double *dst = (s == kDiagSlot) ? vdia + (size_t)i * 9 : vcrs + (size_t)s * 9;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) dst[q] += k[q];
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r) rhs[(size_t)i * 3 + r] += res[r];
+}
+
+// dL/dE_e = -lam_e^T (K_e / E_e) u_e with G(v)[r][c] = sum_k v_k[r] dN_k[c]:
+// lam^T K_e u = vol (lambda1 tr(GL) tr(GU) + myu1 (tr(GL GU) + GL:GU)),
+// lambda1 = nu/((1+nu)(1-2nu)), myu1 = 1/(2(1+nu)) (the moduli at E = 1).
+__global__ void k_tet_dLdE(size_t ntet, const unsigned *__restrict__ tet, const double *__restrict__ xyz, double nu,
+                           const double *__restrict__ u, const double *__restrict__ lamv, double *__restrict__ out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ntet; e += (size_t)gridDim.x * blockDim.x) {
+    unsigned nd[4];
+    double P[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      nd[k] = tet[e * 4 + k];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) P[k][d] = xyz[(size_t)nd[k] * 3 + d];
+    }
+    double dN[4][3];
+    const double vol = tet_geometry(P, dN);
+    double GL[3][3] = {{0}}, GU[3][3] = {{0}};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double *lk = lamv + (size_t)nd[k] * 3, *uk = u + (size_t)nd[k] * 3;
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          GL[r][c] += lk[r] * dN[k][c];
+          GU[r][c] += uk[r] * dN[k][c];
+        }
+    }
+    const double lam1 = nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    const double myu1 = 1.0 / (2.0 * (1.0 + nu));
+    double tr_prod = 0.0, frob = 0.0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        tr_prod += GL[r][c] * GU[c][r];
+        frob += GL[r][c] * GU[r][c];
+      }
+    const double trL = GL[0][0] + GL[1][1] + GL[2][2], trU = GU[0][0] + GU[1][1] + GU[2][2];
+    out[e] = -vol * (lam1 * trL * trU + myu1 * (tr_prod + frob));
+  }
+}
+
+}  // namespace dfm2g
+
+using namespace dfm2g;
+
+extern "C" {
+
+int dfm2g_tetmesh_create(dfm2g_tetmesh *out, dfm2g_bsr m, const double *xyz, size_t np, const unsigned *tet,
+                         size_t ntet) {
+  if (!out) return fail(DFM2G_ERR_ARG, "tetmesh_create: null out");
+  if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "tetmesh_create: matrix has no pattern");
+  if (np != m->nblk) return fail(DFM2G_ERR_ARG, "tetmesh_create: np (%zu) != matrix blocks (%u)", np, m->nblk);
+  if ((ntet && !tet) || (np && !xyz)) return fail(DFM2G_ERR_ARG, "tetmesh_create: null mesh array");
+  if (ntet > 0xFFFFFFFFull / 16) return fail(DFM2G_ERR_ARG, "tetmesh_create: too many tets");
+  DFM2G_TRY(ensure_context());
+  auto *t = new dfm2g_tetmesh_s();
+  t->np = np;
+  t->ntet = ntet;
+  t->nblk = m->nblk;
+  t->bsr = m;
+  t->pattern_version = m->pattern_version;
+  std::vector<unsigned> by_color;
+  int s = color_elements(tet, ntet, 4, np, by_color, t->color_start);
+  if (s == DFM2G_OK) s = t->xyz.resize(np * 3 + 1);
+  if (s == DFM2G_OK) s = t->tet.resize(ntet * 4 + 1);
+  if (s == DFM2G_OK) s = t->slot.resize(ntet * 16 + 1);
+  if (s == DFM2G_OK) s = t->by_color.resize(ntet + 1);
+  if (s == DFM2G_OK && np &&
+      cudaMemcpyAsync(t->xyz.p, xyz, sizeof(double) * np * 3, cudaMemcpyHostToDevice, stream()) != cudaSuccess)
+    s = fail(DFM2G_ERR_CUDA, "tetmesh_create: copy xyz");
+  if (s == DFM2G_OK && ntet &&
+      (cudaMemcpyAsync(t->tet.p, tet, sizeof(unsigned) * ntet * 4, cudaMemcpyHostToDevice, stream()) != cudaSuccess ||
+       cudaMemcpyAsync(t->by_color.p, by_color.data(), sizeof(unsigned) * ntet, cudaMemcpyHostToDevice, stream()) !=
+           cudaSuccess))
+    s = fail(DFM2G_ERR_CUDA, "tetmesh_create: copy tets");
+  if (s == DFM2G_OK) s = build_slot_map(t->tet.p, ntet, 4, m, t->slot.p);
+  if (s != DFM2G_OK) {
+    delete t;
+    return s;
+  }
+  *out = t;
+  return DFM2G_OK;
+}
+
+int dfm2g_tetmesh_destroy(dfm2g_tetmesh t) {
+  if (t) {
+    cudaStreamSynchronize(stream());
+    delete t;
+  }
+  return DFM2G_OK;
+}
+
+int dfm2g_tetmesh_info(dfm2g_tetmesh t, unsigned *ncolor, size_t *ntet) {
+  if (!t) return fail(DFM2G_ERR_ARG, "null tetmesh");
+  if (ncolor) *ncolor = t->color_start.empty() ? 0 : (unsigned)t->color_start.size() - 1;
+  if (ntet) *ntet = t->ntet;
+  return DFM2G_OK;
+}
+
+int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const double *young, double nu, double rho,
+                                  const double *g, const double *disp, double *b, int mem) {
+  if (!t || !m) return fail(DFM2G_ERR_ARG, "assemble: null handle");
+  if (m != t->bsr || m->pattern_version != t->pattern_version)
+    return fail(DFM2G_ERR_STATE, "assemble: matrix pattern differs from the one the mesh was mapped to");
+  if (!young || !g || !b) return fail(DFM2G_ERR_ARG, "assemble: null argument");
+  VecArg<double> ay, ad, ab;
+  DFM2G_TRY(ay.in(young, t->ntet, mem, true));
+  if (disp) DFM2G_TRY(ad.in(disp, t->np * 3, mem, true));
+  DFM2G_TRY(ab.in(b, t->np * 3, mem, true));
+  for (size_t c = 0; c + 1 < t->color_start.size(); ++c) {
+    const unsigned n = t->color_start[c + 1] - t->color_start[c];
+    k_tet_assemble<<<blocks_for((size_t)n * 4, 128), 128, 0, stream()>>>(
+        n, t->by_color.p + t->color_start[c], t->tet.p, t->slot.p, t->xyz.p, ay.dev(), nu, rho, g[0], g[1], g[2],
+        disp ? ad.dev() : nullptr, m->vcrs.p, m->vdia.p, ab.dev());
+  }
+  DFM2G_LAUNCH_CHECK();
+  m->f32_valid = false;
+  return ab.copy_back();
+}
+
+int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu, const double *u, const double *lam,
+                       double *dLdE, int mem) {
+  if (!t) return fail(DFM2G_ERR_ARG, "dLdE: null handle");
+  (void)young;
+  if (!u || !lam || !dLdE) return fail(DFM2G_ERR_ARG, "dLdE: null argument");
+  VecArg<double> au, al, ao;
+  DFM2G_TRY(au.in(u, t->np * 3, mem, true));
+  DFM2G_TRY(al.in(lam, t->np * 3, mem, true));
+  DFM2G_TRY(ao.in(dLdE, t->ntet, mem, false));
+  if (t->ntet)
+    k_tet_dLdE<<<blocks_for(t->ntet, 128, ctx().num_sms * 32), 128, 0, stream()>>>(t->ntet, t->tet.p, t->xyz.p, nu,
+                                                                                  au.dev(), al.dev(), ao.dev());
+  DFM2G_LAUNCH_CHECK();
+  return ao.copy_back();
+}
+
+}  // extern "C"

@@ -1,0 +1,761 @@
+// CPreconditionerILU<double> for 3x3 blocks on the device: SetPattern0,
+// CopyValue, level-scheduled Decompose, and the forward/backward sweeps.
+//
+// Level sets. Forward level: 0 for a row with no column j < i, else
+// 1 + max over its columns j < i; backward: the same over columns j > i. Rows of
+// one level are independent in the sweep (and in the factorisation, which has
+// the forward dependency structure). `order` lists rows by (level, row id);
+// `level_start[l]` is the first position of level l. Everything is computed on
+// the device (iterative level assignment + a stable LSD radix sort) and is
+// bit-exact against a serial CPU recomputation.
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace dfm2g {
+
+// ---------------------------------------------------------------------------
+// SetPattern0: sort each row's columns ascending (thread per row, insertion
+// sort - rows hold a handful of entries) and find dia_ind = first col > i.
+__global__ void k_sort_rows_diaind(unsigned nblk, const unsigned *__restrict__ row_start, unsigned *col,
+                                   unsigned *__restrict__ dia_ind) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
+    const unsigned s0 = row_start[i], s1 = row_start[i + 1];
+    for (unsigned a = s0 + 1; a < s1; ++a) {
+      const unsigned v = col[a];
+      unsigned b = a;
+      while (b > s0 && col[b - 1] > v) {
+        col[b] = col[b - 1];
+        --b;
+      }
+      col[b] = v;
+    }
+    unsigned d = s1;
+    for (unsigned s = s0; s < s1; ++s)
+      if (col[s] > i) {
+        d = s;
+        break;
+      }
+    dia_ind[i] = d;
+  }
+}
+
+// One relaxation sweep of the level assignment. A row gets its level once all
+// of its dependencies have one; a level, once written, is final, so reading a
+// stale "unassigned" only postpones the row to a later sweep.
+__global__ void k_level_sweep(unsigned nblk, const unsigned *__restrict__ row_start,
+                              const unsigned *__restrict__ col, const unsigned *__restrict__ dia_ind,
+                              int backward, int *level, unsigned *n_assigned, unsigned *max_level) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned t0 = blockIdx.x * blockDim.x; t0 < nblk; t0 += stride) {
+    const unsigned t = t0 + threadIdx.x;
+    bool newly = false;
+    int lv = 0;
+    if (t < nblk) {
+      const unsigned i = backward ? nblk - 1 - t : t;
+      if (level[i] < 0) {
+        const unsigned s0 = backward ? dia_ind[i] : row_start[i];
+        const unsigned s1 = backward ? row_start[i + 1] : dia_ind[i];
+        bool ready = true;
+        for (unsigned s = s0; s < s1; ++s) {
+          const int lj = ld_relaxed(level + col[s]);
+          if (lj < 0) {
+            ready = false;
+            break;
+          }
+          lv = max(lv, lj + 1);
+        }
+        if (ready) {
+          level[i] = lv;
+          newly = true;
+        }
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, newly);
+    if (newly) atomicMax(max_level, (unsigned)lv);
+    if (lane == 0 && bal) atomicAdd(n_assigned, (unsigned)__popc(bal));
+  }
+}
+
+// ---- stable LSD radix sort of (key, value) pairs, 8-bit digits ----------------
+constexpr int kRsThreads = 256;
+constexpr int kRsRounds = 8;
+constexpr int kRsTile = kRsThreads * kRsRounds;
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_hist(unsigned n, const unsigned *__restrict__ keys, int shift,
+                                                        unsigned *__restrict__ counts, unsigned ntiles) {
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kRsTile;
+  for (int r = 0; r < kRsRounds; ++r) {
+    const size_t idx = base + (size_t)r * kRsThreads + threadIdx.x;
+    if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  counts[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// In-place exclusive scan of a[0..n) by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_exclusive(unsigned *a, size_t n) {
+  __shared__ unsigned warp_tot[32];
+  __shared__ unsigned carry;
+  const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (size_t base = 0; base < n; base += blockDim.x) {
+    const size_t i = base + threadIdx.x;
+    const unsigned v = i < n ? a[i] : 0u;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (unsigned)o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      unsigned tw = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, tw, o);
+        if (lane >= (unsigned)o) tw += y;
+      }
+      warp_tot[lane] = tw;
+    }
+    __syncthreads();
+    const unsigned excl = (w ? warp_tot[w - 1] : 0u) + x - v;
+    const unsigned c = carry;
+    if (i < n) a[i] = c + excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = c + excl + v;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kRsThreads) k_rs_scatter(unsigned n, const unsigned *__restrict__ kin,
+                                                           const unsigned *__restrict__ vin,
+                                                           unsigned *__restrict__ kout, unsigned *__restrict__ vout,
+                                                           int shift, const unsigned *__restrict__ offsets,
+                                                           unsigned ntiles) {
+  __shared__ unsigned run[256];
+  __shared__ unsigned wc[kRsThreads / 32][256];
+  const unsigned tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  run[tid] = offsets[(size_t)tid * ntiles + blockIdx.x];
+  const size_t base = (size_t)blockIdx.x * kRsTile;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kRsRounds; ++r) {
+    for (unsigned k = tid; k < (kRsThreads / 32) * 256; k += kRsThreads) (&wc[0][0])[k] = 0;
+    __syncthreads();
+    const size_t idx = base + (size_t)r * kRsThreads + tid;
+    const bool ok = idx < n;
+    const unsigned key = ok ? kin[idx] : 0u, val = ok ? vin[idx] : 0u;
+    const unsigned d = (key >> shift) & 255u;
+    const unsigned tag = ok ? d : 0x10000u + lane;  // invalid lanes match nobody
+    const unsigned peers = __match_any_sync(0xffffffffu, tag);
+    const unsigned rank = __popc(peers & lt_mask);
+    if (ok && rank == 0) wc[w][d] = __popc(peers);
+    __syncthreads();
+    {
+      unsigned acc = run[tid];
+#pragma unroll
+      for (int q = 0; q < kRsThreads / 32; ++q) {
+        const unsigned c = wc[q][tid];
+        wc[q][tid] = acc;
+        acc += c;
+      }
+      run[tid] = acc;
+    }
+    __syncthreads();
+    if (ok) {
+      const unsigned pos = wc[w][d] + rank;
+      kout[pos] = key;
+      vout[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_iota(unsigned n, unsigned *a) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = i;
+}
+
+__global__ void k_level_start(unsigned n, const unsigned *__restrict__ sorted_level, unsigned nlev,
+                              unsigned *__restrict__ lstart) {
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned lq = sorted_level[q];
+    const unsigned lp = q ? sorted_level[q - 1] : 0xFFFFFFFFu;
+    if (lq != lp)
+      for (unsigned l = lp + 1; l <= lq; ++l) lstart[l] = q;  // lp+1 wraps to 0 for q == 0
+    if (q == n - 1) lstart[nlev] = n;
+  }
+}
+
+// Sort rows by level (stable): returns order (values) in `order`.
+static int radix_sort_levels(unsigned n, const unsigned *level, unsigned max_key, unsigned *order,
+                             DevBuf<unsigned> &scratch_sorted_keys) {
+  const unsigned ntiles = (n + kRsTile - 1) / kRsTile;
+  DevBuf<unsigned> k0, k1, v0, v1, counts;
+  DFM2G_TRY(k0.resize(n));
+  DFM2G_TRY(k1.resize(n));
+  DFM2G_TRY(v0.resize(n));
+  DFM2G_TRY(v1.resize(n));
+  DFM2G_TRY(counts.resize((size_t)256 * ntiles));
+  DFM2G_CUDA(cudaMemcpyAsync(k0.p, level, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, stream()));
+  k_iota<<<blocks_for(n, 256, ctx().num_sms * 8), 256, 0, stream()>>>(n, v0.p);
+  unsigned *ka = k0.p, *kb = k1.p, *va = v0.p, *vb = v1.p;
+  int shift = 0;
+  do {
+    k_rs_hist<<<ntiles, kRsThreads, 0, stream()>>>(n, ka, shift, counts.p, ntiles);
+    k_scan_exclusive<<<1, 1024, 0, stream()>>>(counts.p, (size_t)256 * ntiles);
+    k_rs_scatter<<<ntiles, kRsThreads, 0, stream()>>>(n, ka, va, kb, vb, shift, counts.p, ntiles);
+    DFM2G_LAUNCH_CHECK();
+    std::swap(ka, kb);
+    std::swap(va, vb);
+    shift += 8;
+  } while (shift < 32 && (max_key >> shift) != 0);
+  DFM2G_CUDA(cudaMemcpyAsync(order, va, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, stream()));
+  DFM2G_TRY(scratch_sorted_keys.resize(n));
+  DFM2G_CUDA(cudaMemcpyAsync(scratch_sorted_keys.p, ka, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+static int compute_levels(dfm2g_ilu_s *p, bool backward) {
+  const unsigned n = p->nblk;
+  DevBuf<unsigned> &level = backward ? p->level_b : p->level_f;
+  DevBuf<unsigned> &order = backward ? p->order_b : p->order_f;
+  DevBuf<unsigned> &lstart = backward ? p->lstart_b : p->lstart_f;
+  DFM2G_TRY(level.resize(n));
+  DFM2G_TRY(order.resize(n));
+  DevBuf<unsigned> counters;  // [0] assigned, [1] max level
+  DFM2G_TRY(counters.resize(2));
+  DFM2G_CUDA(cudaMemsetAsync(level.p, 0xFF, sizeof(unsigned) * n, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(counters.p, 0, sizeof(unsigned) * 2, stream()));
+  unsigned h[2] = {0, 0};
+  unsigned sweeps = 0;
+  const unsigned blocks = blocks_for(n, 256, ctx().num_sms * 8);
+  while (h[0] < n) {
+    const unsigned before = h[0];
+    for (int k = 0; k < 8; ++k)
+      k_level_sweep<<<blocks, 256, 0, stream()>>>(n, p->row_start.p, p->col.p, p->dia_ind.p, backward ? 1 : 0,
+                                                  (int *)level.p, counters.p, counters.p + 1);
+    DFM2G_LAUNCH_CHECK();
+    DFM2G_CUDA(cudaMemcpyAsync(h, counters.p, sizeof(h), cudaMemcpyDeviceToHost, stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+    sweeps += 8;
+    if (h[0] == before || sweeps > n + 16)
+      return fail(DFM2G_ERR_PATTERN, "level sets: no progress (cyclic dependency?)");
+  }
+  const unsigned nlev = n ? h[1] + 1 : 0;
+  DFM2G_TRY(lstart.resize(nlev + 1));
+  std::vector<unsigned> &hl = backward ? p->h_lstart_b : p->h_lstart_f;
+  if (n) {
+    DevBuf<unsigned> sorted_keys;
+    DFM2G_TRY(radix_sort_levels(n, level.p, h[1], order.p, sorted_keys));
+    k_level_start<<<blocks_for(n, 256, ctx().num_sms * 8), 256, 0, stream()>>>(n, sorted_keys.p, nlev, lstart.p);
+    DFM2G_LAUNCH_CHECK();
+    hl.resize(nlev + 1);
+    DFM2G_CUDA(cudaMemcpyAsync(hl.data(), lstart.p, sizeof(unsigned) * (nlev + 1), cudaMemcpyDeviceToHost,
+                               stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  } else {
+    hl.assign(1, 0);
+  }
+  (backward ? p->nlev_b : p->nlev_f) = nlev;
+  return DFM2G_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CopyValue: every matrix block goes to the ILU slot of the same column (binary
+// search in the sorted ILU row); blocks without a slot are dropped.
+__global__ void k_ilu_copy(unsigned nblk, const unsigned *__restrict__ m_row_start,
+                           const unsigned *__restrict__ m_col, const double *__restrict__ m_vcrs,
+                           const unsigned *__restrict__ p_row_start, const unsigned *__restrict__ p_col,
+                           double *__restrict__ p_vcrs) {
+  const unsigned lane = threadIdx.x & 31, nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nblk; i += nwarp) {
+    const unsigned q0 = p_row_start[i], q1 = p_row_start[i + 1];
+    for (unsigned s = m_row_start[i] + lane; s < m_row_start[i + 1]; s += 32) {
+      const unsigned j = m_col[s];
+      unsigned lo = q0, hi = q1;
+      while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (p_col[mid] < j) lo = mid + 1; else hi = mid;
+      }
+      if (lo < q1 && p_col[lo] == j) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) p_vcrs[(size_t)lo * 9 + k] = m_vcrs[(size_t)s * 9 + k];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Decompose, one level at a time, one warp per row. For each k < i of row i
+// (ascending, sequential): A_ik is read fresh (earlier k's may have updated
+// it), and the lanes split the (j in U(k)) x (3x3 entry) updates
+// A_ij -= A_ik A_kj, each touching a distinct entry. Then D_i is inverted by
+// the cofactor formula (|det| <= 1e-30 counts a singular pivot and leaves it),
+// then U_ij <- D_i^-1 U_ij (one lane per block).
+__global__ void __launch_bounds__(256) k_ilu_factor_level(const unsigned *__restrict__ rows, unsigned nrows,
+                                                          const unsigned *__restrict__ row_start,
+                                                          const unsigned *__restrict__ col,
+                                                          const unsigned *__restrict__ dia_ind, double *vcrs,
+                                                          double *vdia, int *nsing) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nrows) return;
+  const unsigned i = rows[w];
+  const unsigned s0 = row_start[i], s1 = row_start[i + 1], sd = dia_ind[i];
+  for (unsigned sk = s0; sk < sd; ++sk) {
+    const unsigned k = col[sk];
+    double aik[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) aik[q] = vcrs[(size_t)sk * 9 + q];
+    const unsigned u0 = dia_ind[k], u1 = row_start[k + 1];
+    const unsigned ntask = (u1 - u0) * 9;
+    for (unsigned t = lane; t < ntask; t += 32) {
+      const unsigned uu = t / 9u, e = t - uu * 9u, r = e / 3u, c = e - r * 3u;
+      const unsigned sj = u0 + uu;
+      const unsigned j = col[sj];
+      double *dst;
+      if (j == i) {
+        dst = vdia + (size_t)i * 9;
+      } else {
+        unsigned lo = s0, hi = s1;
+        while (lo < hi) {
+          const unsigned mid = (lo + hi) >> 1;
+          if (col[mid] < j) lo = mid + 1; else hi = mid;
+        }
+        if (lo >= s1 || col[lo] != j) continue;
+        dst = vcrs + (size_t)lo * 9;
+      }
+      const double *akj = vcrs + (size_t)sj * 9;
+      dst[e] -= aik[r * 3 + 0] * akj[0 * 3 + c] + aik[r * 3 + 1] * akj[1 * 3 + c] + aik[r * 3 + 2] * akj[2 * 3 + c];
+    }
+    __syncwarp();
+  }
+  double d[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) d[q] = vdia[(size_t)i * 9 + q];
+  const double det = d[0] * (d[4] * d[8] - d[5] * d[7]) - d[1] * (d[3] * d[8] - d[5] * d[6]) +
+                     d[2] * (d[3] * d[7] - d[4] * d[6]);
+  double v[9];
+  if (fabs(det) > 1.0e-30) {
+    const double s = 1.0 / det;
+    v[0] = s * (d[4] * d[8] - d[5] * d[7]);
+    v[1] = s * (d[2] * d[7] - d[1] * d[8]);
+    v[2] = s * (d[1] * d[5] - d[2] * d[4]);
+    v[3] = s * (d[5] * d[6] - d[3] * d[8]);
+    v[4] = s * (d[0] * d[8] - d[2] * d[6]);
+    v[5] = s * (d[2] * d[3] - d[0] * d[5]);
+    v[6] = s * (d[3] * d[7] - d[4] * d[6]);
+    v[7] = s * (d[1] * d[6] - d[0] * d[7]);
+    v[8] = s * (d[0] * d[4] - d[1] * d[3]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) v[q] = d[q];
+    if (lane == 0) atomicAdd(nsing, 1);
+  }
+  __syncwarp();
+  if (lane < 9) vdia[(size_t)i * 9 + lane] = v[lane];
+  for (unsigned s = sd + lane; s < s1; s += 32) {
+    double *u = vcrs + (size_t)s * 9;
+    double t[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) t[q] = u[q];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        u[r * 3 + c] = v[r * 3 + 0] * t[0 * 3 + c] + v[r * 3 + 1] * t[1 * 3 + c] + v[r * 3 + 2] * t[2 * 3 + c];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sweeps. Forward: out_i = D_i^-1 (in_i - sum_{j<i} L_ij out_j). Backward:
+// out_i = in_i - sum_{j>i} U'_ij out_j. One warp per row; the row's run of
+// 9*(#blocks) scalars is read coalesced, as in the SpMV.
+template <typename T, bool FWD>
+__device__ __forceinline__ void sweep_row(unsigned i, unsigned lane, const unsigned *__restrict__ row_start,
+                                          const unsigned *__restrict__ col, const unsigned *__restrict__ dia_ind,
+                                          const T *__restrict__ vcrs, const T *__restrict__ vdia, const T *in, T *out,
+                                          bool wait, int *err, unsigned long long timeout_ns) {
+  const unsigned s0 = FWD ? row_start[i] : dia_ind[i];
+  const unsigned s1 = FWD ? dia_ind[i] : row_start[i + 1];
+  T a0 = 0, a1 = 0, a2 = 0;
+  for (unsigned cb = s0; cb < s1; cb += 32) {
+    const unsigned nb = min(32u, s1 - cb);
+    const unsigned my_col = lane < nb ? col[cb + lane] : 0u;
+    const size_t e_begin = (size_t)cb * 9, e_end = e_begin + (size_t)nb * 9;
+    for (size_t base = e_begin; base < e_end; base += 32) {
+      const size_t e = base + lane;
+      const bool ok = e < e_end;
+      const unsigned loc = ok ? (unsigned)(e - e_begin) : 0u;
+      const unsigned b = loc / 9u, rem = loc - b * 9u, r = rem / 3u, c = rem - r * 3u;
+      const unsigned j = __shfl_sync(0xffffffffu, my_col, b);
+      if (ok) {
+        const T a = vcrs[e];
+        T xv;
+        if (wait) {
+          const T *px = out + (size_t)j * 3 + c;
+          xv = ld_relaxed(px);
+          if (is_pending(xv)) {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned spins = 0;
+            while (is_pending(xv = ld_relaxed(px))) {
+              if ((++spins & 15u) == 0 &&
+                  (ld_relaxed(err) != 0 || globaltimer_ns() - t0 > timeout_ns)) {
+                atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
+                xv = T(0);
+                break;
+              }
+            }
+          }
+        } else {
+          xv = out[(size_t)j * 3 + c];
+        }
+        const T v = a * xv;
+        a0 += (r == 0) ? v : T(0);
+        a1 += (r == 1) ? v : T(0);
+        a2 += (r == 2) ? v : T(0);
+      }
+    }
+  }
+  a0 = warp_sum(a0);
+  a1 = warp_sum(a1);
+  a2 = warp_sum(a2);
+  if (lane < 3) {
+    const T t0 = in[(size_t)i * 3 + 0] - a0;
+    const T t1 = in[(size_t)i * 3 + 1] - a1;
+    const T t2 = in[(size_t)i * 3 + 2] - a2;
+    T z;
+    if (FWD) {
+      const T *d = vdia + (size_t)i * 9 + lane * 3;
+      z = d[0] * t0 + d[1] * t1 + d[2] * t2;
+    } else {
+      z = lane == 0 ? t0 : (lane == 1 ? t1 : t2);
+    }
+    if (wait) st_relaxed(out + (size_t)i * 3 + lane, z);
+    else out[(size_t)i * 3 + lane] = z;
+  }
+}
+
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(256) k_sweep_level(const unsigned *__restrict__ rows, unsigned nrows,
+                                                     const unsigned *__restrict__ row_start,
+                                                     const unsigned *__restrict__ col,
+                                                     const unsigned *__restrict__ dia_ind, const T *__restrict__ vcrs,
+                                                     const T *__restrict__ vdia, const T *in, T *out,
+                                                     const int *skip) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nrows || (skip && *skip)) return;
+  sweep_row<T, FWD>(rows[w], lane, row_start, col, dia_ind, vcrs, vdia, in, out, false, nullptr, 0);
+}
+
+// Sync-free sweep: one persistent, co-resident (cooperative) grid; warp w
+// takes positions w, w+W, ... of the level order, and waits (bounded) on each
+// needed out_j until it is no longer the pending marker. Every row depends only
+// on rows earlier in the order and each warp walks its positions in order, so
+// the earliest unfinished position can always proceed.
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(256) k_sweep_syncfree(unsigned nblk, const unsigned *__restrict__ order,
+                                                        const unsigned *__restrict__ row_start,
+                                                        const unsigned *__restrict__ col,
+                                                        const unsigned *__restrict__ dia_ind,
+                                                        const T *__restrict__ vcrs, const T *__restrict__ vdia,
+                                                        const T *in, T *out, int *err,
+                                                        unsigned long long timeout_ns, const int *skip) {
+  if (skip && *skip) return;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nblk; q += nwarp)
+    sweep_row<T, FWD>(order[q], lane, row_start, col, dia_ind, vcrs, vdia, in, out, true, err, timeout_ns);
+}
+
+template <typename T>
+__global__ void k_copy_guarded(size_t n, const T *__restrict__ in, T *__restrict__ out, const int *skip) {
+  if (skip && *skip) return;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
+template <typename T>
+static int coop_blocks(const void *kernel, int *cache) {
+  if (*cache > 0) return DFM2G_OK;
+  int per_sm = 0;
+  DFM2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+  if (per_sm <= 0) return fail(DFM2G_ERR_CUDA, "sweep kernel cannot be resident");
+  *cache = per_sm * ctx().num_sms;
+  return DFM2G_OK;
+}
+
+template <typename T>
+static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia,
+                      const int *skip, bool prefilled) {
+  const unsigned n = p->nblk;
+  if (n == 0) return DFM2G_OK;
+  if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
+    // levels in order; rows of one level are independent (in == out allowed)
+    if (in != out) {
+      k_copy_guarded<T><<<blocks_for((size_t)n * 3, 256, ctx().num_sms * 4), 256, 0, stream()>>>((size_t)n * 3, in,
+                                                                                                 out, skip);
+      DFM2G_LAUNCH_CHECK();
+    }
+    const std::vector<unsigned> &ls = forward ? p->h_lstart_f : p->h_lstart_b;
+    const unsigned *order = forward ? p->order_f.p : p->order_b.p;
+    for (size_t l = 0; l + 1 < ls.size(); ++l) {
+      const unsigned nrows = ls[l + 1] - ls[l];
+      const unsigned blocks = blocks_for((size_t)nrows * 32, 256);
+      if (forward)
+        k_sweep_level<T, true><<<blocks, 256, 0, stream()>>>(order + ls[l], nrows, p->row_start.p, p->col.p,
+                                                            p->dia_ind.p, vcrs, vdia, out, out, skip);
+      else
+        k_sweep_level<T, false><<<blocks, 256, 0, stream()>>>(order + ls[l], nrows, p->row_start.p, p->col.p,
+                                                             p->dia_ind.p, vcrs, vdia, out, out, skip);
+    }
+    note_launches((unsigned)(ls.size() - 1) + (in != out ? 1u : 0u));
+    DFM2G_LAUNCH_CHECK();
+    return DFM2G_OK;
+  }
+  // sync-free: `out` must differ from `in`; it is filled with the pending marker
+  if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
+  if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
+  void *kernel = forward ? (void *)k_sweep_syncfree<T, true> : (void *)k_sweep_syncfree<T, false>;
+  int *cache = sizeof(T) == 8 ? (forward ? &p->coop_blocks64 : &p->coop_blocks64b)
+                              : (forward ? &p->coop_blocks32 : &p->coop_blocks32b);
+  DFM2G_TRY(coop_blocks<T>(kernel, cache));
+  const unsigned want = blocks_for((size_t)n * 32, 256);
+  const unsigned blocks = std::min<unsigned>(want, (unsigned)*cache);
+  const unsigned *order = forward ? p->order_f.p : p->order_b.p;
+  const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+  unsigned long long timeout = kWaitTimeoutNs + 20000ull * nlev;
+  int *err = p->err.p;
+  void *args[] = {(void *)&n, (void *)&order, (void *)&p->row_start.p, (void *)&p->col.p, (void *)&p->dia_ind.p,
+                  (void *)&vcrs, (void *)&vdia, (void *)&in, (void *)&out, (void *)&err, (void *)&timeout, (void *)&skip};
+  DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(256), args, 0, stream()));
+  note_launches(1);
+  return DFM2G_OK;
+}
+
+int ilu_sweep(dfm2g_ilu_s *p, int prec, bool forward, const void *in, void *out) {
+  if (prec == DFM2G_F64)
+    return sweep_impl<double>(p, forward, (const double *)in, (double *)out, p->vcrs.p, p->vdia.p, nullptr, false);
+  DFM2G_TRY(ilu_ensure_f32(p));
+  return sweep_impl<float>(p, forward, (const float *)in, (float *)out, p->vcrs32.p, p->vdia32.p, nullptr, false);
+}
+
+// Variant for the solver loops: the sweep is skipped once *skip != 0, and in
+// sync-free mode `out` must already hold the pending marker.
+int ilu_sweep_guarded(dfm2g_ilu_s *p, int prec, bool forward, const void *in, void *out, const int *skip) {
+  if (prec == DFM2G_F64)
+    return sweep_impl<double>(p, forward, (const double *)in, (double *)out, p->vcrs.p, p->vdia.p, skip, true);
+  return sweep_impl<float>(p, forward, (const float *)in, (float *)out, p->vcrs32.p, p->vdia32.p, skip, true);
+}
+
+int ilu_ensure_f32(dfm2g_ilu_s *p) {
+  if (p->f32_valid) return DFM2G_OK;
+  if (!p->has_factor) return fail(DFM2G_ERR_STATE, "ILU not decomposed");
+  DFM2G_TRY(p->vcrs32.ensure(p->nnz * 9 + 1));
+  DFM2G_TRY(p->vdia32.ensure((size_t)p->nblk * 9 + 1));
+  to_f32(p->nnz * 9, p->vcrs.p, p->vcrs32.p);
+  to_f32((size_t)p->nblk * 9, p->vdia.p, p->vdia32.p);
+  DFM2G_LAUNCH_CHECK();
+  p->f32_valid = true;
+  return DFM2G_OK;
+}
+
+static int read_err(dfm2g_ilu_s *p) {
+  int h = 0;
+  DFM2G_CUDA(cudaMemcpyAsync(&h, p->err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (h != 0) {
+    DFM2G_CUDA(cudaMemsetAsync(p->err.p, 0, sizeof(int), stream()));
+    return fail(h, "ILU sweep: device-side wait timed out");
+  }
+  return DFM2G_OK;
+}
+
+}  // namespace dfm2g
+
+using namespace dfm2g;
+
+static int check_ilu(dfm2g_ilu p, bool pattern, bool factor) {
+  if (!p) return fail(DFM2G_ERR_ARG, "null ILU handle");
+  if (pattern && !p->has_pattern) return fail(DFM2G_ERR_STATE, "ILU has no pattern (call set_pattern0)");
+  if (factor && !p->has_factor) return fail(DFM2G_ERR_STATE, "ILU not decomposed (call decompose)");
+  return DFM2G_OK;
+}
+
+extern "C" {
+
+int dfm2g_ilu_create(dfm2g_ilu *out) {
+  if (!out) return fail(DFM2G_ERR_ARG, "ilu_create: null out");
+  DFM2G_TRY(ensure_context());
+  auto *p = new dfm2g_ilu_s();
+  DFM2G_TRY(p->err.resize(1));
+  DFM2G_TRY(p->nsing.resize(1));
+  DFM2G_CUDA(cudaMemsetAsync(p->err.p, 0, sizeof(int), stream()));
+  *out = p;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_destroy(dfm2g_ilu p) {
+  if (p) {
+    cudaStreamSynchronize(stream());
+    delete p;
+  }
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
+  DFM2G_TRY(check_ilu(p, false, false));
+  if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "set_pattern0: matrix has no pattern");
+  const unsigned n = m->nblk;
+  p->nblk = n;
+  p->nnz = m->nnz;
+  DFM2G_TRY(p->row_start.resize(n + 1));
+  DFM2G_TRY(p->col.resize(m->nnz + 1));
+  DFM2G_TRY(p->dia_ind.resize(n + 1));
+  DFM2G_TRY(p->vcrs.resize(m->nnz * 9 + 1));
+  DFM2G_TRY(p->vdia.resize((size_t)n * 9 + 1));
+  DFM2G_CUDA(cudaMemcpyAsync(p->row_start.p, m->row_start.p, sizeof(unsigned) * (n + 1), cudaMemcpyDeviceToDevice,
+                             stream()));
+  if (m->nnz)
+    DFM2G_CUDA(cudaMemcpyAsync(p->col.p, m->col.p, sizeof(unsigned) * m->nnz, cudaMemcpyDeviceToDevice, stream()));
+  if (n) {
+    k_sort_rows_diaind<<<blocks_for(n, 128, ctx().num_sms * 16), 128, 0, stream()>>>(n, p->row_start.p, p->col.p,
+                                                                                    p->dia_ind.p);
+    DFM2G_LAUNCH_CHECK();
+  }
+  DFM2G_TRY(compute_levels(p, false));
+  DFM2G_TRY(compute_levels(p, true));
+  const size_t nvec = (size_t)n * 3 + 1;
+  DFM2G_TRY(p->tmp64a.resize(nvec));
+  DFM2G_TRY(p->tmp64b.resize(nvec));
+  DFM2G_TRY(p->tmp32a.resize(nvec));
+  DFM2G_TRY(p->tmp32b.resize(nvec));
+  p->has_pattern = true;
+  p->has_factor = false;
+  p->f32_valid = false;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  if (!m || !m->has_pattern || m->nblk != p->nblk) return fail(DFM2G_ERR_ARG, "copy_value: matrix size mismatch");
+  DFM2G_CUDA(cudaMemsetAsync(p->vcrs.p, 0, sizeof(double) * p->nnz * 9, stream()));
+  if (p->nblk) {
+    k_ilu_copy<<<blocks_for((size_t)p->nblk * 32, 256, ctx().num_sms * 16), 256, 0, stream()>>>(
+        p->nblk, m->row_start.p, m->col.p, m->vcrs.p, p->row_start.p, p->col.p, p->vcrs.p);
+    DFM2G_LAUNCH_CHECK();
+    DFM2G_CUDA(cudaMemcpyAsync(p->vdia.p, m->vdia.p, sizeof(double) * 9 * p->nblk, cudaMemcpyDeviceToDevice,
+                               stream()));
+  }
+  p->has_factor = false;
+  p->f32_valid = false;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  DFM2G_CUDA(cudaMemsetAsync(p->nsing.p, 0, sizeof(int), stream()));
+  const std::vector<unsigned> &ls = p->h_lstart_f;
+  for (size_t l = 0; l + 1 < ls.size(); ++l) {
+    const unsigned nrows = ls[l + 1] - ls[l];
+    k_ilu_factor_level<<<blocks_for((size_t)nrows * 32, 256), 256, 0, stream()>>>(
+        p->order_f.p + ls[l], nrows, p->row_start.p, p->col.p, p->dia_ind.p, p->vcrs.p, p->vdia.p, p->nsing.p);
+  }
+  DFM2G_LAUNCH_CHECK();
+  int ns = 0;
+  DFM2G_CUDA(cudaMemcpyAsync(&ns, p->nsing.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (n_singular) *n_singular = ns;
+  p->has_factor = true;
+  p->f32_valid = false;
+  if (ns > 10) return fail(DFM2G_ERR_SINGULAR_PIVOT, "ILU: %d pivots with |det| <= 1e-30", ns);
+  return DFM2G_OK;
+}
+
+static int precond_host(dfm2g_ilu p, int prec, void *vec, int mem, int which /*1 fwd, 2 bwd, 3 both*/) {
+  DFM2G_TRY(check_ilu(p, true, true));
+  if (!vec) return fail(DFM2G_ERR_ARG, "null vector");
+  if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "prec must be F64 or F32");
+  const size_t n = (size_t)p->nblk * 3;
+  const size_t es = prec == DFM2G_F64 ? 8 : 4;
+  void *a = prec == DFM2G_F64 ? (void *)p->tmp64a.p : (void *)p->tmp32a.p;
+  void *b = prec == DFM2G_F64 ? (void *)p->tmp64b.p : (void *)p->tmp32b.p;
+  if (mem == DFM2G_MEM_HOST) {
+    DFM2G_CUDA(cudaMemcpyAsync(a, vec, n * es, cudaMemcpyHostToDevice, stream()));
+  } else {
+    DFM2G_CUDA(cudaMemcpyAsync(a, vec, n * es, cudaMemcpyDeviceToDevice, stream()));
+  }
+  void *res = a;
+  if (which & 1) {
+    DFM2G_TRY(ilu_sweep(p, prec, true, res, b));
+    res = b;
+  }
+  if (which & 2) {
+    void *dst = (res == a) ? b : a;
+    DFM2G_TRY(ilu_sweep(p, prec, false, res, dst));
+    res = dst;
+  }
+  DFM2G_CUDA(cudaMemcpyAsync(vec, res, n * es, mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                             stream()));
+  return read_err(p);
+}
+
+int dfm2g_ilu_forward(dfm2g_ilu p, int prec, void *vec, int mem) { return precond_host(p, prec, vec, mem, 1); }
+int dfm2g_ilu_backward(dfm2g_ilu p, int prec, void *vec, int mem) { return precond_host(p, prec, vec, mem, 2); }
+int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) { return precond_host(p, prec, vec, mem, 3); }
+
+int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
+  DFM2G_TRY(check_ilu(p, false, false));
+  if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS) return fail(DFM2G_ERR_ARG, "unknown sweep mode");
+  p->sweep_mode = mode;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_ind) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  if (col && p->nnz) DFM2G_CUDA(cudaMemcpyAsync(col, p->col.p, sizeof(unsigned) * p->nnz, cudaMemcpyDeviceToHost, stream()));
+  if (dia_ind && p->nblk)
+    DFM2G_CUDA(cudaMemcpyAsync(dia_ind, p->dia_ind.p, sizeof(unsigned) * p->nblk, cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (vcrs && p->nnz) DFM2G_CUDA(cudaMemcpyAsync(vcrs, p->vcrs.p, sizeof(double) * 9 * p->nnz, k, stream()));
+  if (vdia && p->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, p->vdia.p, sizeof(double) * 9 * p->nblk, k, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, unsigned *order, unsigned *level_start,
+                         unsigned *nlevels) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  const unsigned n = p->nblk;
+  const unsigned nlev = backward ? p->nlev_b : p->nlev_f;
+  if (level && n)
+    DFM2G_CUDA(cudaMemcpyAsync(level, backward ? p->level_b.p : p->level_f.p, sizeof(unsigned) * n,
+                               cudaMemcpyDeviceToHost, stream()));
+  if (order && n)
+    DFM2G_CUDA(cudaMemcpyAsync(order, backward ? p->order_b.p : p->order_f.p, sizeof(unsigned) * n,
+                               cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (level_start) {
+    const std::vector<unsigned> &hl = backward ? p->h_lstart_b : p->h_lstart_f;
+    std::memcpy(level_start, hl.data(), sizeof(unsigned) * hl.size());
+  }
+  if (nlevels) *nlevels = nlev;
+  return DFM2G_OK;
+}
+
+}  // extern "C"

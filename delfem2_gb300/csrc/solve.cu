@@ -1,0 +1,577 @@
+// Krylov solvers on the device: Solve_PCG (FP64, the reference's exact
+// semantics), Solve_CG, and the FP32-inner / FP64-refinement PCG.
+//
+// All scalars of the iteration (alpha, beta, (r,Pr), |r|^2, the history and
+// the stop flag) live in device memory. Each reduction is deterministic: every
+// block writes its partial sum and the last block to finish adds the partials
+// in block order and applies the scalar update (alpha = rPr/pAp, ...). Every
+// kernel of an iteration first reads the stop flag and returns if it is set,
+// so the host can queue iterations in chunks and only synchronise between
+// chunks.
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace dfm2g {
+
+struct IterState {
+  double inv_rr0;  // 1/|r0|^2
+  double rPr;      // (r, Pr) of the current iterate (CG: |r|^2)
+  double alpha, beta;
+  double tol;
+  double rr;       // latest |r|^2
+  unsigned it;     // completed iterations
+  unsigned max_iter;
+  int done;        // 0 running, 1 converged, 2 exhausted, 3 |r0|^2 < 1e-30, 4 non-finite
+  unsigned nhist;
+  unsigned hist_cap;
+  int mode;        // 0 PCG (absolute history), 1 CG (relative history)
+  unsigned ticket[4];
+};
+
+constexpr int kThreads = 256;
+
+template <typename T>
+struct Acc {
+  using type = double;
+};
+
+// p.Ap fused into the SpMV Ap = K p (warp per block row).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_spmv_pAp(IterState *st, unsigned nblk,
+                                                       const unsigned *__restrict__ row_start,
+                                                       const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                                       const T *__restrict__ vdia, const T *__restrict__ p,
+                                                       T *__restrict__ Ap, double *partials) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
+  double dot = 0.0;
+  for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nblk; row += nwarp) {
+    const unsigned s0 = row_start[row], s1 = row_start[row + 1];
+    T a0 = 0, a1 = 0, a2 = 0;
+    for (unsigned cb = s0; cb < s1; cb += 32) {
+      const unsigned nb = min(32u, s1 - cb);
+      const unsigned my_col = lane < nb ? col[cb + lane] : 0u;
+      const size_t e_begin = (size_t)cb * 9, e_end = e_begin + (size_t)nb * 9;
+      for (size_t base = e_begin; base < e_end; base += 32) {
+        const size_t e = base + lane;
+        const bool ok = e < e_end;
+        const unsigned loc = ok ? (unsigned)(e - e_begin) : 0u;
+        const unsigned b = loc / 9u, rem = loc - b * 9u, r = rem / 3u, c = rem - r * 3u;
+        const unsigned j = __shfl_sync(0xffffffffu, my_col, b);
+        if (ok) {
+          const T v = vcrs[e] * p[(size_t)j * 3 + c];
+          a0 += (r == 0) ? v : T(0);
+          a1 += (r == 1) ? v : T(0);
+          a2 += (r == 2) ? v : T(0);
+        }
+      }
+    }
+    if (lane < 9) {
+      const unsigned r = lane / 3u, c = lane - r * 3u;
+      const T v = vdia[(size_t)row * 9 + lane] * p[(size_t)row * 3 + c];
+      a0 += (r == 0) ? v : T(0);
+      a1 += (r == 1) ? v : T(0);
+      a2 += (r == 2) ? v : T(0);
+    }
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    a2 = warp_sum(a2);
+    if (lane < 3) {
+      const T s = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
+      Ap[(size_t)row * 3 + lane] = s;
+      dot += (double)(s * p[(size_t)row * 3 + lane]);
+    }
+  }
+  double total;
+  if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
+    st->alpha = st->rPr / total;
+  }
+}
+
+// r -= alpha Ap; x += alpha p; |r|^2 -> history and the stop test.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T *__restrict__ r, T *__restrict__ x,
+                                                     const T *__restrict__ p, const T *__restrict__ Ap,
+                                                     double *partials, double *hist) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  const double alpha = st->alpha;
+  double rr = 0.0;
+  if (sizeof(T) == 8) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const double ri = (double)r[i] + (-alpha) * (double)Ap[i];
+      r[i] = (T)ri;
+      x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+      rr += ri * ri;
+    }
+  } else {
+    const float a = (float)alpha;
+    float acc = 0.f;
+    unsigned k = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const float ri = (float)r[i] - a * (float)Ap[i];
+      r[i] = (T)ri;
+      x[i] = (T)((float)x[i] + a * (float)p[i]);
+      acc += ri * ri;
+      if (++k == 8) {  // short FP32 runs, accumulated in FP64
+        rr += (double)acc;
+        acc = 0.f;
+        k = 0;
+      }
+    }
+    rr += (double)acc;
+  }
+  double total;
+  if (grid_sum_last(rr, partials, &st->ticket[1], sh, &total)) {
+    st->rr = total;
+    const unsigned it = st->it + 1;
+    st->it = it;
+    const double ratio = sqrt(total * st->inv_rr0);
+    const double entry = st->mode == 0 ? sqrt(total) : ratio;
+    if (st->nhist < st->hist_cap) hist[st->nhist] = entry;
+    st->nhist++;
+    if (!isfinite(total)) {
+      st->done = 4;
+    } else if (ratio < st->tol) {
+      st->done = 1;
+    } else if (it >= st->max_iter) {
+      if (st->mode == 0) {  // Solve_PCG appends a final |r| on exhaustion
+        if (st->nhist < st->hist_cap) hist[st->nhist] = sqrt(total);
+        st->nhist++;
+      }
+      st->done = 2;
+    } else if (st->mode == 1) {  // CG: beta = |r1|^2/|r0|^2
+      st->beta = total / st->rPr;
+      st->rPr = total;
+    }
+  }
+}
+
+// rPr1 = (r, Pr); beta = rPr1/rPr.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_dot_beta(IterState *st, size_t n, const T *__restrict__ r,
+                                                       const T *__restrict__ z, double *partials) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  double s = 0.0;
+  float acc = 0.f;
+  unsigned k = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (sizeof(T) == 8) {
+      s += (double)r[i] * (double)z[i];
+    } else {
+      acc += (float)r[i] * (float)z[i];
+      if (++k == 8) {
+        s += (double)acc;
+        acc = 0.f;
+        k = 0;
+      }
+    }
+  }
+  s += (double)acc;
+  double total;
+  if (grid_sum_last(s, partials, &st->ticket[2], sh, &total)) {
+    st->beta = total / st->rPr;
+    st->rPr = total;
+  }
+}
+
+// p = z + beta p
+template <typename T>
+__global__ void k_p_update(const IterState *st, size_t n, T *__restrict__ p, const T *__restrict__ z) {
+  if (st->done) return;
+  const double beta = st->beta;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (sizeof(T) == 8)
+      p[i] = (T)(beta * (double)p[i] + (double)z[i]);
+    else
+      p[i] = (T)((float)beta * (float)p[i] + (float)z[i]);
+  }
+}
+
+template <typename T>
+__global__ void k_fill_pending(const IterState *st, size_t n, T *out) {
+  if (st && st->done) return;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (sizeof(T) == 8)
+      reinterpret_cast<unsigned long long *>(out)[i] = ~0ull;
+    else
+      reinterpret_cast<unsigned *>(out)[i] = ~0u;
+  }
+}
+
+// generic deterministic dot into a device scalar
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_dot(size_t n, const T *__restrict__ a, const T *__restrict__ b,
+                                                  double *partials, unsigned *ticket, double *out) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s += (double)a[i] * (double)b[i];
+  double total;
+  if (grid_sum_last(s, partials, ticket, sh, &total)) *out = total;
+}
+
+// Start of PCG/CG: state from |r0|^2 (scal[0]) and (r0, Pr0) (scal[1]).
+__global__ void k_init_state(IterState *st, const double *scal, double *hist, int mode) {
+  const double rr0 = scal[0];
+  st->rr = rr0;
+  st->it = 0;
+  st->nhist = 0;
+  st->done = 0;
+  if (mode == 0) {
+    if (st->hist_cap > 0) hist[0] = sqrt(rr0);
+    st->nhist = 1;
+  }
+  if (rr0 < 1.0e-30) {
+    st->done = 3;
+    return;
+  }
+  if (!isfinite(rr0)) {
+    st->done = 4;
+    return;
+  }
+  st->inv_rr0 = 1.0 / rr0;
+  st->rPr = mode == 0 ? scal[1] : rr0;
+  if (st->max_iter == 0) {  // no iteration: Solve_PCG still appends the final |r|
+    if (mode == 0) {
+      if (st->nhist < st->hist_cap) hist[st->nhist] = sqrt(rr0);
+      st->nhist++;
+    }
+    st->done = 2;
+  }
+}
+
+template <typename T>
+__global__ void k_scale_convert(size_t n, const double *__restrict__ in, double s, T *__restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (T)(in[i] * s);
+}
+
+template <typename T>
+__global__ void k_accumulate(size_t n, double *__restrict__ x, double s, const T *__restrict__ d) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    x[i] += s * (double)d[i];
+}
+
+// ---------------------------------------------------------------------------
+// Workspace shared by the solvers (grown on demand).
+struct Workspace {
+  DevBuf<IterState> st;
+  DevBuf<double> partials, scal, hist;
+  DevBuf<unsigned> tickets;
+  DevBuf<double> v64[6];
+  DevBuf<float> v32[6];
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+static Workspace g_ws;
+
+static unsigned reduce_blocks() { return (unsigned)ctx().num_sms * 4; }
+
+static int ws_prepare(size_t n, unsigned hist_cap, bool need32) {
+  DFM2G_TRY(g_ws.st.ensure(1));
+  DFM2G_TRY(g_ws.partials.ensure((size_t)ctx().num_sms * 64));
+  DFM2G_TRY(g_ws.scal.ensure(8));
+  DFM2G_TRY(g_ws.tickets.ensure(4));
+  DFM2G_TRY(g_ws.hist.ensure(hist_cap + 4));
+  for (auto &b : g_ws.v64) DFM2G_TRY(b.ensure(n + 1));
+  if (need32)
+    for (auto &b : g_ws.v32) DFM2G_TRY(b.ensure(n + 1));
+  if (!g_ws.ev0) {
+    DFM2G_CUDA(cudaEventCreate(&g_ws.ev0));
+    DFM2G_CUDA(cudaEventCreate(&g_ws.ev1));
+  }
+  return DFM2G_OK;
+}
+
+static int dot_dev(size_t n, const void *a, const void *b, int prec, double *out_dev) {
+  DFM2G_CUDA(cudaMemsetAsync(g_ws.tickets.p, 0, sizeof(unsigned), stream()));
+  note_launches(1);
+  if (prec == DFM2G_F64)
+    k_dot<double><<<reduce_blocks(), kThreads, 0, stream()>>>(n, (const double *)a, (const double *)b,
+                                                             g_ws.partials.p, g_ws.tickets.p, out_dev);
+  else
+    k_dot<float><<<reduce_blocks(), kThreads, 0, stream()>>>(n, (const float *)a, (const float *)b, g_ws.partials.p,
+                                                            g_ws.tickets.p, out_dev);
+  DFM2G_LAUNCH_CHECK();
+  return DFM2G_OK;
+}
+
+static int dot_host(size_t n, const void *a, const void *b, int prec, double *out) {
+  DFM2G_TRY(dot_dev(n, a, b, prec, g_ws.scal.p + 7));
+  DFM2G_CUDA(cudaMemcpyAsync(out, g_ws.scal.p + 7, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+// Core preconditioned CG on device vectors of type T.
+//  r: rhs in, final residual out; x: solution out (starts at 0);
+//  w0..w3: scratch vectors (Pr/Ap share w0 as in the reference, p = w1,
+//  sweep intermediate = w2).
+template <typename T>
+static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T *w2, double tol,
+                    unsigned max_iter, unsigned hist_cap, int mode, IterState *h_state) {
+  const int prec = sizeof(T) == 8 ? DFM2G_F64 : DFM2G_F32;
+  const unsigned nblk = m->nblk;
+  const size_t n = (size_t)nblk * 3;
+  const T *vcrs = sizeof(T) == 8 ? (const T *)m->vcrs.p : (const T *)m->vcrs32.p;
+  const T *vdia = sizeof(T) == 8 ? (const T *)m->vdia.p : (const T *)m->vdia32.p;
+  IterState init{};
+  init.tol = tol;
+  init.max_iter = max_iter;
+  init.hist_cap = hist_cap;
+  init.mode = mode;
+  IterState *st = g_ws.st.p;
+  DFM2G_CUDA(cudaMemcpyAsync(st, &init, sizeof(init), cudaMemcpyHostToDevice, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n, stream()));
+  DFM2G_TRY(dot_dev(n, r, r, prec, g_ws.scal.p + 0));
+  T *Pr = w0, *pv = w1, *mid = w2;
+  if (mode == 0) {
+    // Pr = M^-1 r ; p = Pr ; rPr = (r, Pr)
+    DFM2G_TRY(ilu_sweep(p, prec, true, r, mid));
+    DFM2G_TRY(ilu_sweep(p, prec, false, mid, Pr));
+    DFM2G_CUDA(cudaMemcpyAsync(pv, Pr, sizeof(T) * n, cudaMemcpyDeviceToDevice, stream()));
+    DFM2G_TRY(dot_dev(n, r, Pr, prec, g_ws.scal.p + 1));
+  } else {
+    DFM2G_CUDA(cudaMemcpyAsync(pv, r, sizeof(T) * n, cudaMemcpyDeviceToDevice, stream()));
+  }
+  k_init_state<<<1, 1, 0, stream()>>>(st, g_ws.scal.p, g_ws.hist.p, mode);
+  note_launches(1);
+  DFM2G_LAUNCH_CHECK();
+  const unsigned spmv_blocks = blocks_for((size_t)nblk * 32, kThreads, (unsigned)ctx().num_sms * 8);
+  const unsigned vec_blocks = reduce_blocks();
+  const int chunk = 16;
+  for (;;) {
+    for (int k = 0; k < chunk; ++k) {
+      T *Ap = Pr;
+      {
+        ProfScope ps(DFM2G_PROF_SPMV, 1);
+        k_spmv_pAp<T><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p, vcrs, vdia, pv,
+                                                             Ap, g_ws.partials.p);
+      }
+      {
+        ProfScope ps(DFM2G_PROF_UPDATE, 1);
+        k_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, x, pv, Ap, g_ws.partials.p, g_ws.hist.p);
+      }
+      if (mode == 0) {
+        if (p->sweep_mode == DFM2G_SWEEP_SYNCFREE) {
+          ProfScope ps(DFM2G_PROF_FILL, 2);
+          k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, mid);
+          k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, Pr);
+        }
+        {
+          ProfScope ps(DFM2G_PROF_FWD, 0);
+          DFM2G_TRY(ilu_sweep_guarded(p, prec, true, r, mid, &st->done));
+        }
+        {
+          ProfScope ps(DFM2G_PROF_BWD, 0);
+          DFM2G_TRY(ilu_sweep_guarded(p, prec, false, mid, Pr, &st->done));
+        }
+        {
+          ProfScope ps(DFM2G_PROF_DOT, 1);
+          k_dot_beta<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, Pr, g_ws.partials.p);
+        }
+        {
+          ProfScope ps(DFM2G_PROF_PUPDATE, 1);
+          k_p_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, pv, Pr);
+        }
+      } else {
+        ProfScope ps(DFM2G_PROF_PUPDATE, 1);
+        k_p_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, pv, r);
+      }
+    }
+    DFM2G_LAUNCH_CHECK();
+    DFM2G_CUDA(cudaMemcpyAsync(h_state, st, sizeof(IterState), cudaMemcpyDeviceToHost, stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+    if (h_state->done) break;
+  }
+  if (p) {
+    int e = 0;
+    DFM2G_CUDA(cudaMemcpyAsync(&e, p->err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+    if (e) {
+      DFM2G_CUDA(cudaMemsetAsync(p->err.p, 0, sizeof(int), stream()));
+      return fail(DFM2G_ERR_WAIT_TIMEOUT, "PCG: a triangular-sweep wait timed out");
+    }
+  }
+  return DFM2G_OK;
+}
+
+static int check_pair(dfm2g_bsr m, dfm2g_ilu p) {
+  if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "matrix has no pattern");
+  if (p && (!p->has_factor || p->nblk != m->nblk))
+    return fail(DFM2G_ERR_STATE, "preconditioner not decomposed for this matrix");
+  return DFM2G_OK;
+}
+
+static int true_residual(dfm2g_bsr_s *m, const double *b, const double *x, double *res, double *rel) {
+  const size_t n = (size_t)m->nblk * 3;
+  DFM2G_CUDA(cudaMemcpyAsync(res, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
+  DFM2G_TRY(bsr_spmv(m, DFM2G_F64, res, -1.0, x, 1.0));
+  double rr = 0, bb = 0;
+  DFM2G_TRY(dot_host(n, res, res, DFM2G_F64, &rr));
+  DFM2G_TRY(dot_host(n, b, b, DFM2G_F64, &bb));
+  *rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+  return DFM2G_OK;
+}
+
+}  // namespace dfm2g
+
+using namespace dfm2g;
+
+extern "C" {
+
+int dfm2g_solve_pcg(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol, unsigned max_iter, double *hist,
+                    unsigned hist_cap, unsigned *n_hist, int mem, dfm2g_solve_stats *stats) {
+  DFM2G_TRY(check_pair(m, p));
+  if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg: null preconditioner");
+  if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_pcg: null vector");
+  const size_t n = (size_t)m->nblk * 3;
+  DFM2G_TRY(ws_prepare(n, max_iter + 2, false));
+  VecArg<double> ar, ax;
+  DFM2G_TRY(ar.in(r, n, mem, true));
+  DFM2G_TRY(ax.in(x, n, mem, false));
+  if (stats) DFM2G_CUDA(cudaMemcpyAsync(g_ws.v64[4].p, ar.dev(), sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev0, stream()));
+  IterState hs{};
+  DFM2G_TRY(pcg_core<double>(m, p, ar.dev(), ax.dev(), g_ws.v64[0].p, g_ws.v64[1].p, g_ws.v64[2].p, tol, max_iter,
+                             max_iter + 2, 0, &hs));
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev1, stream()));
+  DFM2G_TRY(ar.copy_back());
+  DFM2G_TRY(ax.copy_back());
+  if (hist && hist_cap) {
+    const unsigned k = std::min(hist_cap, hs.nhist);
+    DFM2G_CUDA(cudaMemcpyAsync(hist, g_ws.hist.p, sizeof(double) * k, cudaMemcpyDeviceToHost, stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  }
+  if (n_hist) *n_hist = hs.nhist;
+  if (stats) {
+    DFM2G_CUDA(cudaEventSynchronize(g_ws.ev1));
+    float ms = 0.f;
+    DFM2G_CUDA(cudaEventElapsedTime(&ms, g_ws.ev0, g_ws.ev1));
+    stats->ms = ms;
+    stats->iterations = hs.it;
+    stats->outer = 1;
+    DFM2G_TRY(true_residual(m, g_ws.v64[4].p, ax.dev(), g_ws.v64[5].p, &stats->rel_residual));
+  }
+  if (hs.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_pcg: non-finite residual");
+  if (hs.done == 2) return fail(DFM2G_ERR_NOT_CONVERGED, "solve_pcg: %u iterations without reaching tol", max_iter);
+  return DFM2G_OK;
+}
+
+int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_iter, double *hist, unsigned hist_cap,
+                   unsigned *n_hist, int mem, dfm2g_solve_stats *stats) {
+  DFM2G_TRY(check_pair(m, nullptr));
+  if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_cg: null vector");
+  const size_t n = (size_t)m->nblk * 3;
+  DFM2G_TRY(ws_prepare(n, max_iter + 2, false));
+  VecArg<double> ar, ax;
+  DFM2G_TRY(ar.in(r, n, mem, true));
+  DFM2G_TRY(ax.in(x, n, mem, false));
+  if (stats) DFM2G_CUDA(cudaMemcpyAsync(g_ws.v64[4].p, ar.dev(), sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev0, stream()));
+  IterState hs{};
+  DFM2G_TRY(pcg_core<double>(m, nullptr, ar.dev(), ax.dev(), g_ws.v64[0].p, g_ws.v64[1].p, g_ws.v64[2].p, tol,
+                             max_iter, max_iter + 2, 1, &hs));
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev1, stream()));
+  DFM2G_TRY(ar.copy_back());
+  DFM2G_TRY(ax.copy_back());
+  if (hist && hist_cap) {
+    const unsigned k = std::min(hist_cap, hs.nhist);
+    DFM2G_CUDA(cudaMemcpyAsync(hist, g_ws.hist.p, sizeof(double) * k, cudaMemcpyDeviceToHost, stream()));
+    DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  }
+  if (n_hist) *n_hist = hs.nhist;
+  if (stats) {
+    DFM2G_CUDA(cudaEventSynchronize(g_ws.ev1));
+    float ms = 0.f;
+    DFM2G_CUDA(cudaEventElapsedTime(&ms, g_ws.ev0, g_ws.ev1));
+    stats->ms = ms;
+    stats->iterations = hs.it;
+    stats->outer = 1;
+    DFM2G_TRY(true_residual(m, g_ws.v64[4].p, ax.dev(), g_ws.v64[5].p, &stats->rel_residual));
+  }
+  if (hs.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_cg: non-finite residual");
+  if (hs.done == 2) return fail(DFM2G_ERR_NOT_CONVERGED, "solve_cg: %u iterations without reaching tol", max_iter);
+  return DFM2G_OK;
+}
+
+int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, double tol, double inner_tol,
+                          unsigned max_iter, unsigned max_outer, int mem, dfm2g_solve_stats *stats) {
+  DFM2G_TRY(check_pair(m, p));
+  if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null preconditioner");
+  if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null vector");
+  if (!(inner_tol > 0 && inner_tol < 1)) return fail(DFM2G_ERR_ARG, "inner_tol must be in (0,1)");
+  const size_t n = (size_t)m->nblk * 3;
+  DFM2G_TRY(ws_prepare(n, 4, true));
+  DFM2G_TRY(bsr_ensure_f32(m));
+  DFM2G_TRY(ilu_ensure_f32(p));
+  VecArg<double> ab, ax;
+  DFM2G_TRY(ab.in(b, n, mem, true));
+  DFM2G_TRY(ax.in(x, n, mem, false));
+  double *r64 = g_ws.v64[3].p;
+  float *r32 = g_ws.v32[3].p, *d32 = g_ws.v32[4].p;
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev0, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(ax.dev(), 0, sizeof(double) * n, stream()));
+  DFM2G_CUDA(cudaMemcpyAsync(r64, ab.dev(), sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
+  double bb = 0;
+  DFM2G_TRY(dot_host(n, ab.dev(), ab.dev(), DFM2G_F64, &bb));
+  const double bnorm = std::sqrt(bb);
+  unsigned total_it = 0, outer = 0;
+  double rel = bnorm > 0 ? 1.0 : 0.0;
+  int status = DFM2G_OK;
+  const unsigned vb = reduce_blocks();
+  while (bnorm > 0) {
+    double rr = 0;
+    DFM2G_TRY(dot_host(n, r64, r64, DFM2G_F64, &rr));
+    rel = std::sqrt(rr) / bnorm;
+    if (!std::isfinite(rel)) {
+      status = fail(DFM2G_ERR_NONFINITE, "solve_pcg_mixed: non-finite residual");
+      break;
+    }
+    if (rel < tol) break;
+    if (outer >= max_outer || total_it >= max_iter) {
+      status = fail(DFM2G_ERR_NOT_CONVERGED, "solve_pcg_mixed: stopped at relative residual %.3e", rel);
+      break;
+    }
+    const double s = std::sqrt(rr);
+    {
+      ProfScope ps(DFM2G_PROF_OUTER, 1);
+      k_scale_convert<float><<<vb, kThreads, 0, stream()>>>(n, r64, 1.0 / s, r32);
+    }
+    DFM2G_LAUNCH_CHECK();
+    IterState hs{};
+    DFM2G_TRY(pcg_core<float>(m, p, r32, d32, g_ws.v32[0].p, g_ws.v32[1].p, g_ws.v32[2].p, inner_tol,
+                              max_iter - total_it, 4, 0, &hs));
+    total_it += hs.it;
+    if (hs.done == 4) {
+      status = fail(DFM2G_ERR_NONFINITE, "solve_pcg_mixed: non-finite inner residual");
+      break;
+    }
+    {
+      ProfScope ps(DFM2G_PROF_OUTER, 1);
+      k_accumulate<float><<<vb, kThreads, 0, stream()>>>(n, ax.dev(), s, d32);
+      DFM2G_CUDA(cudaMemcpyAsync(r64, ab.dev(), sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
+      DFM2G_TRY(bsr_spmv(m, DFM2G_F64, r64, -1.0, ax.dev(), 1.0));
+    }
+    ++outer;
+  }
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev1, stream()));
+  DFM2G_TRY(ax.copy_back());
+  if (stats) {
+    DFM2G_CUDA(cudaEventSynchronize(g_ws.ev1));
+    float ms = 0.f;
+    DFM2G_CUDA(cudaEventElapsedTime(&ms, g_ws.ev0, g_ws.ev1));
+    stats->ms = ms;
+    stats->iterations = total_it;
+    stats->outer = outer;
+    stats->rel_residual = rel;
+  }
+  return status;
+}
+
+}  // extern "C"

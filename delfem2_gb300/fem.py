@@ -1,0 +1,64 @@
+"""Linear-tet elasticity on the device (assembly and the adjoint element term).
+
+TetMesh mirrors the per-element loop of MergeLinSys_SolidLinear_Static_MeshTet3D
+(include/delfem2/fem_solidlinear.h:192-237) with a per-tet Young's modulus;
+the assembly runs as colour-scheduled, atomic-free CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .ls import CMatrixSparse, _same_mem, _vec
+
+
+def lame(E, nu):
+    """(lambda, myu) from Young's modulus and Poisson's ratio."""
+    return E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), E / (2.0 * (1.0 + nu))
+
+
+class TetMesh:
+    """Element->slot map and colouring of a tet mesh against K's pattern."""
+
+    def __init__(self, mat: CMatrixSparse, xyz, tet):
+        self.xyz = np.ascontiguousarray(xyz, np.float64)
+        self.tet = np.ascontiguousarray(tet, np.uint32)
+        self.np = self.xyz.size // 3
+        self.ntet = self.tet.size // 4
+        h = C.c_void_p()
+        N.call("dfm2g_tetmesh_create", C.byref(h), mat._h, self.xyz.ctypes.data, self.np, self.tet.ctypes.data,
+               self.ntet)
+        self._h = h
+        self.mat = mat
+
+    @property
+    def ncolor(self) -> int:
+        n = C.c_uint()
+        N.call("dfm2g_tetmesh_info", self._h, C.byref(n), None)
+        return n.value
+
+    def assemble_linear(self, young, nu: float, rho: float, g, b, disp=None):
+        """K += K_e(E_e); b += rho g vol/4 - K_e u_e (b in place)."""
+        py, my, ky = _vec(young, np.float64, False)
+        pb, mb, kb = _vec(b, np.float64, True)
+        pd, md, kd = _vec(disp, np.float64, False) if disp is not None else (None, None, None)
+        g3 = (C.c_double * 3)(*[float(v) for v in g])
+        N.call("dfm2g_tetmesh_assemble_linear", self._h, self.mat._h, py, float(nu), float(rho), g3, pd, pb,
+               _same_mem(my, mb, md))
+
+    def dLdE(self, nu: float, u, lam, out):
+        """out[e] = -lam_e^T (dK_e/dE_e) u_e."""
+        pu, mu, ku = _vec(u, np.float64, False)
+        pl, ml, kl = _vec(lam, np.float64, False)
+        po, mo, ko = _vec(out, np.float64, True)
+        N.call("dfm2g_tetmesh_dLdE", self._h, None, float(nu), pu, pl, po, _same_mem(mu, ml, mo))
+
+    def __del__(self):
+        try:
+            if self._h is not None:
+                N.load().dfm2g_tetmesh_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass

@@ -1,0 +1,227 @@
+/*
+ * dfm2g.h — C ABI of the GB300-native (sm_103a, one GPU) drop-in for DelFEM2's
+ * implicit-FEM linear-solve path: 3x3 block-CSR assembly (CMatrixSparse /
+ * Merge), ILU(0) (CPreconditionerILU) and preconditioned CG (Solve_PCG).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (DFM2G_OK == 0). A failing call
+ *    leaves a message for dfm2g_last_error() (per host thread).
+ *  - Index arrays are uint32 ("unsigned int" in the reference). Following
+ *    CMatrixSparse, `row_start` is what the reference calls col_ind_ (row
+ *    offsets, nblk+1 entries) and `col` is its row_ptr_ (column id of each
+ *    off-diagonal block). Diagonal blocks are stored separately. Blocks are
+ *    row-major 3x3.
+ *  - Vector arguments live in host or device memory as the per-call `mem`
+ *    flag says (DFM2G_MEM_HOST / DFM2G_MEM_DEVICE). Device pointers must be on
+ *    the library's current device; host pointers are copied in/out.
+ *  - All work is queued on the library stream (dfm2g_set_stream); calls that
+ *    return host data synchronise it.
+ *  - Only 3x3 blocks (ndim == 3) are supported; other block sizes return
+ *    DFM2G_ERR_UNSUPPORTED.
+ */
+#ifndef DFM2G_H
+#define DFM2G_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DFM2G_API __attribute__((visibility("default")))
+
+/* ---- status codes ------------------------------------------------------ */
+enum dfm2g_status {
+  DFM2G_OK = 0,
+  DFM2G_ERR_ARG = 1,             /* bad argument / size mismatch           */
+  DFM2G_ERR_CUDA = 2,            /* a CUDA runtime call failed             */
+  DFM2G_ERR_MISSING_SLOT = 3,    /* Merge target block not in the pattern  */
+  DFM2G_ERR_SINGULAR_PIVOT = 4,  /* more than 10 pivots with |det|<=1e-30  */
+  DFM2G_ERR_NOT_CONVERGED = 5,   /* iteration limit hit (solution valid)   */
+  DFM2G_ERR_WAIT_TIMEOUT = 6,    /* a bounded device-side wait gave up     */
+  DFM2G_ERR_PATTERN = 7,         /* invalid sparsity pattern               */
+  DFM2G_ERR_UNSUPPORTED = 8,     /* block size or mode not supported       */
+  DFM2G_ERR_STATE = 9,           /* call order violated (e.g. no pattern)  */
+  DFM2G_ERR_NONFINITE = 10       /* NaN/Inf met in a solve                 */
+};
+
+enum dfm2g_mem { DFM2G_MEM_HOST = 0, DFM2G_MEM_DEVICE = 1 };
+enum dfm2g_prec { DFM2G_F64 = 0, DFM2G_F32 = 1 };
+
+/* Triangular-sweep schedule (dfm2g_ilu_set_sweep_mode). */
+enum dfm2g_sweep {
+  DFM2G_SWEEP_SYNCFREE = 0, /* one persistent launch, per-row readiness     */
+  DFM2G_SWEEP_LEVELS = 1    /* one launch per level set                     */
+};
+
+typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>, 3x3  */
+typedef struct dfm2g_ilu_s *dfm2g_ilu;       /* CPreconditionerILU<double>  */
+typedef struct dfm2g_tetmesh_s *dfm2g_tetmesh; /* linear-tet assembler      */
+
+/* Per-solve record filled by the solvers (any pointer may be NULL). */
+typedef struct dfm2g_solve_stats {
+  unsigned iterations;     /* total (inner) PCG iterations                  */
+  unsigned outer;          /* refinement steps (1 for plain solves)          */
+  double rel_residual;     /* |b - K x| / |b| in FP64 at exit               */
+  double ms;               /* device time of the solve (CUDA events)         */
+} dfm2g_solve_stats;
+
+/* ---- library ------------------------------------------------------------ */
+DFM2G_API int dfm2g_version(void);
+DFM2G_API const char *dfm2g_status_string(int status);
+DFM2G_API const char *dfm2g_last_error(void);
+/* Use `stream` (a cudaStream_t; NULL = the library's own stream). */
+DFM2G_API int dfm2g_set_stream(void *stream);
+DFM2G_API int dfm2g_synchronize(void);
+
+/* ---- host-side mesh and pattern helpers --------------------------------- */
+/* MeshTet3D_VoxelGrid, include/delfem2/gridvoxel.cpp:194-271, every voxel
+ * active, coordinates multiplied by `scale`. xyz: 3*(nx+1)(ny+1)(nz+1),
+ * tet: 4*6*nx*ny*nz. */
+DFM2G_API int dfm2g_mesh_tet_voxel_grid(unsigned nx, unsigned ny, unsigned nz, double scale,
+                                        double *xyz, unsigned *tet);
+/* JArray_PSuP_MeshElem + JArray_Sort, include/delfem2/msh_topology_uniform.cpp:301-316
+ * and include/delfem2/jagarray.cpp:72-92. Call _count first (fills psup_ind,
+ * np+1 entries, and *npsup), then _fill with a psup buffer of *npsup entries. */
+DFM2G_API int dfm2g_psup_count(const unsigned *elem, size_t nelem, unsigned nnoel, size_t np,
+                               unsigned *psup_ind, size_t *npsup);
+DFM2G_API int dfm2g_psup_fill(const unsigned *elem, size_t nelem, unsigned nnoel, size_t np,
+                              const unsigned *psup_ind, unsigned *psup);
+
+/* ---- CMatrixSparse (include/delfem2/ls_block_sparse.h:24-204) ------------- */
+/* Initialize(nblk, ndim, is_dia=true), ls_block_sparse.h:45-55. */
+DFM2G_API int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim);
+DFM2G_API int dfm2g_bsr_destroy(dfm2g_bsr m);
+/* SetPattern(colind, ncolind, rowptr, nrowptr), ls_block_sparse.h:72-85.
+ * Host arrays. Values become zero. */
+DFM2G_API int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_start,
+                                    const unsigned *col, size_t ncol);
+DFM2G_API int dfm2g_bsr_info(dfm2g_bsr m, unsigned *nblk, size_t *nnz);
+/* setZero, ls_block_sparse.h:92-105. */
+DFM2G_API int dfm2g_bsr_set_zero(dfm2g_bsr m);
+/* Direct access to val_crs_ (9*nnz) and val_dia_ (9*nblk); either may be NULL. */
+DFM2G_API int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, int mem);
+DFM2G_API int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem);
+/* SetFixedBC = SetFixedBC_Dia(1)+Row+Col, ls_block_sparse.h:147-151,
+ * ls_block_sparse.cpp:397-472. bc: 3*nblk ints, nonzero = fixed. */
+DFM2G_API int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem);
+/* AddDia(eps), ls_block_sparse.h:153-164. */
+DFM2G_API int dfm2g_bsr_add_dia(dfm2g_bsr m, double eps);
+/* MatVec: y = alpha*K*x + beta*y, ls_block_sparse.cpp:215-273 (y is scaled by
+ * beta first, so a NaN in y survives beta == 0). prec DFM2G_F32 uses the FP32
+ * mirror of the values (refreshed by dfm2g_bsr_update_f32) and float vectors. */
+DFM2G_API int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x,
+                               double beta, int mem);
+/* Refresh the FP32 mirror of the values from the FP64 values. */
+DFM2G_API int dfm2g_bsr_update_f32(dfm2g_bsr m);
+/* Merge<nno,nno,3,3,double> for a batch of elements, ls_block_sparse.h:260-310:
+ * elem: nelem*nnoel node ids; emat: nelem*(nnoel*nnoel*9) row-major
+ * [irow][jcol][3][3]. The batch is colour-scheduled (no two elements of one
+ * colour share a node), so the scatter is atomic-free and deterministic.
+ * Returns DFM2G_ERR_MISSING_SLOT (and adds nothing) if a block is absent. */
+DFM2G_API int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned *elem,
+                              const double *emat, int mem);
+
+/* setRHS_Zero(b, bc, 0), include/delfem2/vecxitrsol.cpp:286-296 (FP64 vector of ndof). */
+DFM2G_API int dfm2g_vec_zero_bc(double *b, const int *bc, size_t ndof, int mem);
+
+/* ---- CPreconditionerILU (include/delfem2/ls_ilu_block_sparse.h:21-60) ----- */
+DFM2G_API int dfm2g_ilu_create(dfm2g_ilu *out);
+DFM2G_API int dfm2g_ilu_destroy(dfm2g_ilu p);
+/* SetPattern0 / Initialize_ILUk(m, 0), ls_ilu_block_sparse.cpp:1057-1090 and
+ * 854-857: pattern copied and row-sorted on the device, dia_ind found, and the
+ * forward/backward level sets computed on the device. */
+DFM2G_API int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m);
+/* CopyValue, ls_ilu_block_sparse.cpp:1009-1047. */
+DFM2G_API int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m);
+/* Decompose (3x3 branch), ls_ilu_block_sparse.cpp:152-160,286-356, level-
+ * scheduled on the device in FP64; also refreshes the FP32 copy of the factors.
+ * More than 10 pivots with |det| <= 1e-30 -> DFM2G_ERR_SINGULAR_PIVOT.
+ * *n_singular (may be NULL) receives the count of such pivots. */
+DFM2G_API int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular);
+/* ForwardSubstitution / BackwardSubstitution / SolvePrecond (in place),
+ * ls_ilu_block_sparse.cpp:544-573, 721-749, ls_ilu_block_sparse.h:38-41. */
+DFM2G_API int dfm2g_ilu_forward(dfm2g_ilu p, int prec, void *vec, int mem);
+DFM2G_API int dfm2g_ilu_backward(dfm2g_ilu p, int prec, void *vec, int mem);
+DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem);
+DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
+/* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
+ * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
+ * room for nblk+1). */
+DFM2G_API int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_ind);
+DFM2G_API int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem);
+DFM2G_API int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, unsigned *order,
+                                   unsigned *level_start, unsigned *nlevels);
+
+/* ---- Krylov solvers -------------------------------------------------------- */
+/* Solve_PCG, include/delfem2/lsitrsol.h:80-148, in FP64: x starts at 0; r is
+ * overwritten with the final residual; hist receives the ABSOLUTE residual
+ * norms [|r0|, |r1|, ...] (up to hist_cap entries; *n_hist is the full
+ * length); stops when sqrt(|r|^2/|r0|^2) < tol; one extra final entry when
+ * max_iter is exhausted (status DFM2G_ERR_NOT_CONVERGED, x still valid). */
+DFM2G_API int dfm2g_solve_pcg(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol,
+                              unsigned max_iter, double *hist, unsigned hist_cap,
+                              unsigned *n_hist, int mem, dfm2g_solve_stats *stats);
+/* Solve_CG, include/delfem2/lsitrsol.h:35-74, FP64; hist receives the
+ * RELATIVE ratios (the reference's convention for Solve_CG). */
+DFM2G_API int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_iter,
+                             double *hist, unsigned hist_cap, unsigned *n_hist, int mem,
+                             dfm2g_solve_stats *stats);
+/* Mixed precision: FP32 K + FP32 ILU factors + FP32 inner PCG (relative tol
+ * inner_tol per refinement step, FP64 alpha/beta reductions) inside an FP64
+ * iterative-refinement loop (r = b - K x from the FP64 values, x accumulated in
+ * FP64) until |b - K x|/|b| < tol. b is not modified. */
+DFM2G_API int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x,
+                                    double tol, double inner_tol, unsigned max_iter,
+                                    unsigned max_outer, int mem, dfm2g_solve_stats *stats);
+
+/* ---- linear-tet elasticity ------------------------------------------------- */
+/* Builds, for mesh (xyz: 3*np, tet: 4*ntet, host arrays) against the pattern
+ * of K: the element->slot map (device) and a greedy element colouring (no two
+ * tets of one colour share a node). */
+DFM2G_API int dfm2g_tetmesh_create(dfm2g_tetmesh *out, dfm2g_bsr m, const double *xyz, size_t np,
+                                   const unsigned *tet, size_t ntet);
+DFM2G_API int dfm2g_tetmesh_destroy(dfm2g_tetmesh t);
+DFM2G_API int dfm2g_tetmesh_info(dfm2g_tetmesh t, unsigned *ncolor, size_t *ntet);
+/* Per-tet-E assembly (adds): the loop of MergeLinSys_SolidLinear_Static_MeshTet3D,
+ * include/delfem2/fem_solidlinear.h:192-237, with EMat_SolidLinear_Static_Tet
+ * (fem_solidlinear.cpp:409-435) per element and (lambda, myu) from (E_e, nu).
+ * b += rho*g*vol/4 - K_e u_e per node; K += K_e. young: ntet; g: 3 host
+ * doubles; disp may be NULL (zero). */
+DFM2G_API int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const double *young,
+                                            double nu, double rho, const double *g,
+                                            const double *disp, double *b, int mem);
+/* Adjoint element term dL/dE_e = -lam_e^T (dK_e/dE_e) u_e (no reference
+ * counterpart; K_e is linear in E). young is unused except for shape checks. */
+DFM2G_API int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu,
+                                 const double *u, const double *lam, double *dLdE, int mem);
+
+/* ---- instrumentation ------------------------------------------------------- */
+/* Kernel classes timed when profiling is on (CUDA events around every launch
+ * of the solver loops; adds a little overhead, so off by default). */
+enum dfm2g_prof_kind {
+  DFM2G_PROF_SPMV = 0,     /* Ap = K p fused with p.Ap                       */
+  DFM2G_PROF_UPDATE = 1,   /* r -= a Ap, x += a p, |r|^2                       */
+  DFM2G_PROF_FILL = 2,     /* pending-marker fill of sweep outputs             */
+  DFM2G_PROF_FWD = 3,      /* forward sweep                                    */
+  DFM2G_PROF_BWD = 4,      /* backward sweep                                   */
+  DFM2G_PROF_DOT = 5,      /* (r, z) and beta                                  */
+  DFM2G_PROF_PUPDATE = 6,  /* p = z + beta p                                   */
+  DFM2G_PROF_OUTER = 7,    /* FP64 residual / refinement kernels               */
+  DFM2G_PROF_NKIND = 8
+};
+DFM2G_API int dfm2g_profile_enable(int on);
+DFM2G_API int dfm2g_profile_reset(void);
+DFM2G_API int dfm2g_profile_read(int kind, unsigned *launches, double *total_ms);
+/* Number of kernels this library has launched since load (all kinds). */
+DFM2G_API int dfm2g_launch_count(unsigned long long *count);
+
+/* ---- test support ---------------------------------------------------------- */
+/* Launches one tiny kernel that waits on a value nothing ever writes, bounded
+ * by `timeout_ms`; must return DFM2G_ERR_WAIT_TIMEOUT with the context usable. */
+DFM2G_API int dfm2g_debug_wait_timeout(unsigned timeout_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DFM2G_H */

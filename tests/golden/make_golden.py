@@ -1,0 +1,122 @@
+"""Generate the golden fixtures in tests/golden/ from the REFERENCE itself.
+
+Runs oracle/_ref/libdfm2ref.so (the unmodified DelFEM2 headers compiled by
+oracle/Makefile), so it only works where the reference source tree exists.
+The outputs are small .npz files committed next to this script; the tests
+read them on machines without the reference.
+
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4]
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import build, reference  # noqa: E402
+
+NU, RHO, G = 0.3, 1.0, np.array([0.0, 0.0, -1e-3])
+
+
+def young_log_uniform(ntet, lo, hi, seed):
+    # identical to delfem2_gb300.problem.young_log_uniform (kept separate so that
+    # this script does not load the CUDA library)
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), ntet))
+
+
+def sha(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def system(R, nx, ny, nz, h, young):
+    xyz, tet = R.voxel_tet_mesh(nx, ny, nz, h)
+    np_ = xyz.size // 3
+    ind, psup = R.psup(tet, 4, np_)
+    vc = np.zeros(psup.size * 9)
+    vd = np.zeros(np_ * 9)
+    b = np.zeros(np_ * 3)
+    if np.isscalar(young):
+        young = np.full(tet.size // 4, float(young))
+    assert R.assemble_tet_linear(ind, psup, vc, vd, b, xyz, tet, young, NU, RHO, G) == 0
+    bc = np.zeros(np_ * 3, np.int32)
+    bc[np.repeat(xyz[2::3] == 0.0, 3)] = 1
+    R.set_fixed_bc(ind, psup, vc, vd, bc)
+    R.rhs_zero(b, bc)
+    col, dia = R.ilu_pattern0(ind, psup)
+    ivc, ivd = R.ilu_copy_value(ind, col, psup, vc, vd)
+    st, _ = R.ilu_decompose(ind, col, dia, ivc, ivd)
+    assert st == 0
+    return dict(xyz=xyz, tet=tet, ind=ind, psup=psup, vc=vc, vd=vd, b=b, bc=bc, col=col, dia=dia, ivc=ivc,
+                ivd=ivd, young=young)
+
+
+def solve(R, s, tol, maxit=100000):
+    t = time.time()
+    x, r, hist = R.solve_pcg(s["ind"], s["psup"], s["vc"], s["vd"], s["col"], s["dia"], s["ivc"], s["ivd"],
+                             s["b"], tol, maxit)
+    return x, hist, time.time() - t
+
+
+def sample_idx(n, k=2000, seed=123):
+    return np.sort(np.random.default_rng(seed).choice(n, size=min(k, n), replace=False)).astype(np.int64)
+
+
+def make_tiny(R):
+    s = system(R, 3, 2, 2, 1.0 / 3, young_log_uniform(3 * 2 * 2 * 6, 0.1, 10.0, 7))
+    x, hist, _ = solve(R, s, 1e-10)
+    vec = np.random.default_rng(11).standard_normal(s["b"].size)
+    fwd = R.ilu_forward(s["ind"], s["col"], s["dia"], s["ivc"], s["ivd"], vec)
+    both = R.ilu_backward(s["ind"], s["col"], s["dia"], s["ivc"], fwd)
+    mv = R.matvec(s["ind"], s["psup"], s["vc"], s["vd"], np.zeros_like(vec), 1.0, vec, 0.0)
+    np.savez_compressed(os.path.join(HERE, "tiny.npz"), x=x, hist=np.array(hist), vec=vec, fwd=fwd,
+                        precond=both, matvec=mv, **{k: v for k, v in s.items()})
+
+
+def make_cfg(R, name, nx, ny, nz, h, young, tol, full_x):
+    s = system(R, nx, ny, nz, h, young)
+    x, hist, dt = solve(R, s, tol)
+    idx = sample_idx(x.size)
+    out = dict(nx=nx, ny=ny, nz=nz, h=h, tol=tol, n_iter=len(hist) - 1, hist=np.array(hist),
+               pattern_sha=sha(s["ind"], s["psup"]), dia_sha=sha(s["dia"]),
+               young_sha=sha(s["young"]), b=s["b"] if full_x else s["b"][idx],
+               x_norm=np.linalg.norm(x), x_sum=x.sum(), b_norm=np.linalg.norm(s["b"]),
+               K_abs_sum=np.abs(s["vc"]).sum() + np.abs(s["vd"]).sum(), idx=idx, x_sample=x[idx],
+               ilu_dia_sample=s["ivd"][idx % s["ivd"].size], seconds=dt)
+    if full_x:
+        out["x"] = x
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(f"{name}: ndof={x.size} iterations={len(hist) - 1} final={hist[-1]:.3e} "
+          f"rel={hist[-1] / hist[0]:.3e} time={dt:.1f}s")
+
+
+def main(which):
+    build(quiet=True)
+    R = reference()
+    if "tiny" in which:
+        make_tiny(R)
+    if "cfg1" in which:  # unit cube 16^3, E = 1
+        make_cfg(R, "cfg1", 16, 16, 16, 1 / 16, 1.0, 1e-10, True)
+    if "cfg1e" in which:  # 16^3, E log-uniform [0.1, 10], seed 0
+        make_cfg(R, "cfg1e", 16, 16, 16, 1 / 16, young_log_uniform(16 ** 3 * 6, 0.1, 10.0, 0), 1e-10, True)
+    if "cfg2" in which:  # 64^3, E log-uniform [0.1, 10], seed 2, oracle to 1e-12
+        make_cfg(R, "cfg2", 64, 64, 64, 1 / 64, young_log_uniform(64 ** 3 * 6, 0.1, 10.0, 2), 1e-12, False)
+    if "cfg3" in which:  # 128x128x64, spacing 1/128, E log-uniform [0.1, 10], seed 3, to 1e-12
+        make_cfg(R, "cfg3", 128, 128, 64, 1 / 128, young_log_uniform(128 * 128 * 64 * 6, 0.1, 10.0, 3), 1e-12,
+                 False)
+    if "cfg4" in which:  # 48^3, E log-uniform [0.5, 2], seed 4, to 1e-12
+        make_cfg(R, "cfg4", 48, 48, 48, 1 / 48, young_log_uniform(48 ** 3 * 6, 0.5, 2.0, 4), 1e-12, False)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or ["tiny", "cfg1", "cfg1e", "cfg2"])
