@@ -59,6 +59,14 @@ class StaticElasticProblem:
             b = np.zeros(self.ndof, np.float64)
         else:
             b.fill_(0.0) if hasattr(b, "fill_") else b.fill(0.0)
+        on_device = hasattr(b, "is_cuda") and b.is_cuda
+        if on_device and isinstance(young, np.ndarray):
+            import torch
+            key = (young.ctypes.data, young.size, str(b.device))
+            if getattr(self, "_young_key", None) != key:
+                self._young_dev = torch.from_numpy(young).to(b.device)
+                self._young_key = key
+            young = self._young_dev
         self.K.setZero()
         self.mesh.assemble_linear(young, self.nu, self.rho, self.g, b)
         self.K.SetFixedBC(self.a["bc"])
