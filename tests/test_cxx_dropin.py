@@ -1,0 +1,52 @@
+"""The C++ drop-in header (include/dfm2g.hpp) compiles and links against
+libdfm2g.so (CPU), and a DelFEM2-style caller written against it reproduces
+the reference's solve (GPU)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+SRC = os.path.join(ROOT, "tests", "cxx", "dropin_main.cpp")
+EXE = os.path.join(ROOT, "delfem2_gb300", "_build", "dropin_main")
+
+
+@pytest.fixture(scope="module")
+def exe(built_lib):
+    libdir = os.path.join(ROOT, "delfem2_gb300", "_build")
+    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), SRC, "-o", EXE, "-L" + libdir,
+           "-ldfm2g", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return EXE
+
+
+def test_dropin_header_compiles_and_links(exe):
+    assert os.path.exists(exe)
+
+
+@pytest.mark.gpu
+def test_dropin_caller_matches_oracle(exe, gpu, port):
+    out = subprocess.run([exe, "8"], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    f = out.stdout.split()
+    its, res, xsum = int(f[1]), float(f[3]), float(f[5])
+    # the same problem through the oracle
+    xyz, tet = port.voxel_tet_mesh(8, 8, 8, 1 / 8)
+    np_ = xyz.size // 3
+    ind, psup = port.psup(tet, 4, np_)
+    vc, vd, b = np.zeros(psup.size * 9), np.zeros(np_ * 9), np.zeros(np_ * 3)
+    port.assemble_tet_linear(ind, psup, vc, vd, b, xyz, tet, np.ones(tet.size // 4), 0.3, 1.0, [0, 0, -1e-3])
+    bc = np.zeros(np_ * 3, np.int32)
+    bc[np.repeat(xyz[2::3] == 0.0, 3)] = 1
+    port.set_fixed_bc(ind, psup, vc, vd, bc)
+    port.rhs_zero(b, bc)
+    col, dia = port.ilu_pattern0(ind, psup)
+    ivc, ivd = port.ilu_copy_value(ind, col, psup, vc, vd)
+    port.ilu_decompose(ind, col, dia, ivc, ivd)
+    x, _, h = port.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, 1e-10, 1000)
+    assert abs(its - (len(h) - 1)) <= 1
+    assert res < 1e-9
+    assert abs(xsum - x.sum()) <= 1e-8 * np.abs(x).sum()
