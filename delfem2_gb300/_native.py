@@ -84,6 +84,7 @@ SIGNATURES = {
     "dfm2g_ilu_forward": [_vp, _i, _vp, _i],
     "dfm2g_ilu_backward": [_vp, _i, _vp, _i],
     "dfm2g_ilu_solve_precond": [_vp, _i, _vp, _i],
+    "dfm2g_ilu_solve_precond_noalloc": [_vp, _i, _vp],
     "dfm2g_ilu_set_sweep_mode": [_vp, _i],
     "dfm2g_ilu_get_pattern": [_vp, _vp, _vp],
     "dfm2g_ilu_get_values": [_vp, _vp, _vp, _i],

@@ -10,6 +10,7 @@
 // bit-exact against a serial CPU recomputation.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -706,6 +707,65 @@ static int precond_host(dfm2g_ilu p, int prec, void *vec, int mem, int which /*1
   }
   DFM2G_CUDA(cudaMemcpyAsync(vec, res, n * es, mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
                              stream()));
+  return read_err(p);
+}
+
+// ---------------------------------------------------------------------------
+// SolvePrecond without any allocation.
+//
+// The forward sweep needs somewhere to put its result while the backward
+// sweep reads it. Here that intermediate vector is this fixed device array
+// instead of memory the library allocates. It is loaded with the library
+// (with CUDA's lazy module loading, on first use) and every GPU that loads the
+// library keeps it until the process exits. Its size caps the problem:
+// 3 * nblk <= kNoAllocMaxScalars.
+constexpr size_t kNoAllocMaxScalars = size_t(1) << 20;  // 8 MiB as FP64
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxScalars];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current (the host-side name is only a stand-in).
+static void *g_noalloc_addr[64];
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(void **out) {
+  int dev = 0;
+  DFM2G_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(DFM2G_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(DFM2G_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
+    g_noalloc_addr[dev] = ptr;
+  }
+  *out = g_noalloc_addr[dev];
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec) {
+  DFM2G_TRY(check_ilu(p, true, true));
+  if (!vec) return fail(DFM2G_ERR_ARG, "solve_precond_noalloc: null vector");
+  if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "prec must be F64 or F32");
+  const size_t n = (size_t)p->nblk * 3;
+  if (n > kNoAllocMaxScalars)
+    return fail(DFM2G_ERR_ARG,
+                "solve_precond_noalloc: %zu unknowns exceed the fixed scratch of %zu (at most %zu 3x3 block rows); "
+                "use dfm2g_ilu_solve_precond for larger systems",
+                n, kNoAllocMaxScalars, kNoAllocMaxScalars / 3);
+  if (prec == DFM2G_F32 && !p->f32_valid)
+    return fail(DFM2G_ERR_STATE,
+                "solve_precond_noalloc: no FP32 factors yet (creating them allocates); call "
+                "dfm2g_ilu_solve_precond once with DFM2G_F32 first");
+  void *scratch = nullptr;
+  DFM2G_TRY(ensure_context());
+  DFM2G_TRY(noalloc_scratch(&scratch));
+  // forward: vec -> scratch; backward: scratch -> vec. Each sweep first fills
+  // its own output (the pending marker in the sync-free schedule, a copy of
+  // its input in the level schedule), so no scratch content carries over
+  // from an earlier call.
+  DFM2G_TRY(ilu_sweep(p, prec, true, vec, scratch));
+  DFM2G_TRY(ilu_sweep(p, prec, false, scratch, vec));
   return read_err(p);
 }
 

@@ -144,6 +144,18 @@ DFM2G_API int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular);
 DFM2G_API int dfm2g_ilu_forward(dfm2g_ilu p, int prec, void *vec, int mem);
 DFM2G_API int dfm2g_ilu_backward(dfm2g_ilu p, int prec, void *vec, int mem);
 DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem);
+/* SolvePrecond that allocates nothing (no counterpart in the reference).
+ * For callers that cannot allocate device memory while they solve: an
+ * application that reserves all GPU memory up front, or a frame loop that must
+ * not pay for cudaMalloc/cudaFree (cudaFree synchronises the whole device).
+ * `vec` must be in device memory (in/out). The intermediate vector between
+ * the two sweeps lives in one fixed array inside the library (8 MiB), which
+ * every GPU that loads the library keeps until the process exits; so
+ * 3*nblk may not exceed 1,048,576 (DFM2G_ERR_ARG otherwise). The first call on
+ * a device looks up that array's device address. All calls share the array:
+ * calls that overlap on the GPU (other streams, other threads) race. FP32 needs
+ * FP32 factors made earlier by a DFM2G_F32 dfm2g_ilu_solve_precond call. */
+DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
