@@ -92,6 +92,7 @@ SIGNATURES = {
     "dfm2g_solve_pcg": [_vp, _vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
     "dfm2g_solve_cg": [_vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
     "dfm2g_solve_pcg_mixed": [_vp, _vp, _vp, _vp, _d, _d, _u, _u, _i, _pstats],
+    "dfm2g_solve_pcg_mixed_reliable": [_vp, _vp, _vp, _vp, _d, _d, _u, _i, _pstats],
     "dfm2g_tetmesh_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz],
     "dfm2g_tetmesh_destroy": [_vp],
     "dfm2g_tetmesh_info": [_vp, _pu, _psz],

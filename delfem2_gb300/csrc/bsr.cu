@@ -8,59 +8,28 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "rowkern.cuh"
 
 namespace dfm2g {
 
 // ---------------------------------------------------------------------------
-// SpMV y = alpha*K*x + beta*y. One warp per block row (grid-stride). The row's
-// off-diagonal values are one contiguous run of 9*(s1-s0) scalars: lane l
-// reads scalars l, l+32, ... (coalesced), each scalar's block column comes from
-// a per-lane register of col[] via a shuffle, and the three row sums are
-// reduced with xor shuffles. The 3x3 diagonal block is handled by lanes 0-8.
+// SpMV y = alpha*K*x + beta*y, one warp per block row (rows w, w+W, ...), in
+// the lane layout of rowkern.cuh (off-diagonal blocks, then the diagonal as
+// the row's last block). Software-pipelined: the next row's block columns and
+// values are requested before the current row's x entries are gathered, and
+// the row offsets two rows ahead before that.
 template <typename T>
 __global__ void __launch_bounds__(256) k_bsr_spmv(unsigned nblk, const unsigned *__restrict__ row_start,
                                                   const unsigned *__restrict__ col,
                                                   const T *__restrict__ vcrs, const T *__restrict__ vdia,
                                                   T *__restrict__ y, T alpha, const T *__restrict__ x, T beta) {
   const unsigned lane = threadIdx.x & 31;
-  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
-  for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nblk; row += nwarp) {
-    const unsigned s0 = row_start[row], s1 = row_start[row + 1];
-    T a0 = 0, a1 = 0, a2 = 0;
-    for (unsigned cb = s0; cb < s1; cb += 32) {
-      const unsigned nb = min(32u, s1 - cb);
-      const unsigned my_col = lane < nb ? col[cb + lane] : 0u;
-      const size_t e_begin = (size_t)cb * 9, e_end = e_begin + (size_t)nb * 9;
-      for (size_t base = e_begin; base < e_end; base += 32) {
-        const size_t e = base + lane;
-        const bool ok = e < e_end;
-        const unsigned loc = ok ? (unsigned)(e - e_begin) : 0u;
-        const unsigned b = loc / 9u, rem = loc - b * 9u, r = rem / 3u, c = rem - r * 3u;
-        const unsigned j = __shfl_sync(0xffffffffu, my_col, b);
-        if (ok) {
-          const T v = vcrs[e] * x[(size_t)j * 3 + c];
-          a0 += (r == 0) ? v : T(0);
-          a1 += (r == 1) ? v : T(0);
-          a2 += (r == 2) ? v : T(0);
-        }
-      }
-    }
-    if (lane < 9) {
-      const unsigned r = lane / 3u, c = lane - r * 3u;
-      const T v = vdia[(size_t)row * 9 + lane] * x[(size_t)row * 3 + c];
-      a0 += (r == 0) ? v : T(0);
-      a1 += (r == 1) ? v : T(0);
-      a2 += (r == 2) ? v : T(0);
-    }
-    a0 = warp_sum(a0);
-    a1 = warp_sum(a1);
-    a2 = warp_sum(a2);
+  spmv_rows(nblk, row_start, col, vcrs, vdia, x, [&](unsigned row, const T s[3]) {
     if (lane < 3) {
-      const T s = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
       T *py = y + (size_t)row * 3 + lane;
-      *py = beta * *py + alpha * s;
+      *py = beta * *py + alpha * pick3(s, lane);
     }
-  }
+  });
 }
 
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta) {

@@ -237,6 +237,7 @@ struct dfm2g_ilu_s {
   dfm2g::DevBuf<float> vcrs32, vdia32;
   // level sets: level[i], order (rows by (level,row)), level_start (nlev+1)
   dfm2g::DevBuf<unsigned> level_f, order_f, lstart_f, level_b, order_b, lstart_b;
+  dfm2g::DevBuf<uint4> meta_f, meta_b;  // per position of the level order: {row, s0, s1, 0}
   unsigned nlev_f = 0, nlev_b = 0;
   std::vector<unsigned> h_lstart_f, h_lstart_b;
   // scratch for the sweeps (sentinel-filled outputs) and the device error word

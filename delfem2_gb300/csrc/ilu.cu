@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "rowkern.cuh"
 
 namespace dfm2g {
 
@@ -224,6 +225,9 @@ static int radix_sort_levels(unsigned n, const unsigned *level, unsigned max_key
   return DFM2G_OK;
 }
 
+__global__ void k_sweep_meta(unsigned n, const unsigned *__restrict__ order, const unsigned *__restrict__ row_start,
+                             const unsigned *__restrict__ dia_ind, int backward, uint4 *__restrict__ meta);
+
 static int compute_levels(dfm2g_ilu_s *p, bool backward) {
   const unsigned n = p->nblk;
   DevBuf<unsigned> &level = backward ? p->level_b : p->level_f;
@@ -264,6 +268,13 @@ static int compute_levels(dfm2g_ilu_s *p, bool backward) {
     DFM2G_CUDA(cudaStreamSynchronize(stream()));
   } else {
     hl.assign(1, 0);
+  }
+  DevBuf<uint4> &meta = backward ? p->meta_b : p->meta_f;
+  DFM2G_TRY(meta.resize((size_t)n + 1));
+  if (n) {
+    k_sweep_meta<<<blocks_for(n, 256, ctx().num_sms * 8), 256, 0, stream()>>>(n, order.p, p->row_start.p, p->dia_ind.p,
+                                                                              backward ? 1 : 0, meta.p);
+    DFM2G_LAUNCH_CHECK();
   }
   (backward ? p->nlev_b : p->nlev_f) = nlev;
   return DFM2G_OK;
@@ -378,104 +389,122 @@ __global__ void __launch_bounds__(256) k_ilu_factor_level(const unsigned *__rest
 
 // ---------------------------------------------------------------------------
 // Sweeps. Forward: out_i = D_i^-1 (in_i - sum_{j<i} L_ij out_j). Backward:
-// out_i = in_i - sum_{j>i} U'_ij out_j. One warp per row; the row's run of
-// 9*(#blocks) scalars is read coalesced, as in the SpMV.
-template <typename T, bool FWD>
-__device__ __forceinline__ void sweep_row(unsigned i, unsigned lane, const unsigned *__restrict__ row_start,
-                                          const unsigned *__restrict__ col, const unsigned *__restrict__ dia_ind,
-                                          const T *__restrict__ vcrs, const T *__restrict__ vdia, const T *in, T *out,
-                                          bool wait, int *err, unsigned long long timeout_ns) {
-  const unsigned s0 = FWD ? row_start[i] : dia_ind[i];
-  const unsigned s1 = FWD ? dia_ind[i] : row_start[i + 1];
-  T a0 = 0, a1 = 0, a2 = 0;
-  for (unsigned cb = s0; cb < s1; cb += 32) {
-    const unsigned nb = min(32u, s1 - cb);
-    const unsigned my_col = lane < nb ? col[cb + lane] : 0u;
-    const size_t e_begin = (size_t)cb * 9, e_end = e_begin + (size_t)nb * 9;
-    for (size_t base = e_begin; base < e_end; base += 32) {
-      const size_t e = base + lane;
-      const bool ok = e < e_end;
-      const unsigned loc = ok ? (unsigned)(e - e_begin) : 0u;
-      const unsigned b = loc / 9u, rem = loc - b * 9u, r = rem / 3u, c = rem - r * 3u;
-      const unsigned j = __shfl_sync(0xffffffffu, my_col, b);
-      if (ok) {
-        const T a = vcrs[e];
-        T xv;
-        if (wait) {
-          const T *px = out + (size_t)j * 3 + c;
-          xv = ld_relaxed(px);
-          if (is_pending(xv)) {
-            const unsigned long long t0 = globaltimer_ns();
-            unsigned spins = 0;
-            while (is_pending(xv = ld_relaxed(px))) {
-              if ((++spins & 15u) == 0 &&
-                  (ld_relaxed(err) != 0 || globaltimer_ns() - t0 > timeout_ns)) {
-                atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
-                xv = T(0);
-                break;
-              }
-            }
-          }
-        } else {
-          xv = out[(size_t)j * 3 + c];
-        }
-        const T v = a * xv;
-        a0 += (r == 0) ? v : T(0);
-        a1 += (r == 1) ? v : T(0);
-        a2 += (r == 2) ? v : T(0);
-      }
-    }
-  }
-  a0 = warp_sum(a0);
-  a1 = warp_sum(a1);
-  a2 = warp_sum(a2);
-  if (lane < 3) {
-    const T t0 = in[(size_t)i * 3 + 0] - a0;
-    const T t1 = in[(size_t)i * 3 + 1] - a1;
-    const T t2 = in[(size_t)i * 3 + 2] - a2;
-    T z;
-    if (FWD) {
-      const T *d = vdia + (size_t)i * 9 + lane * 3;
-      z = d[0] * t0 + d[1] * t1 + d[2] * t2;
-    } else {
-      z = lane == 0 ? t0 : (lane == 1 ? t1 : t2);
-    }
-    if (wait) st_relaxed(out + (size_t)i * 3 + lane, z);
-    else out[(size_t)i * 3 + lane] = z;
+// out_i = in_i - sum_{j>i} U'_ij out_j. One warp per row in the lane layout of
+// rowkern.cuh. Rows are visited in level order through per-position
+// metadata meta[q] = {row, first block, end block} (one 16-byte load), so a
+// warp can request its next row's blocks and right-hand side before it starts
+// waiting for the current row's dependencies.
+__global__ void k_sweep_meta(unsigned n, const unsigned *__restrict__ order, const unsigned *__restrict__ row_start,
+                             const unsigned *__restrict__ dia_ind, int backward, uint4 *__restrict__ meta) {
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const unsigned i = order[q];
+    const unsigned s0 = backward ? dia_ind[i] : row_start[i];
+    const unsigned s1 = backward ? row_start[i + 1] : dia_ind[i];
+    meta[q] = make_uint4(i, s0, s1, 0u);
   }
 }
 
+template <typename T>
+struct SweepRow {
+  static constexpr unsigned kRounds = 4;  // 12 blocks of one triangle in registers
+  RowFrag<T, kRounds> f;
+  unsigned i, s0, s1;
+  T in[3];  // lanes 0..2: the row's right-hand side
+  T d[3];   // lanes 0..2: row `lane` of D_i^-1 (forward only)
+};
+
 template <typename T, bool FWD>
-__global__ void __launch_bounds__(256) k_sweep_level(const unsigned *__restrict__ rows, unsigned nrows,
-                                                     const unsigned *__restrict__ row_start,
-                                                     const unsigned *__restrict__ col,
-                                                     const unsigned *__restrict__ dia_ind, const T *__restrict__ vcrs,
-                                                     const T *__restrict__ vdia, const T *in, T *out,
-                                                     const int *skip) {
+__device__ __forceinline__ void sweep_load(SweepRow<T> &R, const RowLane &L, unsigned lane, uint4 m,
+                                           const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                           const T *__restrict__ vdia, const T *in) {
+  R.i = m.x;
+  R.s0 = m.y;
+  R.s1 = m.z;
+  row_load(R.f, L, m.y, m.z, col, vcrs, ~0u, (const T *)nullptr);
+  if (lane < 3) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) R.in[k] = in[(size_t)m.x * 3 + k];
+    if (FWD) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) R.d[k] = vdia[(size_t)m.x * 9 + lane * 3 + k];
+    }
+  }
+}
+
+template <typename T, bool FWD, bool WAIT>
+__device__ __forceinline__ void sweep_finish(const SweepRow<T> &R, const RowLane &L, unsigned lane,
+                                             const unsigned *__restrict__ col, const T *__restrict__ vcrs, T *out,
+                                             int *err, unsigned long long timeout_ns) {
+  T acc;
+  if (R.f.nb <= 3 * SweepRow<T>::kRounds)
+    acc = WAIT ? row_dot_wait(R.f, L, out, err, timeout_ns) : row_dot(R.f, L, out);
+  else
+    acc = WAIT ? row_dot_wait_long(L, R.s0, R.s1, col, vcrs, out, err, timeout_ns)
+               : row_dot_long(L, R.s0, R.s1, col, vcrs, ~0u, (const T *)nullptr, out);
+  T s[3];
+  row_reduce(acc, s);
+  if (lane < 3) {
+    const T t0 = R.in[0] - s[0], t1 = R.in[1] - s[1], t2 = R.in[2] - s[2];
+    T z;
+    if (FWD)
+      z = R.d[0] * t0 + R.d[1] * t1 + R.d[2] * t2;
+    else
+      z = lane == 0 ? t0 : (lane == 1 ? t1 : t2);
+    if (WAIT)
+      st_relaxed(out + (size_t)R.i * 3 + lane, z);
+    else
+      out[(size_t)R.i * 3 + lane] = z;
+  }
+}
+
+// One level: rows meta[0..nrows) are independent; `out` holds the input for
+// rows not yet swept (in place), the results of earlier levels otherwise.
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(256) k_sweep_level(const uint4 *__restrict__ meta, unsigned nrows,
+                                                     const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                                     const T *__restrict__ vdia, T *out, const int *skip) {
   const unsigned lane = threadIdx.x & 31;
   const unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= nrows || (skip && *skip)) return;
-  sweep_row<T, FWD>(rows[w], lane, row_start, col, dia_ind, vcrs, vdia, in, out, false, nullptr, 0);
+  const RowLane L(lane);
+  SweepRow<T> R;
+  sweep_load<T, FWD>(R, L, lane, meta[w], col, vcrs, vdia, out);
+  sweep_finish<T, FWD, false>(R, L, lane, col, vcrs, out, nullptr, 0);
 }
 
 // Sync-free sweep: one persistent, co-resident (cooperative) grid; warp w
 // takes positions w, w+W, ... of the level order, and waits (bounded) on each
 // needed out_j until it is no longer the pending marker. Every row depends only
 // on rows earlier in the order and each warp walks its positions in order, so
-// the earliest unfinished position can always proceed.
+// the earliest unfinished position can always proceed. Pipelined: the next
+// position's row is loaded before the current one's wait, and the metadata
+// of the one after that before the current row is finished.
 template <typename T, bool FWD>
-__global__ void __launch_bounds__(256) k_sweep_syncfree(unsigned nblk, const unsigned *__restrict__ order,
-                                                        const unsigned *__restrict__ row_start,
+__global__ void __launch_bounds__(256) k_sweep_syncfree(unsigned n, const uint4 *__restrict__ meta,
                                                         const unsigned *__restrict__ col,
-                                                        const unsigned *__restrict__ dia_ind,
                                                         const T *__restrict__ vcrs, const T *__restrict__ vdia,
                                                         const T *in, T *out, int *err,
                                                         unsigned long long timeout_ns, const int *skip) {
   if (skip && *skip) return;
   const unsigned lane = threadIdx.x & 31;
+  const RowLane L(lane);
   const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
-  for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nblk; q += nwarp)
-    sweep_row<T, FWD>(order[q], lane, row_start, col, dia_ind, vcrs, vdia, in, out, true, err, timeout_ns);
+  unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= n) return;
+  SweepRow<T> cur, nxt;
+  sweep_load<T, FWD>(cur, L, lane, meta[q], col, vcrs, vdia, in);
+  uint4 m1 = (q + nwarp < n) ? meta[q + nwarp] : make_uint4(0u, 0u, 0u, 0u);
+  for (;;) {
+    const unsigned q1 = q + nwarp;
+    if (q1 < n) sweep_load<T, FWD>(nxt, L, lane, m1, col, vcrs, vdia, in);
+    const unsigned q2 = q1 + nwarp;
+    const uint4 m2 = (q2 < n) ? meta[q2] : make_uint4(0u, 0u, 0u, 0u);
+    sweep_finish<T, FWD, true>(cur, L, lane, col, vcrs, out, err, timeout_ns);
+    if (q1 >= n) break;
+    q = q1;
+    cur = nxt;
+    m1 = m2;
+  }
 }
 
 template <typename T>
@@ -508,16 +537,14 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
       DFM2G_LAUNCH_CHECK();
     }
     const std::vector<unsigned> &ls = forward ? p->h_lstart_f : p->h_lstart_b;
-    const unsigned *order = forward ? p->order_f.p : p->order_b.p;
+    const uint4 *meta = forward ? p->meta_f.p : p->meta_b.p;
     for (size_t l = 0; l + 1 < ls.size(); ++l) {
       const unsigned nrows = ls[l + 1] - ls[l];
       const unsigned blocks = blocks_for((size_t)nrows * 32, 256);
       if (forward)
-        k_sweep_level<T, true><<<blocks, 256, 0, stream()>>>(order + ls[l], nrows, p->row_start.p, p->col.p,
-                                                            p->dia_ind.p, vcrs, vdia, out, out, skip);
+        k_sweep_level<T, true><<<blocks, 256, 0, stream()>>>(meta + ls[l], nrows, p->col.p, vcrs, vdia, out, skip);
       else
-        k_sweep_level<T, false><<<blocks, 256, 0, stream()>>>(order + ls[l], nrows, p->row_start.p, p->col.p,
-                                                             p->dia_ind.p, vcrs, vdia, out, out, skip);
+        k_sweep_level<T, false><<<blocks, 256, 0, stream()>>>(meta + ls[l], nrows, p->col.p, vcrs, vdia, out, skip);
     }
     note_launches((unsigned)(ls.size() - 1) + (in != out ? 1u : 0u));
     DFM2G_LAUNCH_CHECK();
@@ -532,12 +559,12 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
   DFM2G_TRY(coop_blocks<T>(kernel, cache));
   const unsigned want = blocks_for((size_t)n * 32, 256);
   const unsigned blocks = std::min<unsigned>(want, (unsigned)*cache);
-  const unsigned *order = forward ? p->order_f.p : p->order_b.p;
+  const uint4 *meta = forward ? p->meta_f.p : p->meta_b.p;
   const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
   unsigned long long timeout = kWaitTimeoutNs + 20000ull * nlev;
   int *err = p->err.p;
-  void *args[] = {(void *)&n, (void *)&order, (void *)&p->row_start.p, (void *)&p->col.p, (void *)&p->dia_ind.p,
-                  (void *)&vcrs, (void *)&vdia, (void *)&in, (void *)&out, (void *)&err, (void *)&timeout, (void *)&skip};
+  void *args[] = {(void *)&n, (void *)&meta, (void *)&p->col.p, (void *)&vcrs, (void *)&vdia, (void *)&in,
+                  (void *)&out, (void *)&err, (void *)&timeout, (void *)&skip};
   DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(256), args, 0, stream()));
   note_launches(1);
   return DFM2G_OK;

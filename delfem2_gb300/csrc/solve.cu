@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "rowkern.cuh"
 
 namespace dfm2g {
 
@@ -26,18 +27,28 @@ struct IterState {
   int done;        // 0 running, 1 converged, 2 exhausted, 3 |r0|^2 < 1e-30, 4 non-finite
   unsigned nhist;
   unsigned hist_cap;
-  int mode;        // 0 PCG (absolute history), 1 CG (relative history)
+  int mode;        // 0 PCG (absolute history), 1 CG (relative history), 2 reliable-update PCG
   unsigned ticket[4];
+  // reliable-update refinement (mode 2)
+  double bnorm;    // |b|
+  double delta;    // refresh the FP64 residual when |r| < delta * rmax
+  double rmax;     // |r| at the last refresh
+  double rtrue;    // |b - K x| at the last refresh
+  int update;      // a refresh is due in this iteration
+  unsigned n_updates;
+  // The FP32 vectors hold scale * (FP64 quantity), with scale = 1/|r| reset at
+  // every refresh, so they stay O(1/sqrt(n)) however small the residual gets
+  // (unscaled, (r,z) and (p,Ap) underflow FP32 near 1e-10 on fine meshes).
+  double scale;       // scale of the current FP32 segment
+  double scale_next;  // scale chosen for the segment after this refresh
+  double ratio;       // scale_new / scale_old, folded into the next beta (1 otherwise)
+  int restart_p;      // the refreshed residual disagrees with the recursive one: p = z
 };
 
 constexpr int kThreads = 256;
 
-template <typename T>
-struct Acc {
-  using type = double;
-};
-
-// p.Ap fused into the SpMV Ap = K p (warp per block row).
+// p.Ap fused into the SpMV Ap = K p (warp per block row); the last block sets
+// alpha = (r, Pr) / (p, Ap).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_spmv_pAp(IterState *st, unsigned nblk,
                                                        const unsigned *__restrict__ row_start,
@@ -47,48 +58,79 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pAp(IterState *st, unsigned n
   __shared__ double sh[32];
   if (st->done) return;
   const unsigned lane = threadIdx.x & 31;
-  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
   double dot = 0.0;
-  for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nblk; row += nwarp) {
-    const unsigned s0 = row_start[row], s1 = row_start[row + 1];
-    T a0 = 0, a1 = 0, a2 = 0;
-    for (unsigned cb = s0; cb < s1; cb += 32) {
-      const unsigned nb = min(32u, s1 - cb);
-      const unsigned my_col = lane < nb ? col[cb + lane] : 0u;
-      const size_t e_begin = (size_t)cb * 9, e_end = e_begin + (size_t)nb * 9;
-      for (size_t base = e_begin; base < e_end; base += 32) {
-        const size_t e = base + lane;
-        const bool ok = e < e_end;
-        const unsigned loc = ok ? (unsigned)(e - e_begin) : 0u;
-        const unsigned b = loc / 9u, rem = loc - b * 9u, r = rem / 3u, c = rem - r * 3u;
-        const unsigned j = __shfl_sync(0xffffffffu, my_col, b);
-        if (ok) {
-          const T v = vcrs[e] * p[(size_t)j * 3 + c];
-          a0 += (r == 0) ? v : T(0);
-          a1 += (r == 1) ? v : T(0);
-          a2 += (r == 2) ? v : T(0);
-        }
-      }
-    }
-    if (lane < 9) {
-      const unsigned r = lane / 3u, c = lane - r * 3u;
-      const T v = vdia[(size_t)row * 9 + lane] * p[(size_t)row * 3 + c];
-      a0 += (r == 0) ? v : T(0);
-      a1 += (r == 1) ? v : T(0);
-      a2 += (r == 2) ? v : T(0);
-    }
-    a0 = warp_sum(a0);
-    a1 = warp_sum(a1);
-    a2 = warp_sum(a2);
+  spmv_rows(nblk, row_start, col, vcrs, vdia, p, [&](unsigned row, const T s[3]) {
     if (lane < 3) {
-      const T s = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
-      Ap[(size_t)row * 3 + lane] = s;
-      dot += (double)(s * p[(size_t)row * 3 + lane]);
+      const T v = pick3(s, lane);
+      Ap[(size_t)row * 3 + lane] = v;
+      dot += (double)(v * p[(size_t)row * 3 + lane]);
     }
-  }
+  });
   double total;
   if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
     st->alpha = st->rPr / total;
+  }
+}
+
+// Reliable update, part 1: x64 += x32, x32 = 0 (only when a refresh is due).
+__global__ void k_flush_x(const IterState *st, size_t n, double *__restrict__ x64, float *__restrict__ x32) {
+  if (st->done || !st->update) return;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    x64[i] += (double)x32[i] / st->scale;
+    x32[i] = 0.f;
+  }
+}
+
+// Reliable update, part 2: r64 = b - K64 x64 in FP64, r32 = (float) r64, and
+// |r64| decides convergence (|r64| < tol |b|) or the next refresh threshold.
+__global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsigned nblk,
+                                                            const unsigned *__restrict__ row_start,
+                                                            const unsigned *__restrict__ col,
+                                                            const double *__restrict__ vcrs,
+                                                            const double *__restrict__ vdia,
+                                                            const double *__restrict__ x64,
+                                                            const double *__restrict__ b, float *__restrict__ r32,
+                                                            double *partials) {
+  __shared__ double sh[32];
+  if (st->done || !st->update) return;
+  __shared__ double sh2[32];
+  const unsigned lane = threadIdx.x & 31;
+  const double sc = st->scale_next, inv_old = 1.0 / st->scale;
+  double rr = 0.0, dd = 0.0;
+  spmv_rows(nblk, row_start, col, vcrs, vdia, x64, [&](unsigned row, const double s[3]) {
+    if (lane < 3) {
+      const size_t k = (size_t)row * 3 + lane;
+      const double r = b[k] - pick3(s, lane);
+      const double gap = r - (double)r32[k] * inv_old;  // true minus recursive residual
+      r32[k] = (float)(r * sc);
+      rr += r * r;
+      dd += gap * gap;
+    }
+  });
+  // |true - recursive|^2: block sums go to partials[gridDim.x + block] (written
+  // before grid_sum_last's fence), the last block adds them in block order
+  dd = block_sum(dd, sh2);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = dd;
+  double total;
+  if (grid_sum_last(rr, partials, &st->ticket[3], sh, &total)) {
+    const double rt = sqrt(total);
+    double gap2 = 0.0;
+    for (unsigned b2 = 0; b2 < gridDim.x; ++b2) gap2 += ld_relaxed(partials + gridDim.x + b2);
+    st->restart_p = sqrt(gap2) > 0.5 * rt ? 1 : 0;
+    st->rtrue = rt;
+    st->update = 0;
+    st->n_updates++;
+    if (!isfinite(rt)) {
+      st->done = 4;
+    } else if (rt < st->tol * st->bnorm) {
+      st->done = 1;
+    } else if (st->it >= st->max_iter) {
+      st->done = 2;
+    } else {
+      st->rmax = rt;
+    }
+    st->ratio = st->scale_next / st->scale;
+    st->scale = st->scale_next;
   }
 }
 
@@ -130,6 +172,19 @@ __global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T 
     st->rr = total;
     const unsigned it = st->it + 1;
     st->it = it;
+    if (st->mode == 2) {  // reliable updates: the FP64 refresh decides convergence
+      const double rn_scaled = sqrt(total);
+      const double rn = rn_scaled / st->scale;
+      if (st->nhist < st->hist_cap) hist[st->nhist] = rn;
+      st->nhist++;
+      if (!isfinite(total)) {
+        st->done = 4;
+      } else if (rn < st->delta * st->rmax || rn < st->tol * st->bnorm || it >= st->max_iter) {
+        st->update = 1;
+        st->scale_next = rn_scaled > 0.0 ? st->scale / rn_scaled : st->scale;
+      }
+      return;
+    }
     const double ratio = sqrt(total * st->inv_rr0);
     const double entry = st->mode == 0 ? sqrt(total) : ratio;
     if (st->nhist < st->hist_cap) hist[st->nhist] = entry;
@@ -175,8 +230,12 @@ __global__ void __launch_bounds__(kThreads) k_dot_beta(IterState *st, size_t n, 
   s += (double)acc;
   double total;
   if (grid_sum_last(s, partials, &st->ticket[2], sh, &total)) {
-    st->beta = total / st->rPr;
+    // after a rescale of the FP32 vectors, the old p and (r,Pr) are in the old
+    // scale: p_new = z + rPr1/(rPr*ratio^2) * (ratio*p) = z + rPr1/(rPr*ratio) * p
+    st->beta = st->restart_p ? 0.0 : total / (st->rPr * st->ratio);
     st->rPr = total;
+    st->ratio = 1.0;
+    st->restart_p = 0;
   }
 }
 
@@ -227,7 +286,7 @@ __global__ void k_init_state(IterState *st, const double *scal, double *hist, in
     if (st->hist_cap > 0) hist[0] = sqrt(rr0);
     st->nhist = 1;
   }
-  if (rr0 < 1.0e-30) {
+  if (mode == 2 ? !(rr0 > 0.0) : rr0 < 1.0e-30) {  // the refinement has no absolute floor
     st->done = 3;
     return;
   }
@@ -236,7 +295,7 @@ __global__ void k_init_state(IterState *st, const double *scal, double *hist, in
     return;
   }
   st->inv_rr0 = 1.0 / rr0;
-  st->rPr = mode == 0 ? scal[1] : rr0;
+  st->rPr = mode != 1 ? scal[1] : rr0;
   if (st->max_iter == 0) {  // no iteration: Solve_PCG still appends the final |r|
     if (mode == 0) {
       if (st->nhist < st->hist_cap) hist[st->nhist] = sqrt(rr0);
@@ -312,25 +371,44 @@ static int dot_host(size_t n, const void *a, const void *b, int prec, double *ou
 //  r: rhs in, final residual out; x: solution out (starts at 0);
 //  w0..w3: scratch vectors (Pr/Ap share w0 as in the reference, p = w1,
 //  sweep intermediate = w2).
+// Reliable-update refinement (mode 2, T = float): `r` holds (float)b and `x`
+// the FP32 correction on entry; x64 accumulates the solution in FP64 and the
+// true residual b - K x64 is recomputed in FP64 whenever the FP32 residual has
+// dropped by `delta` since the last refresh (the Krylov state p is kept).
+struct Refine {
+  double *x64 = nullptr;
+  const double *b64 = nullptr;
+  double delta = 0, bnorm = 0;
+};
+
 template <typename T>
 static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T *w2, double tol,
-                    unsigned max_iter, unsigned hist_cap, int mode, IterState *h_state) {
+                    unsigned max_iter, unsigned hist_cap, int mode, IterState *h_state,
+                    const Refine &rf = Refine()) {
   const int prec = sizeof(T) == 8 ? DFM2G_F64 : DFM2G_F32;
   const unsigned nblk = m->nblk;
   const size_t n = (size_t)nblk * 3;
   const T *vcrs = sizeof(T) == 8 ? (const T *)m->vcrs.p : (const T *)m->vcrs32.p;
   const T *vdia = sizeof(T) == 8 ? (const T *)m->vdia.p : (const T *)m->vdia32.p;
+  if (mode == 2 && sizeof(T) != 4) return fail(DFM2G_ERR_ARG, "reliable-update PCG runs in FP32");
   IterState init{};
   init.tol = tol;
   init.max_iter = max_iter;
   init.hist_cap = hist_cap;
   init.mode = mode;
+  init.bnorm = rf.bnorm;
+  init.delta = rf.delta;
+  init.rmax = rf.bnorm;
+  init.rtrue = rf.bnorm;
+  init.ratio = 1.0;
+  init.scale = (mode == 2 && rf.bnorm > 0) ? 1.0 / rf.bnorm : 1.0;
+  init.scale_next = init.scale;
   IterState *st = g_ws.st.p;
   DFM2G_CUDA(cudaMemcpyAsync(st, &init, sizeof(init), cudaMemcpyHostToDevice, stream()));
   DFM2G_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * n, stream()));
   DFM2G_TRY(dot_dev(n, r, r, prec, g_ws.scal.p + 0));
   T *Pr = w0, *pv = w1, *mid = w2;
-  if (mode == 0) {
+  if (mode != 1) {
     // Pr = M^-1 r ; p = Pr ; rPr = (r, Pr)
     DFM2G_TRY(ilu_sweep(p, prec, true, r, mid));
     DFM2G_TRY(ilu_sweep(p, prec, false, mid, Pr));
@@ -357,7 +435,16 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
         ProfScope ps(DFM2G_PROF_UPDATE, 1);
         k_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, x, pv, Ap, g_ws.partials.p, g_ws.hist.p);
       }
-      if (mode == 0) {
+      if constexpr (sizeof(T) == 4) {
+        if (mode == 2) {
+          ProfScope ps(DFM2G_PROF_OUTER, 2);
+          k_flush_x<<<vec_blocks, kThreads, 0, stream()>>>(st, n, rf.x64, (float *)x);
+          k_true_residual<<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p, m->vcrs.p,
+                                                                  m->vdia.p, rf.x64, rf.b64, (float *)r,
+                                                                  g_ws.partials.p);
+        }
+      }
+      if (mode != 1) {
         if (p->sweep_mode == DFM2G_SWEEP_SYNCFREE) {
           ProfScope ps(DFM2G_PROF_FILL, 2);
           k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, mid);
@@ -497,6 +584,58 @@ int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_i
   }
   if (hs.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_cg: non-finite residual");
   if (hs.done == 2) return fail(DFM2G_ERR_NOT_CONVERGED, "solve_cg: %u iterations without reaching tol", max_iter);
+  return DFM2G_OK;
+}
+
+int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, double tol, double delta,
+                                   unsigned max_iter, int mem, dfm2g_solve_stats *stats) {
+  DFM2G_TRY(check_pair(m, p));
+  if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null preconditioner");
+  if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null vector");
+  if (!(delta > 0 && delta < 1)) return fail(DFM2G_ERR_ARG, "delta must be in (0,1)");
+  const size_t n = (size_t)m->nblk * 3;
+  DFM2G_TRY(ws_prepare(n, max_iter + 4, true));
+  DFM2G_TRY(bsr_ensure_f32(m));
+  DFM2G_TRY(ilu_ensure_f32(p));
+  VecArg<double> ab, ax;
+  DFM2G_TRY(ab.in(b, n, mem, true));
+  DFM2G_TRY(ax.in(x, n, mem, false));
+  float *r32 = g_ws.v32[3].p, *x32 = g_ws.v32[4].p;
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev0, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(ax.dev(), 0, sizeof(double) * n, stream()));
+  double bb = 0;
+  DFM2G_TRY(dot_host(n, ab.dev(), ab.dev(), DFM2G_F64, &bb));
+  const double bnorm = std::sqrt(bb);
+  IterState hs{};
+  if (bnorm > 0) {
+    {
+      ProfScope ps(DFM2G_PROF_OUTER, 1);
+      k_scale_convert<float><<<reduce_blocks(), kThreads, 0, stream()>>>(n, ab.dev(), 1.0 / bnorm, r32);
+    }
+    DFM2G_LAUNCH_CHECK();
+    Refine rf;
+    rf.x64 = ax.dev();
+    rf.b64 = ab.dev();
+    rf.delta = delta;
+    rf.bnorm = bnorm;
+    DFM2G_TRY(pcg_core<float>(m, p, r32, x32, g_ws.v32[0].p, g_ws.v32[1].p, g_ws.v32[2].p, tol, max_iter,
+                              max_iter + 4, 2, &hs, rf));
+  }
+  DFM2G_CUDA(cudaEventRecord(g_ws.ev1, stream()));
+  DFM2G_TRY(ax.copy_back());
+  if (stats) {
+    DFM2G_CUDA(cudaEventSynchronize(g_ws.ev1));
+    float ms = 0.f;
+    DFM2G_CUDA(cudaEventElapsedTime(&ms, g_ws.ev0, g_ws.ev1));
+    stats->ms = ms;
+    stats->iterations = hs.it;
+    stats->outer = hs.n_updates;
+    stats->rel_residual = bnorm > 0 ? hs.rtrue / bnorm : 0.0;
+  }
+  if (hs.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_pcg_mixed_reliable: non-finite residual");
+  if (hs.done == 2)
+    return fail(DFM2G_ERR_NOT_CONVERGED, "solve_pcg_mixed_reliable: stopped at relative residual %.3e",
+                hs.rtrue / bnorm);
   return DFM2G_OK;
 }
 

@@ -296,12 +296,22 @@ def Solve_CG(r_vec, u_vec, conv_ratio_tol: float, max_iteration: int, mat: CMatr
 
 def Solve_PCG_Mixed(b_vec, x_vec, tol: float, mat: CMatrixSparse, ilu: CPreconditionerILU,
                     inner_tol: float = 1e-4, max_iter: int = 100000, max_outer: int = 100,
-                    allow_not_converged: bool = False) -> N.SolveStats:
-    """FP32-inner / FP64-refinement PCG until |b - K x| / |b| < tol (b unchanged)."""
+                    allow_not_converged: bool = False, method: str = "restart") -> N.SolveStats:
+    """FP32-inner / FP64-refinement PCG until |b - K x| / |b| < tol (b unchanged).
+
+    method="reliable": one FP32 PCG whose residual is refreshed in FP64 each time
+    it has dropped by `inner_tol` (Krylov state kept); method="restart": classic
+    iterative refinement, a fresh FP32 PCG to `inner_tol` per FP64 step."""
     pb, mb, kb = _vec(b_vec, np.float64, False)
     px, mx, kx = _vec(x_vec, np.float64, True)
     st = N.SolveStats()
-    N.call("dfm2g_solve_pcg_mixed", mat._h, ilu._h, pb, px, float(tol), float(inner_tol), int(max_iter),
-           int(max_outer), _same_mem(mb, mx), C.byref(st),
-           allow=(N.ERR_NOT_CONVERGED,) if allow_not_converged else ())
+    allow = (N.ERR_NOT_CONVERGED,) if allow_not_converged else ()
+    if method == "reliable":
+        N.call("dfm2g_solve_pcg_mixed_reliable", mat._h, ilu._h, pb, px, float(tol), float(inner_tol),
+               int(max_iter), _same_mem(mb, mx), C.byref(st), allow=allow)
+    elif method == "restart":
+        N.call("dfm2g_solve_pcg_mixed", mat._h, ilu._h, pb, px, float(tol), float(inner_tol), int(max_iter),
+               int(max_outer), _same_mem(mb, mx), C.byref(st), allow=allow)
+    else:
+        raise ValueError(f"unknown method {method!r}")
     return st

@@ -88,7 +88,7 @@ class StaticElasticProblem:
         hist = Solve_PCG(r, x, tol, max_iter, self.K, self.ilu, stats)
         return x, hist
 
-    def solve_mixed(self, b, tol=1e-10, inner_tol=1e-4, max_iter=100000):
+    def solve_mixed(self, b, tol=1e-10, inner_tol=1e-4, max_iter=100000, method="restart"):
         x = b.new_zeros(b.shape) if hasattr(b, "new_zeros") else np.zeros_like(b)
-        st = Solve_PCG_Mixed(b, x, tol, self.K, self.ilu, inner_tol=inner_tol, max_iter=max_iter)
+        st = Solve_PCG_Mixed(b, x, tol, self.K, self.ilu, inner_tol=inner_tol, max_iter=max_iter, method=method)
         return x, st

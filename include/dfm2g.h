@@ -187,6 +187,17 @@ DFM2G_API int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, d
                                     double tol, double inner_tol, unsigned max_iter,
                                     unsigned max_outer, int mem, dfm2g_solve_stats *stats);
 
+/* Mixed precision with reliable updates: one FP32 PCG iteration (FP32 K and
+ * factors, FP64 alpha/beta reductions) whose FP32 iterate is flushed into the
+ * FP64 solution, and whose residual is replaced by the FP64 residual
+ * b - K x (FP64 values), each time the FP32 residual has dropped by `delta`
+ * since the last refresh; the search direction is kept across refreshes, so
+ * the iteration count stays close to the FP64 solve's. Stops when the FP64
+ * residual satisfies |b - K x|/|b| < tol. stats->outer = number of refreshes. */
+DFM2G_API int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x,
+                                             double tol, double delta, unsigned max_iter, int mem,
+                                             dfm2g_solve_stats *stats);
+
 /* ---- linear-tet elasticity ------------------------------------------------- */
 /* Builds, for mesh (xyz: 3*np, tet: 4*ntet, host arrays) against the pattern
  * of K: the element->slot map (device) and a greedy element colouring (no two

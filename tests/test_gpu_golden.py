@@ -66,16 +66,17 @@ def test_fp64_solve_matches_reference(big):
     assert abs(float(torch.linalg.norm(x)) - float(g["x_norm"])) <= 1e-9 * float(g["x_norm"])
 
 
-def test_mixed_solve_agrees_with_reference_to_1e8(big):
+@pytest.mark.parametrize("method", ["reliable", "restart"])
+def test_mixed_solve_agrees_with_reference_to_1e8(big, method):
     import torch
     import delfem2_gb300 as D
     name, a, P, b = big
     g = golden(name)
     x = torch.zeros_like(b)
-    st = D.Solve_PCG_Mixed(b, x, 1e-10, P.K, P.ilu, inner_tol=1e-4)
+    st = D.Solve_PCG_Mixed(b, x, 1e-10, P.K, P.ilu, inner_tol=1e-4, method=method)
     assert st.rel_residual < 1e-10
     xs = x.cpu().numpy()[g["idx"]]
     err = np.abs(xs - g["x_sample"]).max() / np.abs(g["x_sample"]).max()
-    print(f"{name}: mixed {st.iterations} inner / {st.outer} outer, rel res {st.rel_residual:.2e}, "
+    print(f"{name} {method}: mixed {st.iterations} inner / {st.outer} outer, rel res {st.rel_residual:.2e}, "
           f"sample err vs reference {err:.2e}")
     assert err <= 1e-8

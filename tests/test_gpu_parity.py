@@ -198,9 +198,10 @@ def test_solve_cg_matches_oracle(case, port):
     assert rel_err(x, xo) < 1e-6
 
 
-def test_mixed_precision_reaches_fp64_accuracy(case, port):
+@pytest.mark.parametrize("method", ["reliable", "restart"])
+def test_mixed_precision_reaches_fp64_accuracy(case, port, method):
     name, s, P, b = case
-    x, st = P.solve_mixed(b, tol=1e-10, inner_tol=1e-4)
+    x, st = P.solve_mixed(b, tol=1e-10, inner_tol=1e-4, method=method)
     xo, _, _ = port.solve_pcg(s["ind"], s["psup"], s["vc"], s["vd"], s["col"], s["dia"], s["ivc"], s["ivd"],
                               s["b"], 1e-13, 5000)
     assert st.rel_residual < 1e-10
