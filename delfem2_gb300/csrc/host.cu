@@ -169,7 +169,9 @@ const char *dfm2g_last_error(void) { return g_last_error.c_str(); }
 
 int dfm2g_set_stream(void *s) {
   DFM2G_TRY(ensure_context());
-  g_ctx.stream = s ? static_cast<cudaStream_t>(s) : g_ctx.own;
+  // NULL is CUDA's legacy default stream (torch's default stream), not the
+  // library's own non-blocking stream: work must order with the caller's.
+  g_ctx.stream = static_cast<cudaStream_t>(s);
   return DFM2G_OK;
 }
 

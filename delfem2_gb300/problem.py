@@ -77,6 +77,30 @@ class StaticElasticProblem:
         setRHS_Zero(b, bc)
         return b
 
+    def assemble_stiffness(self, young):
+        """K(E) with the clamp applied (no load); young: numpy or CUDA tensor of per-tet E."""
+        import torch
+        dev = young.device if hasattr(young, "device") else None
+        if dev is not None and dev.type == "cuda":
+            scratch = getattr(self, "_scratch_b", None)
+            if scratch is None or scratch.device != dev:
+                self._scratch_b = torch.zeros(self.ndof, dtype=torch.float64, device=dev)
+            b = self._scratch_b
+            b.zero_()
+        else:
+            b = np.zeros(self.ndof)
+        self.K.setZero()
+        self.mesh.assemble_linear(young, self.nu, 0.0, (0.0, 0.0, 0.0), b)
+        self.K.SetFixedBC(self.a["bc"])
+
+    def free_mask(self, like):
+        """1 on free DOFs, 0 on clamped ones, as a tensor/array like `like`."""
+        m = (self.a["bc"] == 0).astype(np.float64)
+        if hasattr(like, "device"):
+            import torch
+            return torch.from_numpy(m).to(like.device)
+        return m
+
     def factor(self) -> bool:
         self.ilu.CopyValue(self.K)
         return self.ilu.Decompose()

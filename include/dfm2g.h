@@ -70,7 +70,9 @@ typedef struct dfm2g_solve_stats {
 DFM2G_API int dfm2g_version(void);
 DFM2G_API const char *dfm2g_status_string(int status);
 DFM2G_API const char *dfm2g_last_error(void);
-/* Use `stream` (a cudaStream_t; NULL = the library's own stream). */
+/* Queue all further work on `stream` (a cudaStream_t; NULL = CUDA's legacy
+ * default stream). Until the first call the library uses a non-blocking
+ * stream of its own. */
 DFM2G_API int dfm2g_set_stream(void *stream);
 DFM2G_API int dfm2g_synchronize(void);
 

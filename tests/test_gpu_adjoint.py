@@ -1,0 +1,100 @@
+"""Adjoint gradients: GPU adjoint vs an FP64 CPU adjoint built from the oracle
+solver, and vs FP64 central finite differences on the 48^3 configuration.
+
+Tolerances: GPU vs CPU adjoint 1e-8 relative (both FP64 solves to 1e-13);
+adjoint vs finite differences (h = 1e-6) 1e-5 relative to max(|fd|, 1e-3 max|g|)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_adjoint_matches_cpu_adjoint(gpu, port):
+    import torch
+    import delfem2_gb300 as D
+    from delfem2_gb300.autograd import linear_elastic_solve
+    n = 8
+    a = D.voxel_problem_arrays(n, n, n, 1.0 / n, seed=4, e_range=(0.5, 2.0))
+    P = D.StaticElasticProblem(a)
+    E = torch.from_numpy(a["young"]).cuda().requires_grad_(True)
+    f = torch.from_numpy(np.random.default_rng(41).standard_normal(a["np"] * 3) * 1e-3).cuda().requires_grad_(True)
+    u_star = torch.from_numpy(np.random.default_rng(3).standard_normal(a["np"] * 3) * 1e-4).cuda()
+    u = linear_elastic_solve(E, f, P, "fp64", 1e-13)
+    L = 0.5 * torch.sum((u - u_star) ** 2)
+    L.backward()
+    # CPU: K(E) with the clamp, forward and adjoint Solve_PCG, element term
+    s = a
+    vc, vd, b = np.zeros(s["psup"].size * 9), np.zeros(s["np"] * 9), np.zeros(s["np"] * 3)
+    port.assemble_tet_linear(s["psup_ind"], s["psup"], vc, vd, b, s["xyz"], s["tet"], s["young"], 0.3, 0.0, [0, 0, 0])
+    port.set_fixed_bc(s["psup_ind"], s["psup"], vc, vd, s["bc"])
+    col, dia = port.ilu_pattern0(s["psup_ind"], s["psup"])
+    ivc, ivd = port.ilu_copy_value(s["psup_ind"], col, s["psup"], vc, vd)
+    port.ilu_decompose(s["psup_ind"], col, dia, ivc, ivd)
+    mask = (s["bc"] == 0).astype(np.float64)
+    fh = f.detach().cpu().numpy()
+    uc, _, _ = port.solve_pcg(s["psup_ind"], s["psup"], vc, vd, col, dia, ivc, ivd, fh * mask, 1e-13, 5000)
+    gu = uc - u_star.cpu().numpy()
+    lam, _, _ = port.solve_pcg(s["psup_ind"], s["psup"], vc, vd, col, dia, ivc, ivd, gu, 1e-13, 5000)
+    gE = port.tet_dLdE(s["xyz"], s["tet"], s["young"], 0.3, uc, lam * mask)
+    assert rel_err(u.detach().cpu().numpy(), uc) < 1e-9
+    assert rel_err(E.grad.cpu().numpy(), gE) < 1e-8
+    assert rel_err(f.grad.cpu().numpy(), lam * mask) < 1e-8
+
+
+def test_adjoint_vs_finite_differences_48cube(gpu):
+    import torch
+    from delfem2_gb300.check_adjoint import fd_loss_change, loss_and_grads, setup
+    from delfem2_gb300.autograd import linear_elastic_solve
+    a, P, E, E_t, f = setup(48)
+    with torch.no_grad():
+        u_star = linear_elastic_solve(E_t, f, P, "fp64", 1e-14)
+        u0 = linear_elastic_solve(E, f, P, "fp64", 1e-14)
+    L, gE_mixed, gf_mixed = loss_and_grads(P, E, f, u_star, "mixed")
+    L64, gE, gf = loss_and_grads(P, E, f, u_star, "fp64", 1e-14)
+    rng = np.random.default_rng(7)
+    h = 1e-6
+    sE, sf = float(gE.abs().max()), float(gf.abs().max())
+
+    def fd_loss(E_, f_):
+        return fd_loss_change(P, E_, f_, u0, u_star)
+
+    for e in rng.choice(a["ntet"], size=6, replace=False):
+        Ep, Em = E.clone(), E.clone()
+        Ep[e] += h
+        Em[e] -= h
+        fd = (fd_loss(Ep, f) - fd_loss(Em, f)) / (2 * h)
+        den = max(abs(fd), 1e-3 * sE)
+        assert abs(float(gE[e]) - fd) / den < 1e-5, (e, float(gE[e]), fd)
+        assert abs(float(gE_mixed[e]) - fd) / den < 1e-5, (e, float(gE_mixed[e]), fd)
+    free = np.nonzero(a["bc"] == 0)[0]
+    for i in rng.choice(free, size=6, replace=False):
+        fp, fm = f.clone(), f.clone()
+        fp[i] += h
+        fm[i] -= h
+        fd = (fd_loss(E, fp) - fd_loss(E, fm)) / (2 * h)
+        den = max(abs(fd), 1e-3 * sf)
+        assert abs(float(gf[i]) - fd) / den < 1e-5, (i, float(gf[i]), fd)
+        assert abs(float(gf_mixed[i]) - fd) / den < 1e-5, (i, float(gf_mixed[i]), fd)
+
+
+def test_backward_rebuilds_factors_after_another_forward(gpu):
+    import torch
+    import delfem2_gb300 as D
+    from delfem2_gb300.autograd import linear_elastic_solve
+    a = D.voxel_problem_arrays(6, 6, 6, 1 / 6, seed=4, e_range=(0.5, 2.0))
+    P = D.StaticElasticProblem(a)
+    E1 = torch.from_numpy(a["young"]).cuda().requires_grad_(True)
+    E2 = (E1.detach() * 1.7).requires_grad_(True)
+    f = torch.full((a["np"] * 3,), 1e-3, dtype=torch.float64, device="cuda")
+    u1 = linear_elastic_solve(E1, f, P, "fp64", 1e-13)
+    u2 = linear_elastic_solve(E2, f, P, "fp64", 1e-13)  # re-assembles K in P
+    u1.sum().backward()
+    g_late = E1.grad.clone()
+    E1.grad = None
+    u1b = linear_elastic_solve(E1, f, P, "fp64", 1e-13)
+    u1b.sum().backward()
+    assert torch.allclose(g_late, E1.grad, rtol=1e-9, atol=0)
+    # u scales as 1/E: u2 = u1 / 1.7
+    assert torch.allclose(u2 * 1.7, u1.detach(), rtol=1e-8, atol=1e-20)
