@@ -30,6 +30,7 @@ F64 = 0
 F32 = 1
 SWEEP_SYNCFREE = 0
 SWEEP_LEVELS = 1
+SWEEP_GROUPS = 2
 
 
 class SolveStats(C.Structure):
@@ -86,6 +87,7 @@ SIGNATURES = {
     "dfm2g_ilu_solve_precond": [_vp, _i, _vp, _i],
     "dfm2g_ilu_solve_precond_noalloc": [_vp, _i, _vp],
     "dfm2g_ilu_set_sweep_mode": [_vp, _i],
+    "dfm2g_ilu_get_sweep_mode": [_vp, _pi],
     "dfm2g_ilu_get_pattern": [_vp, _vp, _vp],
     "dfm2g_ilu_get_values": [_vp, _vp, _vp, _i],
     "dfm2g_ilu_get_levels": [_vp, _i, _vp, _vp, _vp, _pu],

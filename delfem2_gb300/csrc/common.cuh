@@ -227,6 +227,21 @@ struct dfm2g_bsr_s {
   unsigned pattern_version = 0;
 };
 
+// Blob schedule of one sweep direction (FP32): rows partitioned into compact
+// groups, one CTA per group; see groups.cu.
+struct GroupSched {
+  bool ok = false;
+  unsigned ngroups = 0, max_rows = 0, slot_bytes = 0, threads = 0, ring = 0;
+  size_t smem = 0, nvblocks = 0;
+  dfm2g::DevBuf<uint4> units;          // {byte offset, byte length, rows, 0}
+  dfm2g::DevBuf<unsigned> gunit;       // ngroups+1: first unit of each group
+  dfm2g::DevBuf<unsigned> growptr;     // ngroups+1: first position of each group in prow
+  dfm2g::DevBuf<unsigned> prow;        // rows in processing order
+  dfm2g::DevBuf<unsigned char> bytes;  // unit records (headers, dependency codes, values)
+  dfm2g::DevBuf<unsigned> vsrc, vdst;  // value blocks: source (slot, or nnz+row for D^-1), destination
+  bool values_ok = false;
+};
+
 struct dfm2g_ilu_s {
   unsigned nblk = 0;
   size_t nnz = 0;
@@ -238,6 +253,8 @@ struct dfm2g_ilu_s {
   // level sets: level[i], order (rows by (level,row)), level_start (nlev+1)
   dfm2g::DevBuf<unsigned> level_f, order_f, lstart_f, level_b, order_b, lstart_b;
   dfm2g::DevBuf<uint4> meta_f, meta_b;  // per position of the level order: {row, s0, s1, 0}
+  GroupSched gs_f, gs_b;                // FP32 blob schedules (forward, backward)
+  std::vector<unsigned> group_of;       // blob of each row
   unsigned nlev_f = 0, nlev_b = 0;
   std::vector<unsigned> h_lstart_f, h_lstart_b;
   // scratch for the sweeps (sentinel-filled outputs) and the device error word
@@ -268,6 +285,9 @@ int color_elements(const unsigned *elem, size_t nelem, unsigned nno, size_t np, 
                    std::vector<unsigned> &color_start);
 void to_f32(size_t n, const double *in, float *out);
 int build_slot_map(const unsigned *d_elem, size_t nelem, unsigned nno, const dfm2g_bsr_s *m, unsigned *d_slot);
+int group_schedules_build(dfm2g_ilu_s *p);
+int group_values_fill(dfm2g_ilu_s *p);
+int group_sweep(dfm2g_ilu_s *p, bool forward, const float *in, float *out, const int *skip);
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta);
 int ilu_ensure_f32(dfm2g_ilu_s *p);
 int bsr_ensure_f32(dfm2g_bsr_s *m);

@@ -550,9 +550,15 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     DFM2G_LAUNCH_CHECK();
     return DFM2G_OK;
   }
-  // sync-free: `out` must differ from `in`; it is filled with the pending marker
+  // sync-free and blob schedules: `out` must differ from `in`; it is filled
+  // with the pending marker
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
+  if constexpr (sizeof(T) == 4) {
+    const GroupSched &gs = forward ? p->gs_f : p->gs_b;
+    if (p->sweep_mode == DFM2G_SWEEP_GROUPS && gs.ok && gs.values_ok)
+      return group_sweep(p, forward, (const float *)in, (float *)out, skip);
+  }
   void *kernel = forward ? (void *)k_sweep_syncfree<T, true> : (void *)k_sweep_syncfree<T, false>;
   int *cache = sizeof(T) == 8 ? (forward ? &p->coop_blocks64 : &p->coop_blocks64b)
                               : (forward ? &p->coop_blocks32 : &p->coop_blocks32b);
@@ -593,6 +599,7 @@ int ilu_ensure_f32(dfm2g_ilu_s *p) {
   to_f32(p->nnz * 9, p->vcrs.p, p->vcrs32.p);
   to_f32((size_t)p->nblk * 9, p->vdia.p, p->vdia32.p);
   DFM2G_LAUNCH_CHECK();
+  DFM2G_TRY(group_values_fill(p));
   p->f32_valid = true;
   return DFM2G_OK;
 }
@@ -662,6 +669,11 @@ int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
   }
   DFM2G_TRY(compute_levels(p, false));
   DFM2G_TRY(compute_levels(p, true));
+  DFM2G_TRY(group_schedules_build(p));
+  // The blob schedule is correct but, with one CTA barrier per unit, a single
+  // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
+  // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
+  p->sweep_mode = DFM2G_SWEEP_SYNCFREE;
   const size_t nvec = (size_t)n * 3 + 1;
   DFM2G_TRY(p->tmp64a.resize(nvec));
   DFM2G_TRY(p->tmp64b.resize(nvec));
@@ -802,8 +814,18 @@ int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) { return 
 
 int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   DFM2G_TRY(check_ilu(p, false, false));
-  if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS) return fail(DFM2G_ERR_ARG, "unknown sweep mode");
+  if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS)
+    return fail(DFM2G_ERR_ARG, "unknown sweep mode");
+  if (mode == DFM2G_SWEEP_GROUPS && !(p->gs_f.ok && p->gs_b.ok))
+    return fail(DFM2G_ERR_UNSUPPORTED, "blob schedule unavailable for this pattern");
   p->sweep_mode = mode;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode) {
+  DFM2G_TRY(check_ilu(p, false, false));
+  if (!mode) return fail(DFM2G_ERR_ARG, "get_sweep_mode: null out");
+  *mode = p->sweep_mode;
   return DFM2G_OK;
 }
 

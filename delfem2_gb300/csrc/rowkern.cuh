@@ -17,6 +17,13 @@
 
 namespace dfm2g {
 
+// Pause between polls of a value another warp has not written yet (limits the
+// L2 request traffic of thousands of waiting warps). 0 = spin.
+#ifndef DFM2G_POLL_BACKOFF_NS
+#define DFM2G_POLL_BACKOFF_NS 0
+#endif
+constexpr unsigned kPollBackoffNs = DFM2G_POLL_BACKOFF_NS;
+
 template <typename T, unsigned R>
 struct RowFrag {
   T v[R];
@@ -197,6 +204,7 @@ __device__ __forceinline__ T row_dot_wait(const RowFrag<T, R> &f, const RowLane 
     const unsigned long long t0 = globaltimer_ns();
     unsigned spins = 0;
     for (;;) {
+      if (kPollBackoffNs) __nanosleep(kPollBackoffNs);
 #pragma unroll
       for (unsigned k = 0; k < R; ++k)
         if (is_pending(xv[k])) xv[k] = ld_relaxed(px[k]);

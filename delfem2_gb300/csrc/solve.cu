@@ -445,7 +445,7 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
         }
       }
       if (mode != 1) {
-        if (p->sweep_mode == DFM2G_SWEEP_SYNCFREE) {
+        if (p->sweep_mode != DFM2G_SWEEP_LEVELS) {
           ProfScope ps(DFM2G_PROF_FILL, 2);
           k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, mid);
           k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, Pr);

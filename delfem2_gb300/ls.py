@@ -234,6 +234,11 @@ class CPreconditionerILU:
     def set_sweep_mode(self, mode: int):
         N.call("dfm2g_ilu_set_sweep_mode", self._h, mode)
 
+    def sweep_mode(self) -> int:
+        m = C.c_int(0)
+        N.call("dfm2g_ilu_get_sweep_mode", self._h, C.byref(m))
+        return m.value
+
     def pattern(self):
         col = np.zeros(max(self._nnz, 1), np.uint32)
         dia = np.zeros(max(self.nblk, 1), np.uint32)

@@ -51,7 +51,10 @@ enum dfm2g_prec { DFM2G_F64 = 0, DFM2G_F32 = 1 };
 /* Triangular-sweep schedule (dfm2g_ilu_set_sweep_mode). */
 enum dfm2g_sweep {
   DFM2G_SWEEP_SYNCFREE = 0, /* one persistent launch, per-row readiness     */
-  DFM2G_SWEEP_LEVELS = 1    /* one launch per level set                     */
+  DFM2G_SWEEP_LEVELS = 1,   /* one launch per level set                     */
+  DFM2G_SWEEP_GROUPS = 2    /* FP32: rows in compact blobs, one CTA per blob
+                               (shared-memory dependencies inside a blob);
+                               FP64 sweeps use the sync-free schedule        */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>, 3x3  */
@@ -159,6 +162,8 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * FP32 factors made earlier by a DFM2G_F32 dfm2g_ilu_solve_precond call. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
+/* Current schedule (set_pattern0 picks DFM2G_SWEEP_GROUPS when it fits). */
+DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
  * room for nblk+1). */

@@ -103,9 +103,10 @@ def test_ilu_factors_match_oracle(case):
     assert rel_err(vd, s["ivd"]) < 1e-10
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_sweeps_match_oracle(case, port, mode):
     name, s, P, b = case
+    default = P.ilu.sweep_mode()
     P.ilu.set_sweep_mode(mode)
     try:
         v = np.random.default_rng(4).standard_normal(s["b"].size)
@@ -124,7 +125,7 @@ def test_sweeps_match_oracle(case, port, mode):
         P.ilu.SolvePrecond(z32)
         assert rel_err(z32, go) < 1e-4
     finally:
-        P.ilu.set_sweep_mode(0)
+        P.ilu.set_sweep_mode(default)
 
 
 def test_matvec_matches_oracle(case, port):
@@ -148,10 +149,11 @@ def test_matvec_matches_oracle(case, port):
     assert np.isnan(y[5]) and np.isfinite(np.delete(y, 5)).all()
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_solve_pcg_matches_oracle(case, port, mode):
     import delfem2_gb300 as D
     name, s, P, b = case
+    default = P.ilu.sweep_mode()
     P.ilu.set_sweep_mode(mode)
     try:
         r = s["b"].copy()
@@ -172,7 +174,7 @@ def test_solve_pcg_matches_oracle(case, port, mode):
             assert abs(len(hist) - 1 - int(g["n_iter"])) <= 1
             assert rel_err(x, g["x"]) < 1e-8
     finally:
-        P.ilu.set_sweep_mode(0)
+        P.ilu.set_sweep_mode(default)
 
 
 def test_solve_pcg_semantics_exhaustion_and_tiny_rhs(case):
