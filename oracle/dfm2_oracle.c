@@ -639,3 +639,307 @@ uint32_t orc_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *
   free(Ap);
   return nh;
 }
+
+/* ====================================================================== */
+/* Cloth (implicit, backward Euler).                                       */
+
+/* SetClothShape_Square, include/delfem2/cloth_internal.h:333-397 (mesh     */
+/* part): (ndiv+1)^2 nodes (ix major), two triangles per cell, and the four-*/
+/* node bending stencils: one per cell diagonal, then the y-direction and   */
+/* the x-direction interior edges.                                           */
+void orc_cloth_square(uint32_t ndiv, double size, double *xyz0, uint32_t *tri, uint32_t *quad) {
+  const double h = size / ndiv;
+  const uint32_t m = ndiv + 1;
+  size_t k = 0;
+  for (uint32_t ix = 0; ix <= ndiv; ++ix)
+    for (uint32_t iy = 0; iy <= ndiv; ++iy) {
+      xyz0[k++] = ix * h;
+      xyz0[k++] = iy * h;
+      xyz0[k++] = 0.0;
+    }
+#define ORC_ID(x, y) ((x) * m + (y))
+  size_t t = 0;
+  for (uint32_t ix = 0; ix < ndiv; ++ix)
+    for (uint32_t iy = 0; iy < ndiv; ++iy) {
+      tri[t++] = ORC_ID(ix, iy);
+      tri[t++] = ORC_ID(ix + 1, iy);
+      tri[t++] = ORC_ID(ix, iy + 1);
+      tri[t++] = ORC_ID(ix + 1, iy + 1);
+      tri[t++] = ORC_ID(ix, iy + 1);
+      tri[t++] = ORC_ID(ix + 1, iy);
+    }
+  size_t q = 0;
+  for (uint32_t ix = 0; ix < ndiv; ++ix)
+    for (uint32_t iy = 0; iy < ndiv; ++iy) {
+      quad[q++] = ORC_ID(ix, iy);
+      quad[q++] = ORC_ID(ix + 1, iy + 1);
+      quad[q++] = ORC_ID(ix + 1, iy);
+      quad[q++] = ORC_ID(ix, iy + 1);
+    }
+  for (uint32_t ix = 0; ix < ndiv; ++ix)
+    for (uint32_t iy = 0; iy + 1 < ndiv; ++iy) {
+      quad[q++] = ORC_ID(ix + 1, iy);
+      quad[q++] = ORC_ID(ix, iy + 2);
+      quad[q++] = ORC_ID(ix + 1, iy + 1);
+      quad[q++] = ORC_ID(ix, iy + 1);
+    }
+  for (uint32_t ix = 0; ix + 1 < ndiv; ++ix)
+    for (uint32_t iy = 0; iy < ndiv; ++iy) {
+      quad[q++] = ORC_ID(ix, iy + 1);
+      quad[q++] = ORC_ID(ix + 2, iy);
+      quad[q++] = ORC_ID(ix + 1, iy);
+      quad[q++] = ORC_ID(ix + 1, iy + 1);
+    }
+#undef ORC_ID
+}
+
+static void orc_cross(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+static double orc_dot3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* MakePositiveDefinite_Sim22, include/delfem2/fem_stvk.cpp:211-264, on the  */
+/* symmetric 2x2 [[s0,s2],[s2,s1]] with eigenvalues b-e <= b+e: kept when    */
+/* b-e > 1e-20, zeroed when b+e < 0, else l*t t^T with l = b+e and t the     */
+/* normalised longer row of (S - l I) (zero if both rows are < 1e-10 long). */
+/* Note t is orthogonal to the eigenvector of l: the reference's rank-1      */
+/* result is kept as is for parity.                                          */
+void orc_make_pd_sim22(const double s2[3], double s3[3]) {
+  const double b = 0.5 * (s2[0] + s2[1]);
+  const double e = sqrt(0.25 * (s2[0] - s2[1]) * (s2[0] - s2[1]) + s2[2] * s2[2]);
+  if (b - e > 1.0e-20) {
+    s3[0] = s2[0];
+    s3[1] = s2[1];
+    s3[2] = s2[2];
+    return;
+  }
+  if (b + e < 0) {
+    s3[0] = s3[1] = s3[2] = 0.0;
+    return;
+  }
+  const double l = b + e;
+  double t0[2] = {s2[0] - l, s2[2]}, t1[2] = {s2[2], s2[1] - l};
+  const double q0 = t0[0] * t0[0] + t0[1] * t0[1], q1 = t1[0] * t1[0] + t1[1] * t1[1];
+  const double *t = q0 > q1 ? t0 : t1;
+  const double qq = q0 > q1 ? q0 : q1;
+  if (qq < 1.0e-20) {
+    s3[0] = s3[1] = s3[2] = 0.0;
+    return;
+  }
+  const double inv = 1.0 / sqrt(qq);
+  const double u0 = t[0] * inv, u1 = t[1] * inv;
+  s3[0] = l * u0 * u0;
+  s3[1] = l * u1 * u1;
+  s3[2] = l * u0 * u1;
+}
+
+/* WdWddW_CST, include/delfem2/fem_stvk.cpp:267-374: St.Venant-Kirchhoff    */
+/* constant-strain triangle. Covariant rest edges G0, G1 and contravariant   */
+/* G^0, G^1; Green strain E = (E00, E11, 2E01); S = C E with the plane       */
+/* constitutive matrix in the contravariant metric; W = A/2 E.S;             */
+/* dW[a][i] = A sum_p S_p B_p(a,i) with B_0 = g0_i dN_a0, B_1 = g1_i dN_a1,   */
+/* B_2 = g0_i dN_a1 + g1_i dN_a0; ddW = A B^T C B + A (S+ : dN dN) I where  */
+/* S+ is S made positive definite (orc_make_pd_sim22).                       */
+void orc_wdwddw_cst(const double C[3][3], const double c[3][3], double lambda, double myu, double *W,
+                    double dW[3][3], double ddW[3][3][3][3]) {
+  double G0[3], G1[3], n[3];
+  for (int d = 0; d < 3; ++d) {
+    G0[d] = C[1][d] - C[0][d];
+    G1[d] = C[2][d] - C[0][d];
+  }
+  orc_cross(G0, G1, n);
+  const double nlen = sqrt(orc_dot3(n, n));
+  const double area = 0.5 * nlen;
+  for (int d = 0; d < 3; ++d) n[d] /= nlen;
+  double Gu0[3], Gu1[3];
+  orc_cross(G1, n, Gu0);
+  orc_cross(n, G0, Gu1);
+  const double s0 = 1.0 / orc_dot3(Gu0, G0), s1 = 1.0 / orc_dot3(Gu1, G1);
+  for (int d = 0; d < 3; ++d) {
+    Gu0[d] *= s0;
+    Gu1[d] *= s1;
+  }
+  double g0[3], g1[3];
+  for (int d = 0; d < 3; ++d) {
+    g0[d] = c[1][d] - c[0][d];
+    g1[d] = c[2][d] - c[0][d];
+  }
+  const double E[3] = {0.5 * (orc_dot3(g0, g0) - orc_dot3(G0, G0)), 0.5 * (orc_dot3(g1, g1) - orc_dot3(G1, G1)),
+                       orc_dot3(g0, g1) - orc_dot3(G0, G1)};
+  const double m00 = orc_dot3(Gu0, Gu0), m11 = orc_dot3(Gu1, Gu1), m01 = orc_dot3(Gu1, Gu0);
+  const double Cm[3][3] = {{lambda * m00 * m00 + 2 * myu * m00 * m00, lambda * m00 * m11 + 2 * myu * m01 * m01,
+                            lambda * m00 * m01 + 2 * myu * m00 * m01},
+                           {lambda * m11 * m00 + 2 * myu * m01 * m01, lambda * m11 * m11 + 2 * myu * m11 * m11,
+                            lambda * m11 * m01 + 2 * myu * m01 * m11},
+                           {lambda * m01 * m00 + 2 * myu * m00 * m01, lambda * m01 * m11 + 2 * myu * m01 * m11,
+                            lambda * m01 * m01 + myu * (m00 * m11 + m01 * m01)}};
+  double S[3];
+  for (int p = 0; p < 3; ++p) S[p] = Cm[p][0] * E[0] + Cm[p][1] * E[1] + Cm[p][2] * E[2];
+  *W = 0.5 * area * (E[0] * S[0] + E[1] * S[1] + E[2] * S[2]);
+  static const double dN[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+  double B[3][3][3]; /* B[p][a][i] */
+  for (int a = 0; a < 3; ++a)
+    for (int i = 0; i < 3; ++i) {
+      B[0][a][i] = g0[i] * dN[a][0];
+      B[1][a][i] = g1[i] * dN[a][1];
+      B[2][a][i] = g0[i] * dN[a][1] + g1[i] * dN[a][0];
+      dW[a][i] = area * (S[0] * B[0][a][i] + S[1] * B[1][a][i] + S[2] * B[2][a][i]);
+    }
+  double Sp[3];
+  orc_make_pd_sim22(S, Sp);
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double v = 0.0;
+          for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) v += B[p][a][i] * Cm[p][q] * B[q][b][j];
+          ddW[a][b][i][j] = area * v;
+        }
+      const double g = area * (Sp[0] * dN[a][0] * dN[b][0] + Sp[2] * (dN[a][0] * dN[b][1] + dN[a][1] * dN[b][0]) +
+                               Sp[1] * dN[a][1] * dN[b][1]);
+      for (int i = 0; i < 3; ++i) ddW[a][b][i][i] += g;
+    }
+}
+
+static double orc_tri_area(const double *a, const double *b, const double *c) {
+  double u[3], w[3], n[3];
+  for (int d = 0; d < 3; ++d) {
+    u[d] = b[d] - a[d];
+    w[d] = c[d] - a[d];
+  }
+  orc_cross(u, w, n);
+  return 0.5 * sqrt(orc_dot3(n, n));
+}
+
+/* WdWddW_Bend, include/delfem2/fem_quadratic_bending.cpp:49-107: quadratic  */
+/* bending of the hinge (C2,C3) shared by triangles (C0,C2,C3), (C1,C3,C2):  */
+/* cotangent weights K, ddW[a][b] = K_a K_b stiff/((A0+A1) L^2) I (constant), */
+/* dW = ddW c, W = dW . c.                                                    */
+void orc_wdwddw_bend(const double C[4][3], const double c[4][3], double stiff, double *W, double dW[4][3],
+                     double ddW[4][4][3][3]) {
+  const double A0 = orc_tri_area(C[0], C[2], C[3]), A1 = orc_tri_area(C[1], C[3], C[2]);
+  double e23[3], e02[3], e03[3], e12[3], e13[3];
+  for (int d = 0; d < 3; ++d) {
+    e23[d] = C[3][d] - C[2][d];
+    e02[d] = C[2][d] - C[0][d];
+    e03[d] = C[3][d] - C[0][d];
+    e12[d] = C[2][d] - C[1][d];
+    e13[d] = C[3][d] - C[1][d];
+  }
+  const double L = sqrt(orc_dot3(e23, e23));
+  const double H0 = 2.0 * A0 / L, H1 = 2.0 * A1 / L;
+  const double c023 = -orc_dot3(e02, e23) / H0, c032 = orc_dot3(e03, e23) / H0;
+  const double c123 = -orc_dot3(e12, e23) / H1, c132 = orc_dot3(e13, e23) / H1;
+  const double k = stiff / ((A0 + A1) * L * L);
+  const double K[4] = {-c023 - c032, -c123 - c132, c032 + c132, c023 + c123};
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b)
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) ddW[a][b][i][j] = (i == j) ? K[a] * K[b] * k : 0.0;
+  *W = 0.0;
+  for (int a = 0; a < 4; ++a)
+    for (int i = 0; i < 3; ++i) {
+      double s = 0.0;
+      for (int b = 0; b < 4; ++b) s += K[a] * K[b] * k * c[b][i];
+      dW[a][i] = s;
+      *W += s * c[a][i];
+    }
+}
+
+/* MergeLinSys_Cloth, include/delfem2/femcloth.h:48-114, with the membrane    */
+/* moduli per triangle (lambda, myu from E_t and nu): adds the CST and bending */
+/* Hessians into K and their gradients into dW; returns the energy (or NaN on */
+/* a missing slot).                                                           */
+double orc_cloth_assemble(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                          double *vdia, double *dW, const double *xyz0, const double *xyz, const uint32_t *tri,
+                          size_t ntri, const uint32_t *quad, size_t nquad, const double *young_tri, double nu,
+                          double stiff_bend) {
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t));
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  double W = 0.0;
+  for (size_t t = 0; t < ntri; ++t) {
+    const uint32_t *n = tri + t * 3;
+    double C[3][3], c[3][3], w, dw[3][3], ddw[3][3][3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) {
+        C[a][d] = xyz0[(size_t)n[a] * 3 + d];
+        c[a][d] = xyz[(size_t)n[a] * 3 + d];
+      }
+    const double E = young_tri[t];
+    orc_wdwddw_cst(C, c, E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), E / (2.0 * (1.0 + nu)), &w, dw, ddw);
+    W += w;
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) dW[(size_t)n[a] * 3 + d] += dw[a][d];
+    if (orc_merge(nblk, row_start, col, vcrs, vdia, 3, n, &ddw[0][0][0][0], buf)) W = NAN;
+  }
+  for (size_t q = 0; q < nquad; ++q) {
+    const uint32_t *n = quad + q * 4;
+    double C[4][3], c[4][3], w, dw[4][3], ddw[4][4][3][3];
+    for (int a = 0; a < 4; ++a)
+      for (int d = 0; d < 3; ++d) {
+        C[a][d] = xyz0[(size_t)n[a] * 3 + d];
+        c[a][d] = xyz[(size_t)n[a] * 3 + d];
+      }
+    orc_wdwddw_bend(C, c, stiff_bend, &w, dw, ddw);
+    W += w;
+    for (int a = 0; a < 4; ++a)
+      for (int d = 0; d < 3; ++d) dW[(size_t)n[a] * 3 + d] += dw[a][d];
+    if (orc_merge(nblk, row_start, col, vcrs, vdia, 4, n, &ddw[0][0][0][0], buf)) W = NAN;
+  }
+  free(buf);
+  return W;
+}
+
+/* One backward-Euler step, the sequence of StepTime_InternalDynamicsILU     */
+/* (include/delfem2/cloth_internal.h:179-269) with the gravity term of       */
+/* AddWdW_Gravity (76-92) and the caller's tolerance and iteration limit:    */
+/*   A = M/dt^2 + ddW(x), b = -(dW(x) - M g) + M v/dt, clamp, ILU(0)-PCG;     */
+/*   free DOFs: x += dx, v = dx/dt. Returns the PCG history length.           */
+uint32_t orc_cloth_step(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *xyz, double *uvw,
+                        const double *xyz0, const int *bc, const uint32_t *tri, size_t ntri, const uint32_t *quad,
+                        size_t nquad, const double *young_tri, double nu, double stiff_bend, const double g[3],
+                        double mass, double dt, double tol, uint32_t max_iter) {
+  const size_t nnz = row_start[nblk], n = (size_t)nblk * 3;
+  double *vcrs = (double *)calloc(nnz * 9 + 1, sizeof(double));
+  double *vdia = (double *)calloc((size_t)nblk * 9, sizeof(double));
+  double *b = (double *)calloc(n, sizeof(double));
+  orc_cloth_assemble(nblk, row_start, col, vcrs, vdia, b, xyz0, xyz, tri, ntri, quad, nquad, young_tri, nu,
+                     stiff_bend);
+  for (uint32_t i = 0; i < nblk; ++i)
+    for (int d = 0; d < 3; ++d) b[(size_t)i * 3 + d] -= mass * g[d];
+  for (size_t k = 0; k < n; ++k) b[k] = -b[k] + mass * uvw[k] / dt;
+  for (uint32_t i = 0; i < nblk; ++i)
+    for (int d = 0; d < 3; ++d) vdia[(size_t)i * 9 + d * 4] += mass / (dt * dt);
+  orc_set_fixed_bc(nblk, row_start, col, vcrs, vdia, bc);
+  orc_rhs_zero(b, bc, n);
+  uint32_t *icol = (uint32_t *)malloc((nnz + 1) * sizeof(uint32_t));
+  uint32_t *dia = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t));
+  double *ivcrs = (double *)malloc((nnz * 9 + 1) * sizeof(double));
+  double *ivdia = (double *)malloc((size_t)nblk * 9 * sizeof(double));
+  orc_ilu_pattern0(nblk, row_start, col, icol, dia);
+  orc_ilu_copy_value(nblk, row_start, icol, ivcrs, ivdia, col, vcrs, vdia);
+  int ns = 0;
+  orc_ilu_decompose(nblk, row_start, icol, dia, ivcrs, ivdia, &ns);
+  double *dx = (double *)calloc(n, sizeof(double));
+  double *hist = (double *)malloc(((size_t)max_iter + 2) * sizeof(double));
+  const uint32_t nh = orc_solve_pcg(nblk, row_start, col, vcrs, vdia, icol, dia, ivcrs, ivdia, b, dx, tol, max_iter,
+                                    hist, max_iter + 2);
+  for (size_t k = 0; k < n; ++k) {
+    if (bc[k] != 0) continue;
+    xyz[k] += dx[k];
+    uvw[k] = dx[k] / dt;
+  }
+  free(vcrs);
+  free(vdia);
+  free(b);
+  free(icol);
+  free(dia);
+  free(ivcrs);
+  free(ivdia);
+  free(dx);
+  free(hist);
+  return nh;
+}

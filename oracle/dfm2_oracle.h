@@ -87,6 +87,22 @@ uint32_t orc_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *
                       double tol, uint32_t max_iter, double *hist, uint32_t hist_cap);
 double orc_dot(const double *a, const double *b, size_t n);
 
+/* --- cloth ------------------------------------------------------------- */
+void orc_cloth_square(uint32_t ndiv, double size, double *xyz0, uint32_t *tri, uint32_t *quad);
+void orc_make_pd_sim22(const double s2[3], double s3[3]);
+void orc_wdwddw_cst(const double C[3][3], const double c[3][3], double lambda, double myu, double *W,
+                    double dW[3][3], double ddW[3][3][3][3]);
+void orc_wdwddw_bend(const double C[4][3], const double c[4][3], double stiff, double *W, double dW[4][3],
+                     double ddW[4][4][3][3]);
+double orc_cloth_assemble(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                          double *vdia, double *dW, const double *xyz0, const double *xyz, const uint32_t *tri,
+                          size_t ntri, const uint32_t *quad, size_t nquad, const double *young_tri, double nu,
+                          double stiff_bend);
+uint32_t orc_cloth_step(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *xyz, double *uvw,
+                        const double *xyz0, const int *bc, const uint32_t *tri, size_t ntri, const uint32_t *quad,
+                        size_t nquad, const double *young_tri, double nu, double stiff_bend, const double g[3],
+                        double mass, double dt, double tol, uint32_t max_iter);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,7 +5,7 @@ oracle/Makefile), so it only works where the reference source tree exists.
 The outputs are small .npz files committed next to this script; the tests
 read them on machines without the reference.
 
-  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4]
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth]
 """
 from __future__ import annotations
 
@@ -100,6 +100,57 @@ def make_cfg(R, name, nx, ny, nz, h, young, tol, full_x):
           f"rel={hist[-1] / hist[0]:.3e} time={dt:.1f}s")
 
 
+def make_cloth(R):
+    """Cloth element functions on seeded inputs and short backward-Euler runs on
+    a 16x16-cell sheet (289 vertices): StepTime_InternalDynamicsILU itself
+    (uniform E = 1e3, its own 1e-4 / 100) and the same step with per-triangle
+    E and PCG to 1e-8 (the cloth workload's settings)."""
+    from oracle import cloth as CL
+    rng = np.random.default_rng(55)
+    out = {}
+    Cc = rng.standard_normal((32, 3, 3))
+    cc = Cc + 0.3 * rng.standard_normal((32, 3, 3))
+    lm = rng.uniform(0.2, 2.0, (32, 2))
+    res = [CL.wdwddw_cst(R, Cc[i], cc[i], lm[i, 0], lm[i, 1]) for i in range(32)]
+    out.update(cst_C=Cc, cst_c=cc, cst_lm=lm, cst_W=np.array([r[0] for r in res]),
+               cst_dW=np.array([r[1] for r in res]), cst_ddW=np.array([r[2] for r in res]))
+    Cq = rng.standard_normal((32, 4, 3))
+    cq = Cq + 0.2 * rng.standard_normal((32, 4, 3))
+    res = [CL.wdwddw_bend(R, Cq[i], cq[i], 1e-3) for i in range(32)]
+    out.update(bend_C=Cq, bend_c=cq, bend_W=np.array([r[0] for r in res]),
+               bend_dW=np.array([r[1] for r in res]), bend_ddW=np.array([r[2] for r in res]))
+    s2 = rng.standard_normal((64, 3))
+    out.update(pd_s2=s2, pd_s3=np.array([CL.make_pd_sim22(R, v) for v in s2]))
+    ndiv = 16
+    xyz0, tri, quad = CL.cloth_square(R, ndiv)
+    np_ = xyz0.size // 3
+    ind, psup = R.psup(quad, 4, np_)
+    bc = np.zeros(np_ * 3, np.int32)
+    bc[0:3] = 1
+    bc[ndiv * 3:ndiv * 3 + 3] = 1
+    g = np.array([0.0, 0.0, -10.0])
+    mass = 1.0 / np_
+    young_rand = young_log_uniform(tri.size // 3, 5e2, 2e3, 56)
+    out.update(xyz0=xyz0, tri=tri, quad=quad, ind=ind, psup=psup, bc=bc, young_rand=young_rand)
+    xyz = xyz0 + 0.01 * rng.standard_normal(xyz0.size)
+    W, vc, vd, dW = CL.cloth_assemble(R, ind, psup, xyz0, xyz, tri, quad, young_rand, 0.3, 1e-3)
+    out.update(asm_xyz=xyz, asm_W=W, asm_vc=vc, asm_vd=vd, asm_dW=dW)
+    for tag, young, tol, mi, nstep in (("own", np.full(tri.size // 3, 1e3), 1e-4, 100, 10),
+                                       ("rand", young_rand, 1e-8, 1000, 10)):
+        x, v = xyz0.copy(), np.zeros_like(xyz0)
+        traj, nh = [], []
+        for _ in range(nstep):
+            x, v, n = CL.cloth_step(R, ind, psup, x, v, xyz0, bc, tri, quad, young, 0.3, 1e-3, g, mass, 0.01, tol,
+                                    mi)
+            traj.append(x.copy())
+            nh.append(n)
+        out[f"step_{tag}_x"] = np.array(traj)
+        out[f"step_{tag}_v"] = v
+        out[f"step_{tag}_nhist"] = np.array(nh)
+    np.savez_compressed(os.path.join(HERE, "cloth.npz"), **out)
+    print("cloth: rand-E iterations per step", out["step_rand_nhist"] - 1)
+
+
 def main(which):
     build(quiet=True)
     R = reference()
@@ -116,6 +167,8 @@ def main(which):
                  False)
     if "cfg4" in which:  # 48^3, E log-uniform [0.5, 2], seed 4, to 1e-12
         make_cfg(R, "cfg4", 48, 48, 48, 1 / 48, young_log_uniform(48 ** 3 * 6, 0.5, 2.0, 4), 1e-12, False)
+    if "cloth" in which:
+        make_cloth(R)
 
 
 if __name__ == "__main__":
