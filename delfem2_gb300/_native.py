@@ -100,6 +100,15 @@ SIGNATURES = {
     "dfm2g_tetmesh_info": [_vp, _pu, _psz],
     "dfm2g_tetmesh_assemble_linear": [_vp, _vp, _vp, _d, _d, _vp, _vp, _vp, _i],
     "dfm2g_tetmesh_dLdE": [_vp, _vp, _d, _vp, _vp, _vp, _i],
+    "dfm2g_cloth_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz, _vp, _sz],
+    "dfm2g_cloth_destroy": [_vp],
+    "dfm2g_cloth_info": [_vp, _pu, _pu],
+    "dfm2g_cloth_merge": [_vp, _vp, _vp, _vp, _d, _d, _vp, C.POINTER(C.c_double), _i],
+    "dfm2g_cloth_step": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp, _d, _d, _d, _u, _i, _pstats, _i],
+    "dfm2g_cloth_adjoint_terms": [_vp, _vp, _vp, _d, _d, _vp, _vp, _vp, _vp, _i],
+    "dfm2g_cloth_rollout": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp, _d, _d, _d, _u, _i, _u, _u, _pstats,
+                            _i],
+    "dfm2g_cloth_rollout_adjoint": [_vp, _vp, _vp, _vp, _vp, _vp, _pstats, _i],
     "dfm2g_profile_enable": [_i],
     "dfm2g_profile_reset": [],
     "dfm2g_profile_read": [_i, _pu, C.POINTER(C.c_double)],

@@ -226,6 +226,62 @@ DFM2G_API int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const 
 DFM2G_API int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu,
                                  const double *u, const double *lam, double *dLdE, int mem);
 
+/* ---- implicit cloth (include/delfem2/femcloth.h, cloth_internal.h) --------- */
+/* Triangle sheet with StVK CST membrane + quadratic bending over the quads of
+ * adjacent triangle pairs. Built from host arrays (xyz0: 3*np rest positions,
+ * tri: 3*ntri, quad: 4*nquad in WdWddW_Bend's order) against the pattern of K
+ * (which must contain every tri and quad block): element->slot maps, greedy
+ * colourings, per-element rest constants. */
+typedef struct dfm2g_cloth_s *dfm2g_cloth;
+DFM2G_API int dfm2g_cloth_create(dfm2g_cloth *out, dfm2g_bsr m, const double *xyz0, size_t np,
+                                 const unsigned *tri, size_t ntri, const unsigned *quad, size_t nquad);
+DFM2G_API int dfm2g_cloth_destroy(dfm2g_cloth c);
+DFM2G_API int dfm2g_cloth_info(dfm2g_cloth c, unsigned *ncolor_tri, unsigned *ncolor_quad);
+/* MergeLinSys_Cloth, femcloth.h:48-114, with per-triangle moduli: adds the
+ * PD-projected CST Hessians (WdWddW_CST, fem_stvk.cpp:267-374) and the bending
+ * Hessians (WdWddW_Bend, fem_quadratic_bending.cpp:49-107) into K and their
+ * gradients into dW (3*np); *W (host, may be NULL) receives the energy.
+ * young_tri: ntri; (lambda, myu) = (E nu/((1+nu)(1-2nu)), E/(2(1+nu))). */
+DFM2G_API int dfm2g_cloth_merge(dfm2g_cloth c, dfm2g_bsr m, const double *xyz, const double *young_tri,
+                                double nu, double stiff_bend, double *dW, double *W, int mem);
+/* Linear solver inside the cloth step. */
+enum dfm2g_cloth_solver {
+  DFM2G_CLOTH_PCG_F64 = 0,      /* Solve_PCG in FP64 (the reference's solver)  */
+  DFM2G_CLOTH_PCG_MIXED = 1     /* FP32 PCG with FP64 reliable updates         */
+};
+/* StepTime_InternalDynamicsILU, cloth_internal.h:179-269 (no contact): one
+ * backward-Euler step with one Newton linearisation,
+ *   A = M/dt^2 + ddW(x), b = -(dW(x) - M g) + M v/dt, clamped at bc,
+ *   ILU(0)-PCG(tol, max_iter), free DOFs: x += dx, v = dx/dt.
+ * g: 3 host doubles; mass: per vertex. Not reaching tol is not an error (the
+ * reference continues with the last iterate); stats tells the iterations. */
+DFM2G_API int dfm2g_cloth_step(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xyz, double *uvw,
+                               const int *bc, const double *young_tri, double nu, double stiff_bend,
+                               const double *g, double mass, double dt, double tol, unsigned max_iter,
+                               int solver, dfm2g_solve_stats *stats, int mem);
+/* Adjoint element terms of one step (no reference counterpart): with mu the
+ * adjoint solve and dx the step's increment,
+ *   xbar += -H(x) mu - grad_x( mu^T A(x) dx )   (H: unprojected Hessian),
+ *   Ebar_t += -( mu_t . dW_t + mu_t^T A_t dx_t ) / E_t. */
+DFM2G_API int dfm2g_cloth_adjoint_terms(dfm2g_cloth c, const double *xyz, const double *young_tri,
+                                        double nu, double stiff_bend, const double *mu, const double *dx,
+                                        double *xbar, double *Ebar, int mem);
+/* Runs nsteps steps (as dfm2g_cloth_step) from (xyz, uvw), keeping on the
+ * device the state every ckpt_every steps (0: no checkpoints) and the step
+ * settings for dfm2g_cloth_rollout_adjoint. stats sums over the steps. */
+DFM2G_API int dfm2g_cloth_rollout(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xyz, double *uvw,
+                                  const int *bc, const double *young_tri, double nu, double stiff_bend,
+                                  const double *g, double mass, double dt, double tol, unsigned max_iter,
+                                  int solver, unsigned nsteps, unsigned ckpt_every,
+                                  dfm2g_solve_stats *stats, int mem);
+/* Reverse pass of the last rollout (checkpoint-and-recompute): from
+ * xbar = dL/dx_N, vbar = dL/dv_N to dL/dx_0, dL/dv_0 in place, and
+ * dLdE = dL/dE_t (ntri, overwritten). Re-runs each checkpoint segment forward,
+ * then per step re-assembles and re-factorises A, solves A mu = P(xbar + vbar/dt)
+ * and applies dfm2g_cloth_adjoint_terms. Needs ckpt_every > 0. */
+DFM2G_API int dfm2g_cloth_rollout_adjoint(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xbar,
+                                          double *vbar, double *dLdE, dfm2g_solve_stats *stats, int mem);
+
 /* ---- instrumentation ------------------------------------------------------- */
 /* Kernel classes timed when profiling is on (CUDA events around every launch
  * of the solver loops; adds a little overhead, so off by default). */

@@ -80,3 +80,63 @@ def cloth_step(O, row_start, col, xyz, uvw, xyz0, bc, tri, quad, young_tri, nu, 
            _nz(quad), quad.size // 4, np.ascontiguousarray(young_tri, np.float64), nu, stiff_bend,
            np.ascontiguousarray(g, np.float64), mass, dt, tol, max_iter)
     return x, v, nh
+
+
+def pd_sim22_jac(O, s2):
+    J = np.zeros(9)
+    _fn(O, "pd_sim22_jac", [_f64p, _f64p])(np.ascontiguousarray(s2, np.float64), J)
+    return J.reshape(3, 3)
+
+
+def adjoint_terms(O, xyz0, xyz, tri, quad, young_tri, nu, stiff_bend, mu, dx, xbar, Ebar):
+    """In place: xbar += -H mu - grad(mu^T ddW dx); Ebar += -(mu.dW + mu^T ddW dx)/E."""
+    f = _fn(O, "cloth_adjoint_terms", [_f64p, _f64p, _u32p, C.c_size_t, _u32p, C.c_size_t, _f64p, C.c_double,
+                                       C.c_double, _f64p, _f64p, _f64p, _f64p])
+    f(xyz0, np.ascontiguousarray(xyz, np.float64), tri, tri.size // 3, _nz(quad), quad.size // 4,
+      np.ascontiguousarray(young_tri, np.float64), nu, stiff_bend, np.ascontiguousarray(mu, np.float64),
+      np.ascontiguousarray(dx, np.float64), xbar, Ebar)
+
+
+def step_matrix(O, row_start, col, xyz0, xyz, bc, tri, quad, young_tri, nu, stiff_bend, mass, dt):
+    """The clamped A = M/dt^2 + ddW(x) of a step and its ILU(0) factors."""
+    W, vc, vd, dW = cloth_assemble(O, row_start, col, xyz0, xyz, tri, quad, young_tri, nu, stiff_bend)
+    for d in (0, 4, 8):
+        vd[d::9] += mass / (dt * dt)
+    O.set_fixed_bc(row_start, col, vc, vd, np.ascontiguousarray(bc, np.int32))
+    icol, dia = O.ilu_pattern0(row_start, col)
+    ivc, ivd = O.ilu_copy_value(row_start, icol, col, vc, vd)
+    st, _ = O.ilu_decompose(row_start, icol, dia, ivc, ivd)
+    assert st == 0
+    return vc, vd, icol, dia, ivc, ivd
+
+
+def rollout(O, row_start, col, xyz0, bc, tri, quad, young_tri, nu, stiff_bend, g, mass, dt, tol, max_iter, nsteps):
+    """All positions x_0..x_N (from rest, zero velocity) and the final velocity."""
+    x, v = xyz0.copy(), np.zeros_like(xyz0)
+    xs = [x.copy()]
+    for _ in range(nsteps):
+        x, v, _ = cloth_step(O, row_start, col, x, v, xyz0, bc, tri, quad, young_tri, nu, stiff_bend, g, mass, dt,
+                             tol, max_iter)
+        xs.append(x.copy())
+    return xs, v
+
+
+def rollout_adjoint(O, row_start, col, xyz0, xs, bc, tri, quad, young_tri, nu, stiff_bend, mass, dt, tol, max_iter,
+                    xbar, vbar):
+    """FP64 CPU adjoint of `rollout` (all states kept): returns dL/dx_0,
+    dL/dv_0, dL/dE from xbar = dL/dx_N, vbar = dL/dv_N. Per step, with
+    mu = A^-1 P (xbar + vbar/dt): xbar <- xbar - H mu - grad(mu^T A dx),
+    vbar <- M mu/dt on free DOFs."""
+    xbar, vbar = np.array(xbar, np.float64), np.array(vbar, np.float64)
+    Ebar = np.zeros(tri.size // 3)
+    free = np.asarray(bc) == 0
+    for k in range(len(xs) - 2, -1, -1):
+        xk, xk1 = xs[k], xs[k + 1]
+        vc, vd, icol, dia, ivc, ivd = step_matrix(O, row_start, col, xyz0, xk, bc, tri, quad, young_tri, nu,
+                                                  stiff_bend, mass, dt)
+        dxbar = np.where(free, xbar + vbar / dt, 0.0)
+        dx = np.where(free, xk1 - xk, 0.0)
+        mu, _, _ = O.solve_pcg(row_start, col, vc, vd, icol, dia, ivc, ivd, dxbar, tol, max_iter)
+        adjoint_terms(O, xyz0, xk, tri, quad, young_tri, nu, stiff_bend, mu, dx, xbar, Ebar)
+        vbar = np.where(free, mass * mu / dt, vbar)
+    return xbar, vbar, Ebar

@@ -943,3 +943,188 @@ uint32_t orc_cloth_step(uint32_t nblk, const uint32_t *row_start, const uint32_t
   free(hist);
   return nh;
 }
+
+/* ---- cloth adjoint (no reference counterpart; checker for the device's) ---- */
+
+/* Jacobian J[k][l] = d s3_k / d s2_l of orc_make_pd_sim22, branch by branch:  */
+/* identity, zero, or the derivative of l u u^T (l = b + e, u = t/|t|, t the   */
+/* chosen row of S - l I; the branch choice is locally constant).              */
+void orc_pd_sim22_jac(const double s2[3], double J[3][3]) {
+  for (int k = 0; k < 3; ++k)
+    for (int l = 0; l < 3; ++l) J[k][l] = 0.0;
+  const double b = 0.5 * (s2[0] + s2[1]);
+  const double e = sqrt(0.25 * (s2[0] - s2[1]) * (s2[0] - s2[1]) + s2[2] * s2[2]);
+  if (b - e > 1.0e-20) {
+    for (int k = 0; k < 3; ++k) J[k][k] = 1.0;
+    return;
+  }
+  if (b + e < 0) return;
+  const double lam = b + e;
+  double t0[2] = {s2[0] - lam, s2[2]}, t1[2] = {s2[2], s2[1] - lam};
+  const double q0 = t0[0] * t0[0] + t0[1] * t0[1], q1 = t1[0] * t1[0] + t1[1] * t1[1];
+  const int first = q0 > q1;
+  const double qq = first ? q0 : q1;
+  if (qq < 1.0e-20) return;
+  /* dl/ds */
+  const double dl[3] = {0.5 + 0.25 * (s2[0] - s2[1]) / e, 0.5 - 0.25 * (s2[0] - s2[1]) / e, s2[2] / e};
+  /* dt/ds (2 x 3) */
+  double dt[2][3];
+  for (int l = 0; l < 3; ++l) {
+    if (first) {
+      dt[0][l] = (l == 0) - dl[l];
+      dt[1][l] = (l == 2);
+    } else {
+      dt[0][l] = (l == 2);
+      dt[1][l] = (l == 1) - dl[l];
+    }
+  }
+  const double *t = first ? t0 : t1;
+  const double r = sqrt(qq);
+  const double u[2] = {t[0] / r, t[1] / r};
+  for (int l = 0; l < 3; ++l) {
+    /* du = (I - u u^T) dt / r */
+    const double ud = u[0] * dt[0][l] + u[1] * dt[1][l];
+    const double du[2] = {(dt[0][l] - u[0] * ud) / r, (dt[1][l] - u[1] * ud) / r};
+    J[0][l] = dl[l] * u[0] * u[0] + lam * 2.0 * u[0] * du[0];
+    J[1][l] = dl[l] * u[1] * u[1] + lam * 2.0 * u[1] * du[1];
+    J[2][l] = dl[l] * u[0] * u[1] + lam * (du[0] * u[1] + u[0] * du[1]);
+  }
+}
+
+/* Per triangle (per-triangle E), with mu the adjoint solve and dx the step  */
+/* increment:                                                                */
+/*   xbar += -H_true mu - grad_c (mu^T ddW(c) dx),                           */
+/*   Ebar_t += -(mu.dW_t + mu^T ddW_t dx) / E_t;                              */
+/* per quad: xbar += -H_bend mu. H_true is ddW with the raw stress S in the  */
+/* geometric term instead of S+. Written in node space with explicit B       */
+/* matrices (dB/dc is constant: dB_p(a,i)/dc(b,j) = delta_ij w_p(a,b)).      */
+void orc_cloth_adjoint_terms(const double *xyz0, const double *xyz, const uint32_t *tri, size_t ntri,
+                             const uint32_t *quad, size_t nquad, const double *young_tri, double nu,
+                             double stiff_bend, const double *mu, const double *dx, double *xbar, double *Ebar) {
+  static const double dN[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+  for (size_t t = 0; t < ntri; ++t) {
+    const uint32_t *n = tri + t * 3;
+    double C[3][3], c[3][3], M[3][3], D[3][3];
+    for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d) {
+        C[a][d] = xyz0[(size_t)n[a] * 3 + d];
+        c[a][d] = xyz[(size_t)n[a] * 3 + d];
+        M[a][d] = mu[(size_t)n[a] * 3 + d];
+        D[a][d] = dx[(size_t)n[a] * 3 + d];
+      }
+    const double E = young_tri[t];
+    const double lambda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), myu = E / (2.0 * (1.0 + nu));
+    /* W, dW, ddW at c give S (through dW is awkward): recompute the pieces. */
+    double G0[3], G1[3], nr[3];
+    for (int d = 0; d < 3; ++d) {
+      G0[d] = C[1][d] - C[0][d];
+      G1[d] = C[2][d] - C[0][d];
+    }
+    orc_cross(G0, G1, nr);
+    const double nlen = sqrt(orc_dot3(nr, nr));
+    const double area = 0.5 * nlen;
+    for (int d = 0; d < 3; ++d) nr[d] /= nlen;
+    double Gu0[3], Gu1[3];
+    orc_cross(G1, nr, Gu0);
+    orc_cross(nr, G0, Gu1);
+    const double s0 = 1.0 / orc_dot3(Gu0, G0), s1 = 1.0 / orc_dot3(Gu1, G1);
+    for (int d = 0; d < 3; ++d) {
+      Gu0[d] *= s0;
+      Gu1[d] *= s1;
+    }
+    double g0[3], g1[3];
+    for (int d = 0; d < 3; ++d) {
+      g0[d] = c[1][d] - c[0][d];
+      g1[d] = c[2][d] - c[0][d];
+    }
+    const double Es[3] = {0.5 * (orc_dot3(g0, g0) - orc_dot3(G0, G0)),
+                          0.5 * (orc_dot3(g1, g1) - orc_dot3(G1, G1)), orc_dot3(g0, g1) - orc_dot3(G0, G1)};
+    const double m00 = orc_dot3(Gu0, Gu0), m11 = orc_dot3(Gu1, Gu1), m01 = orc_dot3(Gu1, Gu0);
+    const double Cm[3][3] = {{lambda * m00 * m00 + 2 * myu * m00 * m00, lambda * m00 * m11 + 2 * myu * m01 * m01,
+                              lambda * m00 * m01 + 2 * myu * m00 * m01},
+                             {lambda * m11 * m00 + 2 * myu * m01 * m01, lambda * m11 * m11 + 2 * myu * m11 * m11,
+                              lambda * m11 * m01 + 2 * myu * m01 * m11},
+                             {lambda * m01 * m00 + 2 * myu * m00 * m01, lambda * m01 * m11 + 2 * myu * m01 * m11,
+                              lambda * m01 * m01 + myu * (m00 * m11 + m01 * m01)}};
+    double S[3], Sp[3], J[3][3];
+    for (int p = 0; p < 3; ++p) S[p] = Cm[p][0] * Es[0] + Cm[p][1] * Es[1] + Cm[p][2] * Es[2];
+    orc_make_pd_sim22(S, Sp);
+    orc_pd_sim22_jac(S, J);
+    double B[3][3][3], w[3][3][3]; /* B[p][a][i]; w[p][a][b] = dB_p(a,.)/dc(b,.) */
+    for (int a = 0; a < 3; ++a) {
+      for (int i = 0; i < 3; ++i) {
+        B[0][a][i] = g0[i] * dN[a][0];
+        B[1][a][i] = g1[i] * dN[a][1];
+        B[2][a][i] = g0[i] * dN[a][1] + g1[i] * dN[a][0];
+      }
+      for (int b = 0; b < 3; ++b) {
+        w[0][a][b] = dN[a][0] * dN[b][0];
+        w[1][a][b] = dN[a][1] * dN[b][1];
+        w[2][a][b] = dN[a][1] * dN[b][0] + dN[a][0] * dN[b][1];
+      }
+    }
+    double Bm[3] = {0, 0, 0}, Bd[3] = {0, 0, 0}; /* B mu, B dx */
+    for (int p = 0; p < 3; ++p)
+      for (int a = 0; a < 3; ++a)
+        for (int i = 0; i < 3; ++i) {
+          Bm[p] += B[p][a][i] * M[a][i];
+          Bd[p] += B[p][a][i] * D[a][i];
+        }
+    double CBm[3], CBd[3];
+    for (int p = 0; p < 3; ++p) {
+      CBm[p] = Cm[p][0] * Bm[0] + Cm[p][1] * Bm[1] + Cm[p][2] * Bm[2];
+      CBd[p] = Cm[p][0] * Bd[0] + Cm[p][1] * Bd[1] + Cm[p][2] * Bd[2];
+    }
+    /* Q_p = sum_ab w_p(a,b) mu_a . dx_b, so mu^T (S+ : dN dN) dx = S+ . Q */
+    double Q[3] = {0, 0, 0};
+    for (int p = 0; p < 3; ++p)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) Q[p] += w[p][a][b] * orc_dot3(M[a], D[b]);
+    double JtQ[3];
+    for (int l = 0; l < 3; ++l) JtQ[l] = J[0][l] * Q[0] + J[1][l] * Q[1] + J[2][l] * Q[2];
+    for (int b = 0; b < 3; ++b)
+      for (int j = 0; j < 3; ++j) {
+        /* H_true mu at (b,j) */
+        double h = 0.0;
+        for (int p = 0; p < 3; ++p) h += B[p][b][j] * CBm[p];
+        for (int a = 0; a < 3; ++a) h += (S[0] * w[0][b][a] + S[1] * w[1][b][a] + S[2] * w[2][b][a]) * M[a][j];
+        /* d/dc(b,j) of Bm.Cm.Bd + S+.Q */
+        double dBm[3], dBd[3], dS[3];
+        for (int p = 0; p < 3; ++p) {
+          dBm[p] = 0.0;
+          dBd[p] = 0.0;
+          for (int a = 0; a < 3; ++a) {
+            dBm[p] += w[p][a][b] * M[a][j];
+            dBd[p] += w[p][a][b] * D[a][j];
+          }
+          dS[p] = 0.0;
+        }
+        for (int p = 0; p < 3; ++p)
+          for (int q = 0; q < 3; ++q) dS[p] += Cm[p][q] * B[q][b][j]; /* dS/dc(b,j) = Cm dE/dc = Cm B(.,b,j) */
+        double gphi = 0.0;
+        for (int p = 0; p < 3; ++p) gphi += dBm[p] * CBd[p] + CBm[p] * dBd[p] + JtQ[p] * dS[p];
+        xbar[(size_t)n[b] * 3 + j] -= area * (h + gphi);
+      }
+    const double muW = area * (S[0] * Bm[0] + S[1] * Bm[1] + S[2] * Bm[2]);
+    const double phi = area * (Bm[0] * CBd[0] + Bm[1] * CBd[1] + Bm[2] * CBd[2] + Sp[0] * Q[0] + Sp[1] * Q[1] +
+                               Sp[2] * Q[2]);
+    Ebar[t] -= (muW + phi) / E;
+  }
+  for (size_t q = 0; q < nquad; ++q) {
+    const uint32_t *n = quad + q * 4;
+    double C[4][3], c[4][3], w, dw[4][3], ddw[4][4][3][3];
+    for (int a = 0; a < 4; ++a)
+      for (int d = 0; d < 3; ++d) {
+        C[a][d] = xyz0[(size_t)n[a] * 3 + d];
+        c[a][d] = xyz[(size_t)n[a] * 3 + d];
+      }
+    orc_wdwddw_bend(C, c, stiff_bend, &w, dw, ddw);
+    for (int a = 0; a < 4; ++a)
+      for (int i = 0; i < 3; ++i) {
+        double h = 0.0;
+        for (int b = 0; b < 4; ++b)
+          for (int j = 0; j < 3; ++j) h += ddw[a][b][i][j] * mu[(size_t)n[b] * 3 + j];
+        xbar[(size_t)n[a] * 3 + i] -= h;
+      }
+  }
+}

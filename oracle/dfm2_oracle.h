@@ -102,6 +102,10 @@ uint32_t orc_cloth_step(uint32_t nblk, const uint32_t *row_start, const uint32_t
                         const double *xyz0, const int *bc, const uint32_t *tri, size_t ntri, const uint32_t *quad,
                         size_t nquad, const double *young_tri, double nu, double stiff_bend, const double g[3],
                         double mass, double dt, double tol, uint32_t max_iter);
+void orc_pd_sim22_jac(const double s2[3], double J[3][3]);
+void orc_cloth_adjoint_terms(const double *xyz0, const double *xyz, const uint32_t *tri, size_t ntri,
+                             const uint32_t *quad, size_t nquad, const double *young_tri, double nu,
+                             double stiff_bend, const double *mu, const double *dx, double *xbar, double *Ebar);
 
 #ifdef __cplusplus
 }

@@ -142,3 +142,105 @@ def test_port_equals_reference_directly(port):
                                    1.0 / np_, 0.01, 1e-8, 1000)
         assert na == nb
     assert rel_err(xa - x0, xb - x0) < 1e-12 and rel_err(va, vb) < 1e-12
+
+
+# ---- adjoint (no reference counterpart): the oracle's terms against central
+# differences of the reference-pinned element functions ----
+
+def _fd(f, x, h):
+    x = np.array(x, np.float64)
+    out = []
+    for i in range(x.size):
+        xp, xm = x.copy(), x.copy()
+        xp.flat[i] += h
+        xm.flat[i] -= h
+        out.append((np.asarray(f(xp)) - np.asarray(f(xm))) / (2 * h))
+    return np.array(out)
+
+
+def test_pd_jacobian_matches_differences(port):
+    rng = np.random.default_rng(4)
+    branches = set()
+    for _ in range(300):
+        s = rng.standard_normal(3)
+        b, e = 0.5 * (s[0] + s[1]), np.hypot(0.5 * (s[0] - s[1]), s[2])
+        if min(abs(b - e), abs(b + e)) < 1e-3:
+            continue  # too close to a branch switch for differences
+        branches.add((b - e > 0, b + e < 0))
+        J = CL.pd_sim22_jac(port, s)
+        fd = _fd(lambda v: CL.make_pd_sim22(port, v), s, 1e-7).T
+        assert np.abs(J - fd).max() < 1e-6 * max(1.0, np.abs(fd).max())
+    assert len(branches) == 3  # kept, zeroed and rank-1 cases all met
+
+
+def _sheet(port, ndiv, rng, amp):
+    x0, tri, quad = CL.cloth_square(port, ndiv)
+    ind, psup = port.psup(quad, 4, x0.size // 3)
+    x = x0 + amp / ndiv * rng.standard_normal(x0.size)
+    return x0, tri, quad, ind, psup, x
+
+
+def test_adjoint_terms_match_differences(port):
+    rng = np.random.default_rng(8)
+    x0, tri, quad, ind, psup, x = _sheet(port, 3, rng, 0.3)
+    young = rng.uniform(500, 2000, tri.size // 3)
+    nu, kb = 0.3, 1e-3
+    mu, dx = rng.standard_normal(x.size), rng.standard_normal(x.size)
+    xbar, Ebar = np.zeros(x.size), np.zeros(tri.size // 3)
+    CL.adjoint_terms(port, x0, x, tri, quad, young, nu, kb, mu, dx, xbar, Ebar)
+
+    def grad(xx, E=young):
+        return CL.cloth_assemble(port, ind, psup, x0, xx, tri, quad, E, nu, kb)[3]
+
+    def phi(xx, E=young):
+        _, vc, vd, _ = CL.cloth_assemble(port, ind, psup, x0, xx, tri, quad, E, nu, kb)
+        Ad = port.matvec(ind, psup, vc, vd, np.zeros_like(dx), 1.0, dx, 0.0)
+        return mu @ Ad
+
+    h = 1e-6 / 3
+    Hmu = (grad(x + h * mu) - grad(x - h * mu)) / (2 * h)
+    gphi = _fd(phi, x, h)
+    want = -Hmu - gphi
+    assert rel_err(xbar, want) < 1e-6
+    # per-triangle modulus: d/dE_t of (mu . dW + mu^T A dx)
+    for t in range(0, tri.size // 3, 3):
+        def s(E):
+            yy = young.copy()
+            yy[t] = E
+            return mu @ grad(x, yy) + phi(x, yy)
+        hE = 1e-4 * young[t]
+        fd = (s(young[t] + hE) - s(young[t] - hE)) / (2 * hE)
+        assert abs(Ebar[t] + fd) < 1e-6 * max(abs(fd), np.abs(Ebar).max())
+
+
+def test_rollout_adjoint_matches_differences(port):
+    """dL/dE of L = |x_N - x*|^2 / 2 over three backward-Euler steps (PCG to
+    1e-14 so that the discrete map is the differentiated one)."""
+    rng = np.random.default_rng(12)
+    ndiv = 4
+    x0, tri, quad = CL.cloth_square(port, ndiv)
+    np_ = x0.size // 3
+    ind, psup = port.psup(quad, 4, np_)
+    bc = np.zeros(np_ * 3, np.int32)
+    bc[0:3] = 1
+    bc[ndiv * 3:ndiv * 3 + 3] = 1
+    young = rng.uniform(50, 200, tri.size // 3)
+    target = x0 + 0.05 * rng.standard_normal(x0.size)
+    args = dict(nu=0.3, stiff_bend=1e-3, mass=1.0 / np_, dt=0.01, tol=1e-14, max_iter=2000)
+
+    def loss(E):
+        xs, v = CL.rollout(port, ind, psup, x0, bc, tri, quad, E, args["nu"], args["stiff_bend"], [0, 0, -10.0],
+                           args["mass"], args["dt"], args["tol"], args["max_iter"], 3)
+        return 0.5 * np.sum((xs[-1] - target) ** 2), xs
+
+    L, xs = loss(young)
+    xbar, vbar, Ebar = CL.rollout_adjoint(port, ind, psup, x0, xs, bc, tri, quad, young, args["nu"],
+                                          args["stiff_bend"], args["mass"], args["dt"], args["tol"],
+                                          args["max_iter"], xs[-1] - target, np.zeros_like(x0))
+    for t in rng.choice(tri.size // 3, 6, replace=False):
+        h = 1e-5 * young[t]
+        yp, ym = young.copy(), young.copy()
+        yp[t] += h
+        ym[t] -= h
+        fd = (loss(yp)[0] - loss(ym)[0]) / (2 * h)
+        assert abs(Ebar[t] - fd) < 1e-5 * np.abs(Ebar).max(), (t, Ebar[t], fd)
