@@ -31,6 +31,7 @@ F32 = 1
 SWEEP_SYNCFREE = 0
 SWEEP_LEVELS = 1
 SWEEP_GROUPS = 2
+SWEEP_BLOCK = 3
 
 
 class SolveStats(C.Structure):

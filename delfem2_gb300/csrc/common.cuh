@@ -253,6 +253,7 @@ struct dfm2g_ilu_s {
   // level sets: level[i], order (rows by (level,row)), level_start (nlev+1)
   dfm2g::DevBuf<unsigned> level_f, order_f, lstart_f, level_b, order_b, lstart_b;
   dfm2g::DevBuf<uint4> meta_f, meta_b;  // per position of the level order: {row, s0, s1, 0}
+  dfm2g::DevBuf<unsigned> pos_f, pos_b; // position of each row in the level order
   GroupSched gs_f, gs_b;                // FP32 blob schedules (forward, backward)
   std::vector<unsigned> group_of;       // blob of each row
   unsigned nlev_f = 0, nlev_b = 0;

@@ -52,9 +52,12 @@ enum dfm2g_prec { DFM2G_F64 = 0, DFM2G_F32 = 1 };
 enum dfm2g_sweep {
   DFM2G_SWEEP_SYNCFREE = 0, /* one persistent launch, per-row readiness     */
   DFM2G_SWEEP_LEVELS = 1,   /* one launch per level set                     */
-  DFM2G_SWEEP_GROUPS = 2    /* FP32: rows in compact blobs, one CTA per blob
+  DFM2G_SWEEP_GROUPS = 2,   /* FP32: rows in compact blobs, one CTA per blob
                                (shared-memory dependencies inside a blob);
                                FP64 sweeps use the sync-free schedule        */
+  DFM2G_SWEEP_BLOCK = 3     /* one CTA walks the levels, one barrier per level,
+                               recent results in a shared-memory ring (for
+                               patterns with few rows per level)             */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>, 3x3  */

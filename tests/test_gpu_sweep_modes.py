@@ -1,0 +1,61 @@
+"""Sweep schedules on patterns that stress their edge paths, against the oracle.
+
+The arrow pattern (row 0 coupled to every row) has two levels per direction:
+the forward sweep's second level reads row 0 from more than a shared-memory
+ring's length back (the single-CTA schedule's global-memory path), and the
+backward sweep's row 0 has n-1 blocks (the long-row paths). The chain pattern
+(tridiagonal blocks) has one row per level (n levels). Tolerance 1e-12
+relative (FP64), 1e-5 (FP32).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(kind, n, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "arrow":
+        nbr = [list(range(1, n))] + [[0] for _ in range(1, n)]
+    else:
+        nbr = [[j for j in (i - 1, i + 1) if 0 <= j < n] for i in range(n)]
+    ind = np.zeros(n + 1, np.uint32)
+    ind[1:] = np.cumsum([len(a) for a in nbr])
+    psup = np.array([j for a in nbr for j in a], np.uint32)
+    vc = 0.1 * rng.standard_normal(psup.size * 9) / max(1.0, np.sqrt(n) if kind == "arrow" else 1.0)
+    vd = np.tile(np.eye(3).ravel(), n) * 4.0 + 0.1 * rng.standard_normal(n * 9)
+    return ind, psup, vc, vd
+
+
+@pytest.mark.parametrize("kind,n", [("arrow", 20000), ("chain", 3000)])
+@pytest.mark.parametrize("mode", [0, 1, 3])
+def test_sweep_modes_on_edge_patterns(gpu, port, kind, n, mode):
+    import delfem2_gb300 as D
+    ind, psup, vc, vd = _system(kind, n, 3)
+    K = D.CMatrixSparse()
+    K.Initialize(n, 3, True)
+    K.SetPattern(ind, psup)
+    K.set_values(vc, vd)
+    ilu = D.CPreconditionerILU()
+    ilu.SetPattern0(K)
+    ilu.CopyValue(K)
+    assert ilu.Decompose()
+    ilu.set_sweep_mode(mode)
+    col, dia = port.ilu_pattern0(ind, psup)
+    ivc, ivd = port.ilu_copy_value(ind, col, psup, vc, vd)
+    st, _ = port.ilu_decompose(ind, col, dia, ivc, ivd)
+    assert st == 0
+    v = np.random.default_rng(5).standard_normal(n * 3)
+    f = v.copy()
+    ilu.ForwardSubstitution(f)
+    fo = port.ilu_forward(ind, col, dia, ivc, ivd, v)
+    assert rel_err(f, fo) < 1e-12
+    g = fo.copy()
+    ilu.BackwardSubstitution(g)
+    go = port.ilu_backward(ind, col, dia, ivc, fo)
+    assert rel_err(g, go) < 1e-12
+    z32 = v.astype(np.float32)
+    ilu.SolvePrecond(z32)
+    assert rel_err(z32, go) < 1e-5
