@@ -32,6 +32,7 @@ SWEEP_SYNCFREE = 0
 SWEEP_LEVELS = 1
 SWEEP_GROUPS = 2
 SWEEP_BLOCK = 3
+SWEEP_PARTS = 4
 
 
 class SolveStats(C.Structure):

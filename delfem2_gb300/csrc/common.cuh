@@ -242,6 +242,13 @@ struct GroupSched {
   bool values_ok = false;
 };
 
+// Row-range partition of one sweep direction (parts.cu): per part, its rows in
+// the sweep's level order as position metadata {row, s0, s1, 0}.
+struct PartSched {
+  dfm2g::DevBuf<uint4> meta;
+  dfm2g::DevBuf<unsigned> pstart;  // nparts+1 offsets into meta
+};
+
 struct dfm2g_ilu_s {
   unsigned nblk = 0;
   size_t nnz = 0;
@@ -255,6 +262,9 @@ struct dfm2g_ilu_s {
   dfm2g::DevBuf<uint4> meta_f, meta_b;  // per position of the level order: {row, s0, s1, 0}
   dfm2g::DevBuf<unsigned> pos_f, pos_b; // position of each row in the level order
   GroupSched gs_f, gs_b;                // FP32 blob schedules (forward, backward)
+  PartSched parts_f, parts_b;           // row-range partitions (forward, backward)
+  bool parts_ok = false;
+  unsigned parts_rpp = 0, parts_n = 0;  // rows per part, number of parts
   std::vector<unsigned> group_of;       // blob of each row
   unsigned nlev_f = 0, nlev_b = 0;
   std::vector<unsigned> h_lstart_f, h_lstart_b;
@@ -289,6 +299,10 @@ int build_slot_map(const unsigned *d_elem, size_t nelem, unsigned nno, const dfm
 int group_schedules_build(dfm2g_ilu_s *p);
 int group_values_fill(dfm2g_ilu_s *p);
 int group_sweep(dfm2g_ilu_s *p, bool forward, const float *in, float *out, const int *skip);
+int part_schedules_build(dfm2g_ilu_s *p);
+template <typename T>
+int part_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
+               unsigned long long timeout);
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta);
 int ilu_ensure_f32(dfm2g_ilu_s *p);
 int bsr_ensure_f32(dfm2g_bsr_s *m);

@@ -700,6 +700,11 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
   if (p->sweep_mode == DFM2G_SWEEP_BLOCK)
     return forward ? launch_sweep_block<T, true>(p, in, out, vcrs, vdia, skip)
                    : launch_sweep_block<T, false>(p, in, out, vcrs, vdia, skip);
+  if (p->sweep_mode == DFM2G_SWEEP_PARTS && p->parts_ok) {
+    if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
+    const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+    return part_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev);
+  }
   // sync-free and blob schedules: `out` is filled with the pending marker
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
   if constexpr (sizeof(T) == 4) {
@@ -818,6 +823,7 @@ int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
   DFM2G_TRY(compute_levels(p, false));
   DFM2G_TRY(compute_levels(p, true));
   DFM2G_TRY(group_schedules_build(p));
+  DFM2G_TRY(part_schedules_build(p));
   // The blob schedule is correct but, with one CTA barrier per unit, a single
   // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
   // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
@@ -963,8 +969,10 @@ int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) { return 
 int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
-      mode != DFM2G_SWEEP_BLOCK)
+      mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
+  if (mode == DFM2G_SWEEP_PARTS && !p->parts_ok)
+    return fail(DFM2G_ERR_UNSUPPORTED, "row-range partition unavailable for this pattern");
   if (mode == DFM2G_SWEEP_GROUPS && !(p->gs_f.ok && p->gs_b.ok))
     return fail(DFM2G_ERR_UNSUPPORTED, "blob schedule unavailable for this pattern");
   p->sweep_mode = mode;

@@ -55,9 +55,14 @@ enum dfm2g_sweep {
   DFM2G_SWEEP_GROUPS = 2,   /* FP32: rows in compact blobs, one CTA per blob
                                (shared-memory dependencies inside a blob);
                                FP64 sweeps use the sync-free schedule        */
-  DFM2G_SWEEP_BLOCK = 3     /* one CTA walks the levels, one barrier per level,
+  DFM2G_SWEEP_BLOCK = 3,    /* one CTA walks the levels, one barrier per level,
                                recent results in a shared-memory ring (for
                                patterns with few rows per level)             */
+  DFM2G_SWEEP_PARTS = 4     /* sync-free over contiguous row ranges, one CTA
+                               per range: dependencies inside a range are
+                               polled in shared memory, only cross-range ones
+                               in global memory (when a range's results fit
+                               in shared memory)                            */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>, 3x3  */
