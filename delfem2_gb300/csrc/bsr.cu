@@ -9,6 +9,7 @@
 
 #include "common.cuh"
 #include "rowkern.cuh"
+#include "spmv_tma.cuh"
 
 namespace dfm2g {
 
@@ -32,7 +33,103 @@ __global__ void __launch_bounds__(256) k_bsr_spmv(unsigned nblk, const unsigned 
   });
 }
 
+// Same product through the TMA-staged pipeline of spmv_tma.cuh.
+template <typename T>
+__global__ void __launch_bounds__(kTmaThreads, 2) k_bsr_spmv_tma(const unsigned *__restrict__ tiles, unsigned ntiles,
+                                                                 const unsigned *__restrict__ row_start,
+                                                                 const unsigned *__restrict__ col,
+                                                                 const T *__restrict__ vcrs,
+                                                                 const T *__restrict__ vdia, T *__restrict__ y,
+                                                                 T alpha, const T *__restrict__ x, T beta, int *err,
+                                                                 unsigned long long timeout_ns) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  const unsigned lane = threadIdx.x & 31;
+  spmv_tma_rows<T>(tiles, ntiles, row_start, col, vcrs, vdia, x, err, timeout_ns, tma_smem,
+                   [&](unsigned row, const T s[3]) {
+                     if (lane < 3) {
+                       T *py = y + (size_t)row * 3 + lane;
+                       *py = beta * *py + alpha * pick3(s, lane);
+                     }
+                   });
+}
+
+// Tiles of consecutive rows with at most `maxb` off-diagonal blocks and `maxr`
+// rows each; false when one row alone has more than `maxb` blocks.
+static bool make_tiles(const std::vector<unsigned> &rs, unsigned nblk, unsigned maxb, unsigned maxr,
+                       std::vector<unsigned> &t) {
+  t.assign(1, 0u);
+  unsigned r0 = 0;
+  for (unsigned i = 0; i < nblk; ++i) {
+    if (rs[i + 1] - rs[i] > maxb) return false;
+    if (rs[i + 1] - rs[r0] > maxb || i + 1 - r0 > maxr) {
+      t.push_back(i);
+      r0 = i;
+    }
+  }
+  if (nblk) t.push_back(nblk);
+  return true;
+}
+
+int bsr_tiles_build(dfm2g_bsr_s *m) {
+  m->tiles_ok = false;
+  std::vector<unsigned> t32, t64;
+  if (m->nblk == 0 || !make_tiles(m->h_row_start, m->nblk, TileCfg<float>::kBlocks, TileCfg<float>::kRows, t32) ||
+      !make_tiles(m->h_row_start, m->nblk, TileCfg<double>::kBlocks, TileCfg<double>::kRows, t64))
+    return DFM2G_OK;
+  DFM2G_TRY(m->tiles32.resize(t32.size()));
+  DFM2G_TRY(m->tiles64.resize(t64.size()));
+  DFM2G_TRY(m->err.resize(1));
+  DFM2G_CUDA(cudaMemcpyAsync(m->tiles32.p, t32.data(), sizeof(unsigned) * t32.size(), cudaMemcpyHostToDevice,
+                             stream()));
+  DFM2G_CUDA(cudaMemcpyAsync(m->tiles64.p, t64.data(), sizeof(unsigned) * t64.size(), cudaMemcpyHostToDevice,
+                             stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->err.p, 0, sizeof(int), stream()));
+  static int attr_device = -1;  // opt the kernels in to their shared memory once per device
+  if (attr_device != ctx().device) {
+    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)TileCfg<float>::kSmem));
+    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)TileCfg<double>::kSmem));
+    attr_device = ctx().device;
+  }
+  m->ntiles32 = (unsigned)t32.size() - 1;
+  m->ntiles64 = (unsigned)t64.size() - 1;
+  m->tiles_ok = true;
+  return DFM2G_OK;
+}
+
+// Reads and clears the SpMV error word (a bounded wait that gave up).
+int bsr_check_err(dfm2g_bsr_s *m) {
+  if (!m->tiles_ok) return DFM2G_OK;
+  int e = 0;
+  DFM2G_CUDA(cudaMemcpyAsync(&e, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (e) {
+    DFM2G_CUDA(cudaMemsetAsync(m->err.p, 0, sizeof(int), stream()));
+    return fail(DFM2G_ERR_WAIT_TIMEOUT, "SpMV: a pipeline wait timed out");
+  }
+  return DFM2G_OK;
+}
+
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta) {
+  if (m->tiles_ok && (prec == DFM2G_F64 || prec == DFM2G_F32)) {
+    const unsigned long long timeout = kWaitTimeoutNs;
+    if (prec == DFM2G_F64) {
+      const unsigned grid = std::min(m->ntiles64, (unsigned)ctx().num_sms * 2);
+      k_bsr_spmv_tma<double><<<grid, kTmaThreads, TileCfg<double>::kSmem, stream()>>>(
+          m->tiles64.p, m->ntiles64, m->row_start.p, m->col.p, m->vcrs.p, m->vdia.p, (double *)y, alpha,
+          (const double *)x, beta, m->err.p, timeout);
+    } else {
+      DFM2G_TRY(bsr_ensure_f32(m));
+      const unsigned grid = std::min(m->ntiles32, (unsigned)ctx().num_sms * 2);
+      k_bsr_spmv_tma<float><<<grid, kTmaThreads, TileCfg<float>::kSmem, stream()>>>(
+          m->tiles32.p, m->ntiles32, m->row_start.p, m->col.p, m->vcrs32.p, m->vdia32.p, (float *)y, (float)alpha,
+          (const float *)x, (float)beta, m->err.p, timeout);
+    }
+    note_launches(1);
+    DFM2G_LAUNCH_CHECK();
+    return DFM2G_OK;
+  }
   const unsigned blocks = blocks_for((size_t)m->nblk * 32, 256, (unsigned)ctx().num_sms * 16);
   if (prec == DFM2G_F64) {
     k_bsr_spmv<double><<<blocks, 256, 0, stream()>>>(m->nblk, m->row_start.p, m->col.p, m->vcrs.p,
@@ -62,8 +159,9 @@ void to_f32(size_t n, const double *in, float *out) {
 
 int bsr_ensure_f32(dfm2g_bsr_s *m) {
   if (m->f32_valid) return DFM2G_OK;
-  DFM2G_TRY(m->vcrs32.ensure(m->nnz * 9 + 1));
-  DFM2G_TRY(m->vdia32.ensure((size_t)m->nblk * 9 + 1));
+  // +8 floats: bulk copies round their byte range up to 16 B past the last element
+  DFM2G_TRY(m->vcrs32.ensure(m->nnz * 9 + 8));
+  DFM2G_TRY(m->vdia32.ensure((size_t)m->nblk * 9 + 8));
   const unsigned cap = (unsigned)ctx().num_sms * 8;
   if (m->nnz)
     k_to_f32<<<blocks_for(m->nnz * 9, 256, cap), 256, 0, stream()>>>(m->nnz * 9, m->vcrs.p, m->vcrs32.p);
@@ -265,9 +363,10 @@ int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_s
   m->h_row_start.assign(row_start, row_start + m->nblk + 1);
   m->h_col.assign(col, col + ncol);
   DFM2G_TRY(m->row_start.resize(m->nblk + 1));
-  DFM2G_TRY(m->col.resize(ncol + 1));
-  DFM2G_TRY(m->vcrs.resize(ncol * 9 + 1));
-  DFM2G_TRY(m->vdia.resize((size_t)m->nblk * 9 + 1));
+  // slack past the last element: bulk copies round their byte range up to 16 B
+  DFM2G_TRY(m->col.resize(ncol + 8));
+  DFM2G_TRY(m->vcrs.resize(ncol * 9 + 4));
+  DFM2G_TRY(m->vdia.resize((size_t)m->nblk * 9 + 4));
   DFM2G_CUDA(cudaMemcpyAsync(m->row_start.p, row_start, sizeof(unsigned) * (m->nblk + 1), cudaMemcpyHostToDevice,
                              stream()));
   if (ncol) DFM2G_CUDA(cudaMemcpyAsync(m->col.p, col, sizeof(unsigned) * ncol, cudaMemcpyHostToDevice, stream()));
@@ -277,6 +376,8 @@ int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_s
   m->has_pattern = true;
   m->f32_valid = false;
   m->pattern_version++;
+  DFM2G_TRY(bsr_tiles_build(m));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
 }
 
@@ -350,6 +451,7 @@ int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x
     DFM2G_TRY(ay.in((double *)y, n, mem, true));
     DFM2G_TRY(ax.in((const double *)x, n, mem, true));
     DFM2G_TRY(bsr_spmv(m, prec, ay.dev(), alpha, ax.dev(), beta));
+    DFM2G_TRY(bsr_check_err(m));
     return ay.copy_back();
   }
   if (prec == DFM2G_F32) {
@@ -357,6 +459,7 @@ int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x
     DFM2G_TRY(ay.in((float *)y, n, mem, true));
     DFM2G_TRY(ax.in((const float *)x, n, mem, true));
     DFM2G_TRY(bsr_spmv(m, prec, ay.dev(), alpha, ax.dev(), beta));
+    DFM2G_TRY(bsr_check_err(m));
     return ay.copy_back();
   }
   return fail(DFM2G_ERR_ARG, "matvec: prec must be DFM2G_F64 or DFM2G_F32");

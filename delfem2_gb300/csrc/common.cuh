@@ -225,6 +225,12 @@ struct dfm2g_bsr_s {
   dfm2g::DevBuf<float> vcrs32, vdia32;
   bool f32_valid = false;
   unsigned pattern_version = 0;
+  // row tiles of the TMA-staged SpMV (FP32 and FP64 tile sizes); tiles_ok is
+  // false when a row alone exceeds a tile
+  dfm2g::DevBuf<unsigned> tiles32, tiles64;
+  unsigned ntiles32 = 0, ntiles64 = 0;
+  bool tiles_ok = false;
+  dfm2g::DevBuf<int> err;  // bounded-wait error word of the SpMV kernels
 };
 
 // Blob schedule of one sweep direction (FP32): rows partitioned into compact
@@ -304,6 +310,8 @@ template <typename T>
 int part_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout);
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta);
+int bsr_tiles_build(dfm2g_bsr_s *m);
+int bsr_check_err(dfm2g_bsr_s *m);
 int ilu_ensure_f32(dfm2g_ilu_s *p);
 int bsr_ensure_f32(dfm2g_bsr_s *m);
 }  // namespace dfm2g

@@ -13,6 +13,7 @@
 
 #include "common.cuh"
 #include "rowkern.cuh"
+#include "spmv_tma.cuh"
 
 namespace dfm2g {
 
@@ -70,6 +71,58 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pAp(IterState *st, unsigned n
   if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
     st->alpha = st->rPr / total;
   }
+}
+
+// Ap = K p and alpha = rPr / (p, Ap) through the TMA-staged pipeline of
+// spmv_tma.cuh (the producer warp contributes 0 to the dot product).
+template <typename T>
+__global__ void __launch_bounds__(kTmaThreads, 2) k_spmv_pAp_tma(IterState *st, const unsigned *__restrict__ tiles,
+                                                                 unsigned ntiles,
+                                                                 const unsigned *__restrict__ row_start,
+                                                                 const unsigned *__restrict__ col,
+                                                                 const T *__restrict__ vcrs,
+                                                                 const T *__restrict__ vdia, const T *__restrict__ p,
+                                                                 T *__restrict__ Ap, double *partials, int *err,
+                                                                 unsigned long long timeout_ns) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  __shared__ double sh[32];
+  if (st->done) return;
+  const unsigned lane = threadIdx.x & 31;
+  double dot = 0.0;
+  spmv_tma_rows<T>(tiles, ntiles, row_start, col, vcrs, vdia, p, err, timeout_ns, tma_smem,
+                   [&](unsigned row, const T s[3]) {
+                     if (lane < 3) {
+                       const T v = pick3(s, lane);
+                       Ap[(size_t)row * 3 + lane] = v;
+                       dot += (double)(v * p[(size_t)row * 3 + lane]);
+                     }
+                   });
+  double total;
+  if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
+    st->alpha = st->rPr / total;
+  }
+}
+
+template <typename T>
+static int launch_spmv_pAp(dfm2g_bsr_s *m, IterState *st, const T *vcrs, const T *vdia, const T *pv, T *Ap,
+                           double *partials, unsigned spmv_blocks) {
+  if (m->tiles_ok) {
+    static int attr_device = -1;  // per instantiation, once per device
+    if (attr_device != ctx().device) {
+      DFM2G_CUDA(cudaFuncSetAttribute(k_spmv_pAp_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)TileCfg<T>::kSmem));
+      attr_device = ctx().device;
+    }
+    const unsigned nt = sizeof(T) == 8 ? m->ntiles64 : m->ntiles32;
+    const unsigned *tiles = sizeof(T) == 8 ? m->tiles64.p : m->tiles32.p;
+    const unsigned grid = std::min(nt, (unsigned)ctx().num_sms * 2);
+    k_spmv_pAp_tma<T><<<grid, kTmaThreads, TileCfg<T>::kSmem, stream()>>>(
+        st, tiles, nt, m->row_start.p, m->col.p, vcrs, vdia, pv, Ap, partials, m->err.p, kWaitTimeoutNs);
+  } else {
+    k_spmv_pAp<T><<<spmv_blocks, kThreads, 0, stream()>>>(st, m->nblk, m->row_start.p, m->col.p, vcrs, vdia, pv, Ap,
+                                                         partials);
+  }
+  return DFM2G_OK;
 }
 
 // Reliable update, part 1: x64 += x32, x32 = 0 (only when a refresh is due).
@@ -428,8 +481,7 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
       T *Ap = Pr;
       {
         ProfScope ps(DFM2G_PROF_SPMV, 1);
-        k_spmv_pAp<T><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p, vcrs, vdia, pv,
-                                                             Ap, g_ws.partials.p);
+        DFM2G_TRY(launch_spmv_pAp<T>(m, st, vcrs, vdia, pv, Ap, g_ws.partials.p, spmv_blocks));
       }
       {
         ProfScope ps(DFM2G_PROF_UPDATE, 1);
@@ -485,7 +537,7 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
       return fail(DFM2G_ERR_WAIT_TIMEOUT, "PCG: a triangular-sweep wait timed out");
     }
   }
-  return DFM2G_OK;
+  return bsr_check_err(m);
 }
 
 static int check_pair(dfm2g_bsr m, dfm2g_ilu p) {

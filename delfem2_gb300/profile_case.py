@@ -1,10 +1,11 @@
 """One static-elasticity solve on a voxel block, for profiler captures.
 
-  python -m delfem2_gb300.profile_case [--nx 64 --ny 64 --nz 64] [--fp64] [--solves 1]
+  python -m delfem2_gb300.profile_case [--nx 64 --ny 64 --nz 64] [--fp64] [--solves 1] [--method reliable]
 
 Sets the problem up (mesh, pattern, level sets, assembly, ILU(0)) and runs
 `--solves` solves of K u = b to 1e-10 (FP32-inner/FP64-refinement by default,
-plain FP64 Solve_PCG with --fp64), printing the device time of each.
+with reliable updates or restarted refinement; plain FP64 Solve_PCG with
+--fp64), printing the device time of each.
 """
 from __future__ import annotations
 
@@ -20,6 +21,7 @@ def main():
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--levels", action="store_true", help="level-by-level sweep schedule")
+    ap.add_argument("--method", choices=["reliable", "restart"], default="reliable")
     args = ap.parse_args()
 
     import torch
@@ -42,7 +44,7 @@ def main():
             print(f"solve {k}: fp64 {len(hist) - 1} iterations, {1e3 * (time.perf_counter() - t):.1f} ms")
         else:
             x = torch.zeros_like(b)
-            st = D.Solve_PCG_Mixed(b, x, 1e-10, P.K, P.ilu)
+            st = D.Solve_PCG_Mixed(b, x, 1e-10, P.K, P.ilu, method=args.method)
             torch.cuda.synchronize()
             print(f"solve {k}: mixed {st.iterations} inner / {st.outer} outer, rel {st.rel_residual:.2e}, "
                   f"{1e3 * (time.perf_counter() - t):.1f} ms")
