@@ -255,6 +255,19 @@ struct PartSched {
   dfm2g::DevBuf<unsigned> pstart;  // nparts+1 offsets into meta
 };
 
+// Level-ordered record stream of one sweep direction and value type
+// (stream.cu): unit descriptors, records, and where each factor block goes.
+struct StreamSched {
+  bool built = false, ok = false;
+  unsigned nunits = 0;
+  size_t nvblocks = 0;
+  unsigned values_version = ~0u;  // factor_version the values were copied from
+  dfm2g::DevBuf<unsigned char> bytes;
+  dfm2g::DevBuf<uint4> units;     // 2 per unit
+  dfm2g::DevBuf<unsigned> vsrc;   // factor block: slot, or nnz + row for D^-1
+  dfm2g::DevBuf<size_t> vdst;     // its first value in the stream
+};
+
 struct dfm2g_ilu_s {
   unsigned nblk = 0;
   size_t nnz = 0;
@@ -269,6 +282,10 @@ struct dfm2g_ilu_s {
   dfm2g::DevBuf<unsigned> pos_f, pos_b; // position of each row in the level order
   GroupSched gs_f, gs_b;                // FP32 blob schedules (forward, backward)
   PartSched parts_f, parts_b;           // row-range partitions (forward, backward)
+  StreamSched ss32_f, ss32_b, ss64_f, ss64_b;  // level streams of the single-CTA sweep
+  dfm2g::DevBuf<double> in_lv64;        // right-hand side gathered in level order
+  dfm2g::DevBuf<float> in_lv32;
+  unsigned factor_version = 0;          // incremented by each decomposition
   bool parts_ok = false;
   unsigned parts_rpp = 0, parts_n = 0;  // rows per part, number of parts
   std::vector<unsigned> group_of;       // blob of each row
@@ -306,6 +323,10 @@ int group_schedules_build(dfm2g_ilu_s *p);
 int group_values_fill(dfm2g_ilu_s *p);
 int group_sweep(dfm2g_ilu_s *p, bool forward, const float *in, float *out, const int *skip);
 int part_schedules_build(dfm2g_ilu_s *p);
+template <typename T>
+int stream_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
+                 unsigned long long timeout, bool *usable);
+void stream_schedules_reset(dfm2g_ilu_s *p);
 template <typename T>
 int part_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout);

@@ -477,147 +477,6 @@ __global__ void __launch_bounds__(256) k_sweep_level(const uint4 *__restrict__ m
   sweep_finish<T, FWD, false>(R, L, lane, col, vcrs, out, nullptr, 0);
 }
 
-// Single-CTA sweep for patterns with few rows per level. The CTA walks the
-// levels with one barrier between consecutive levels; warp w takes positions
-// a+w, a+w+NW, ... of level [a, b). Every result goes to `out` and to the
-// shared-memory ring slot (position mod kSlots). A dependency at position p
-// is read from the ring when no position of the current level can have reused
-// its slot (p >= b - kSlots), else from `out` with ordinary loads (ordered by
-// the barrier). Each warp loads its next row (values, right-hand side,
-// dependency positions) before it finishes the current one, across the
-// barrier too: none of that depends on results.
-template <typename T>
-struct BlockRow {
-  static constexpr unsigned kRounds = 4;
-  RowFrag<T, kRounds> f;
-  unsigned pos[kRounds];  // level-order position of each round's block column
-  unsigned i, s0, s1, q;
-  T in[3];
-  T d[3];
-};
-
-template <typename T>
-struct BlockRing {
-  static constexpr unsigned kSlots = sizeof(T) == 8 ? 8192u : 16384u;  // 192 KiB either way
-  static constexpr size_t kBytes = (size_t)kSlots * 3 * sizeof(T);
-};
-
-template <typename T, bool FWD>
-__device__ __forceinline__ void block_load(BlockRow<T> &R, const RowLane &L, unsigned lane, unsigned q,
-                                           const uint4 *__restrict__ meta, const unsigned *__restrict__ pos,
-                                           const unsigned *__restrict__ col, const T *__restrict__ vcrs,
-                                           const T *__restrict__ vdia, const T *__restrict__ in) {
-  const uint4 m = meta[q];
-  R.q = q;
-  R.i = m.x;
-  R.s0 = m.y;
-  R.s1 = m.z;
-  row_load(R.f, L, m.y, m.z, col, vcrs, ~0u, (const T *)nullptr);
-#pragma unroll
-  for (unsigned k = 0; k < BlockRow<T>::kRounds; ++k)
-    R.pos[k] = (L.active && 3u * k + L.g < R.f.nb) ? pos[R.f.j[k]] : 0u;
-  if (lane < 3) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) R.in[k] = in[(size_t)m.x * 3 + k];
-    if (FWD) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) R.d[k] = vdia[(size_t)m.x * 9 + lane * 3 + k];
-    }
-  }
-}
-
-template <typename T, bool FWD>
-__device__ __forceinline__ void block_finish(const BlockRow<T> &R, const RowLane &L, unsigned lane, unsigned lim,
-                                             const unsigned *__restrict__ col, const T *__restrict__ vcrs, T *out,
-                                             T (*ring)[3]) {
-  constexpr unsigned S = BlockRing<T>::kSlots;
-  T acc = T(0);
-  if (R.f.nb <= 3 * BlockRow<T>::kRounds) {
-#pragma unroll
-    for (unsigned k = 0; k < BlockRow<T>::kRounds; ++k) {
-      if (L.active && 3u * k + L.g < R.f.nb) {
-        const unsigned p = R.pos[k];
-        const T xv = (p >= lim) ? ring[p & (S - 1)][L.c] : out[(size_t)R.f.j[k] * 3 + L.c];
-        acc += R.f.v[k] * xv;
-      }
-    }
-  } else if (L.active) {
-    for (unsigned t = L.g; t < R.s1 - R.s0; t += 3u) {
-      const unsigned j = col[R.s0 + t];
-      acc += vcrs[(size_t)(R.s0 + t) * 9 + L.e] * out[(size_t)j * 3 + L.c];
-    }
-  }
-  T s[3];
-  row_reduce(acc, s);
-  if (lane < 3) {
-    const T t0 = R.in[0] - s[0], t1 = R.in[1] - s[1], t2 = R.in[2] - s[2];
-    T z;
-    if (FWD)
-      z = R.d[0] * t0 + R.d[1] * t1 + R.d[2] * t2;
-    else
-      z = lane == 0 ? t0 : (lane == 1 ? t1 : t2);
-    out[(size_t)R.i * 3 + lane] = z;
-    ring[R.q & (S - 1)][lane] = z;
-  }
-}
-
-template <typename T, bool FWD, unsigned NT>
-__global__ void __launch_bounds__(NT) k_sweep_block(const uint4 *__restrict__ meta, const unsigned *__restrict__ pos,
-                                                    const unsigned *__restrict__ lstart, unsigned nlev,
-                                                    const unsigned *__restrict__ col, const T *__restrict__ vcrs,
-                                                    const T *__restrict__ vdia, const T *__restrict__ in, T *out,
-                                                    const int *skip) {
-  extern __shared__ __align__(16) unsigned char block_smem[];
-  T(*ring)[3] = reinterpret_cast<T(*)[3]>(block_smem);
-  if (skip && *skip) return;
-  constexpr unsigned NW = NT / 32u, S = BlockRing<T>::kSlots;
-  const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-  const RowLane L(lane);
-  BlockRow<T> nxt;
-  unsigned a = lstart[0], b = lstart[1];
-  if (a + w < b) block_load<T, FWD>(nxt, L, lane, a + w, meta, pos, col, vcrs, vdia, in);
-  for (unsigned l = 0; l < nlev; ++l) {
-    const unsigned na = b, nb = (l + 1 < nlev) ? lstart[l + 2] : b;
-    const unsigned lim = b > S ? b - S : 0u;
-    unsigned q = a + w;
-    if (q >= b && na + w < nb) block_load<T, FWD>(nxt, L, lane, na + w, meta, pos, col, vcrs, vdia, in);
-    for (; q < b; q += NW) {
-      const BlockRow<T> cur = nxt;
-      const unsigned qn = q + NW;
-      if (qn < b)
-        block_load<T, FWD>(nxt, L, lane, qn, meta, pos, col, vcrs, vdia, in);
-      else if (na + w < nb)
-        block_load<T, FWD>(nxt, L, lane, na + w, meta, pos, col, vcrs, vdia, in);
-      block_finish<T, FWD>(cur, L, lane, lim, col, vcrs, out, ring);
-    }
-    __syncthreads();
-    a = na;
-    b = nb;
-  }
-}
-
-constexpr unsigned kBlockSweepThreads = 512;
-
-template <typename T, bool FWD>
-static int launch_sweep_block(dfm2g_ilu_s *p, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip) {
-  auto kernel = k_sweep_block<T, FWD, kBlockSweepThreads>;
-  static int attr_device = -1;  // per instantiation: opt-in to the ring's shared memory once per device
-  if (attr_device != ctx().device) {
-    DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)BlockRing<T>::kBytes));
-    attr_device = ctx().device;
-  }
-  const uint4 *meta = FWD ? p->meta_f.p : p->meta_b.p;
-  const unsigned *pos = FWD ? p->pos_f.p : p->pos_b.p;
-  const unsigned *ls = FWD ? p->lstart_f.p : p->lstart_b.p;
-  const unsigned nlev = FWD ? p->nlev_f : p->nlev_b;
-  kernel<<<1, kBlockSweepThreads, BlockRing<T>::kBytes, stream()>>>(meta, pos, ls, nlev, p->col.p, vcrs, vdia, in,
-                                                                    out, skip);
-  note_launches(1);
-  DFM2G_LAUNCH_CHECK();
-  return DFM2G_OK;
-}
-
 // Sync-free sweep: one persistent, co-resident (cooperative) grid; warp w
 // takes positions w, w+W, ... of the level order, and waits (bounded) on each
 // needed out_j until it is no longer the pending marker. Every row depends only
@@ -697,9 +556,12 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     return DFM2G_OK;
   }
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
-  if (p->sweep_mode == DFM2G_SWEEP_BLOCK)
-    return forward ? launch_sweep_block<T, true>(p, in, out, vcrs, vdia, skip)
-                   : launch_sweep_block<T, false>(p, in, out, vcrs, vdia, skip);
+  if (p->sweep_mode == DFM2G_SWEEP_BLOCK) {
+    const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+    bool usable = false;
+    DFM2G_TRY(stream_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, &usable));
+    if (usable) return DFM2G_OK;  // else (a row too long for a unit): the sync-free schedule below
+  }
   if (p->sweep_mode == DFM2G_SWEEP_PARTS && p->parts_ok) {
     if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
@@ -824,6 +686,7 @@ int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
   DFM2G_TRY(compute_levels(p, true));
   DFM2G_TRY(group_schedules_build(p));
   DFM2G_TRY(part_schedules_build(p));
+  stream_schedules_reset(p);
   // The blob schedule is correct but, with one CTA barrier per unit, a single
   // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
   // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
@@ -871,6 +734,7 @@ int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular) {
   if (n_singular) *n_singular = ns;
   p->has_factor = true;
   p->f32_valid = false;
+  p->factor_version++;
   if (ns > 10) return fail(DFM2G_ERR_SINGULAR_PIVOT, "ILU: %d pivots with |det| <= 1e-30", ns);
   return DFM2G_OK;
 }
