@@ -14,8 +14,8 @@
 //
 // CST quantities per triangle, in terms of the deformed edges g0 = c1 - c0,
 // g1 = c2 - c0 (fem_stvk.cpp:267-374):
-//   strain  E = (g0.g0 - G0.G0, g1.g1 - G1.G1, 2(g0.g1 - G0.G1)) / 2 ... as
-//           (E00, E11, 2E01); stress S = Cm E; W = A E.S / 2;
+//   strain  E = (E00, E11, 2 E01) = ((g0.g0 - G0.G0) / 2, (g1.g1 - G1.G1) / 2,
+//           g0.g1 - G0.G1); stress S = Cm E; W = A E.S / 2;
 //   dW_a    = A sum_p S_p beta_a^p with beta_a^0 = dN_a0 g0, beta_a^1 = dN_a1 g1,
 //             beta_a^2 = dN_a1 g0 + dN_a0 g1, dN = {(-1,-1), (1,0), (0,1)};
 //   K_ab    = A sum_pq beta_a^p Cm_pq beta_b^q^T + A (S+ : dN_a dN_b) I with S+
@@ -561,7 +561,7 @@ static int cloth_solve(dfm2g_bsr m, dfm2g_ilu p, double *rhs, double *y, double 
   const size_t n = (size_t)m->nblk * 3;
   int s;
   if (a.solver == DFM2G_CLOTH_PCG_MIXED) {
-    s = dfm2g_solve_pcg_mixed_reliable(m, p, rhs, y, a.tol, 1e-2, a.max_iter, DFM2G_MEM_DEVICE, st);
+    s = dfm2g_solve_pcg_mixed_reliable(m, p, rhs, y, a.tol, 0.1, a.max_iter, DFM2G_MEM_DEVICE, st);
   } else {
     DFM2G_CUDA(cudaMemcpyAsync(scratch, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
     s = dfm2g_solve_pcg(m, p, scratch, y, a.tol, a.max_iter, nullptr, 0, nullptr, DFM2G_MEM_DEVICE, st);

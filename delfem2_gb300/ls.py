@@ -299,20 +299,26 @@ def Solve_CG(r_vec, u_vec, conv_ratio_tol: float, max_iteration: int, mat: CMatr
     return list(hist[: min(nh.value, cap)])
 
 
+RELIABLE_REFRESH = 0.1  # |r| drop between FP64 residual refreshes of the reliable-update solver
+
+
 def Solve_PCG_Mixed(b_vec, x_vec, tol: float, mat: CMatrixSparse, ilu: CPreconditionerILU,
                     inner_tol: float = 1e-4, max_iter: int = 100000, max_outer: int = 100,
-                    allow_not_converged: bool = False, method: str = "restart") -> N.SolveStats:
+                    allow_not_converged: bool = False, method: str = "restart",
+                    refresh: float = RELIABLE_REFRESH) -> N.SolveStats:
     """FP32-inner / FP64-refinement PCG until |b - K x| / |b| < tol (b unchanged).
 
     method="reliable": one FP32 PCG whose residual is refreshed in FP64 each time
-    it has dropped by `inner_tol` (Krylov state kept); method="restart": classic
-    iterative refinement, a fresh FP32 PCG to `inner_tol` per FP64 step."""
+    it has dropped by the factor `refresh` (Krylov state kept; at 3.24M DOF a
+    refresh every 0.1 keeps the FP32 iteration count at the FP64 one);
+    method="restart": classic iterative refinement, a fresh FP32 PCG to
+    `inner_tol` per FP64 step."""
     pb, mb, kb = _vec(b_vec, np.float64, False)
     px, mx, kx = _vec(x_vec, np.float64, True)
     st = N.SolveStats()
     allow = (N.ERR_NOT_CONVERGED,) if allow_not_converged else ()
     if method == "reliable":
-        N.call("dfm2g_solve_pcg_mixed_reliable", mat._h, ilu._h, pb, px, float(tol), float(inner_tol),
+        N.call("dfm2g_solve_pcg_mixed_reliable", mat._h, ilu._h, pb, px, float(tol), float(refresh),
                int(max_iter), _same_mem(mb, mx), C.byref(st), allow=allow)
     elif method == "restart":
         N.call("dfm2g_solve_pcg_mixed", mat._h, ilu._h, pb, px, float(tol), float(inner_tol), int(max_iter),
