@@ -111,6 +111,13 @@ SIGNATURES = {
     "dfm2g_cloth_rollout": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp, _d, _d, _d, _u, _i, _u, _u, _pstats,
                             _i],
     "dfm2g_cloth_rollout_adjoint": [_vp, _vp, _vp, _vp, _vp, _vp, _pstats, _i],
+    "dfm2g_dev_alloc": [C.POINTER(_vp), _sz],
+    "dfm2g_dev_free": [_vp],
+    "dfm2g_dev_copy": [_vp, _vp, _sz, _i],
+    "dfm2g_vec_dot": [_vp, _vp, _sz, C.POINTER(C.c_double), _i],
+    "dfm2g_vec_axpy": [_vp, _d, _vp, _sz, _i],
+    "dfm2g_vec_scale_add": [_vp, _d, _vp, _sz, _i],
+    "dfm2g_vec_set_zero": [_vp, _sz, _i],
     "dfm2g_profile_enable": [_i],
     "dfm2g_profile_reset": [],
     "dfm2g_profile_read": [_i, _pu, C.POINTER(C.c_double)],

@@ -766,3 +766,105 @@ int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, 
 }
 
 }  // extern "C"
+
+// ---- device vectors of the compatibility path (view_vectorx.h:61-109) ----------------
+namespace dfm2g {
+namespace {
+__global__ void k_vec_axpy(size_t n, double *__restrict__ y, double a, const double *__restrict__ x) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+__global__ void k_vec_scale_add(size_t n, double *__restrict__ y, double b, const double *__restrict__ x) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = b * y[i] + x[i];
+}
+int vec_ws() {
+  DFM2G_TRY(ensure_context());
+  DFM2G_TRY(g_ws.partials.ensure((size_t)ctx().num_sms * 64));
+  DFM2G_TRY(g_ws.scal.ensure(8));
+  DFM2G_TRY(g_ws.tickets.ensure(4));
+  return DFM2G_OK;
+}
+}  // namespace
+}  // namespace dfm2g
+
+extern "C" {
+
+int dfm2g_dev_alloc(void **p, size_t bytes) {
+  if (!p) return fail(DFM2G_ERR_ARG, "dev_alloc: null out");
+  DFM2G_TRY(ensure_context());
+  *p = nullptr;
+  if (bytes == 0) return DFM2G_OK;
+  DFM2G_CUDA(cudaMalloc(p, bytes));
+  return DFM2G_OK;
+}
+
+int dfm2g_dev_free(void *p) {
+  if (p) {
+    cudaStreamSynchronize(stream());
+    DFM2G_CUDA(cudaFree(p));
+  }
+  return DFM2G_OK;
+}
+
+int dfm2g_dev_copy(void *dst, const void *src, size_t bytes, int kind) {
+  if ((!dst || !src) && bytes) return fail(DFM2G_ERR_ARG, "dev_copy: null pointer");
+  DFM2G_TRY(ensure_context());
+  cudaMemcpyKind k;
+  switch (kind) {
+    case DFM2G_COPY_H2D: k = cudaMemcpyHostToDevice; break;
+    case DFM2G_COPY_D2H: k = cudaMemcpyDeviceToHost; break;
+    case DFM2G_COPY_D2D: k = cudaMemcpyDeviceToDevice; break;
+    default: return fail(DFM2G_ERR_ARG, "dev_copy: unknown kind %d", kind);
+  }
+  if (bytes) DFM2G_CUDA(cudaMemcpyAsync(dst, src, bytes, k, stream()));
+  if (kind != DFM2G_COPY_D2D) DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+int dfm2g_vec_dot(const double *x, const double *y, size_t n, double *out, int mem) {
+  if (!x || !y || !out) return fail(DFM2G_ERR_ARG, "vec_dot: null argument");
+  DFM2G_TRY(vec_ws());
+  VecArg<double> ax, ay;
+  DFM2G_TRY(ax.in(x, n, mem, true));
+  DFM2G_TRY(ay.in(y, n, mem, true));
+  return dot_host(n, ax.dev(), ay.dev(), DFM2G_F64, out);
+}
+
+int dfm2g_vec_axpy(double *y, double alpha, const double *x, size_t n, int mem) {
+  if (!x || !y) return fail(DFM2G_ERR_ARG, "vec_axpy: null argument");
+  DFM2G_TRY(ensure_context());
+  VecArg<double> ax, ay;
+  DFM2G_TRY(ax.in(x, n, mem, true));
+  DFM2G_TRY(ay.in(y, n, mem, true));
+  if (n) k_vec_axpy<<<blocks_for(n, 256, ctx().num_sms * 8), 256, 0, stream()>>>(n, ay.dev(), alpha, ax.dev());
+  note_launches(1);
+  DFM2G_LAUNCH_CHECK();
+  return ay.copy_back();
+}
+
+int dfm2g_vec_scale_add(double *y, double beta, const double *x, size_t n, int mem) {
+  if (!x || !y) return fail(DFM2G_ERR_ARG, "vec_scale_add: null argument");
+  DFM2G_TRY(ensure_context());
+  VecArg<double> ax, ay;
+  DFM2G_TRY(ax.in(x, n, mem, true));
+  DFM2G_TRY(ay.in(y, n, mem, true));
+  if (n) k_vec_scale_add<<<blocks_for(n, 256, ctx().num_sms * 8), 256, 0, stream()>>>(n, ay.dev(), beta, ax.dev());
+  note_launches(1);
+  DFM2G_LAUNCH_CHECK();
+  return ay.copy_back();
+}
+
+int dfm2g_vec_set_zero(double *x, size_t n, int mem) {
+  if (!x) return fail(DFM2G_ERR_ARG, "vec_set_zero: null argument");
+  if (mem == DFM2G_MEM_HOST) {
+    std::memset(x, 0, sizeof(double) * n);
+    return DFM2G_OK;
+  }
+  if (mem != DFM2G_MEM_DEVICE) return fail(DFM2G_ERR_ARG, "mem flag must be 0 (host) or 1 (device)");
+  DFM2G_TRY(ensure_context());
+  if (n) DFM2G_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, stream()));
+  return DFM2G_OK;
+}
+
+}  // extern "C"

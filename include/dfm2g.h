@@ -55,9 +55,10 @@ enum dfm2g_sweep {
   DFM2G_SWEEP_GROUPS = 2,   /* FP32: rows in compact blobs, one CTA per blob
                                (shared-memory dependencies inside a blob);
                                FP64 sweeps use the sync-free schedule        */
-  DFM2G_SWEEP_BLOCK = 3,    /* one CTA walks the levels, one barrier per level,
-                               recent results in a shared-memory ring (for
-                               patterns with few rows per level)             */
+  DFM2G_SWEEP_BLOCK = 3,    /* one CTA walks the levels over a TMA-streamed,
+                               level-ordered copy of the factors, one barrier
+                               per level, recent results in a shared-memory
+                               ring (for patterns with few rows per level)   */
   DFM2G_SWEEP_PARTS = 4     /* sync-free over contiguous row ranges, one CTA
                                per range: dependencies inside a range are
                                polled in shared memory, only cross-range ones
@@ -289,6 +290,20 @@ DFM2G_API int dfm2g_cloth_rollout(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, doubl
  * and applies dfm2g_cloth_adjoint_terms. Needs ckpt_every > 0. */
 DFM2G_API int dfm2g_cloth_rollout_adjoint(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xbar,
                                           double *vbar, double *dLdE, dfm2g_solve_stats *stats, int mem);
+
+/* ---- device vectors (the compatibility path of dfm2g.hpp) ---------------- */
+/* For callers without CUDA of their own: device memory and copies. */
+enum dfm2g_copy_kind { DFM2G_COPY_H2D = 0, DFM2G_COPY_D2H = 1, DFM2G_COPY_D2D = 2 };
+DFM2G_API int dfm2g_dev_alloc(void **p, size_t bytes);
+DFM2G_API int dfm2g_dev_free(void *p);
+DFM2G_API int dfm2g_dev_copy(void *dst, const void *src, size_t bytes, int kind);
+/* The vector primitives Solve_PCG calls through ADL (view_vectorx.h:61-109),
+ * FP64: Dot (deterministic reduction, result to the host), AddScaledVec
+ * (y += alpha x), ScaleAndAddVec (y = beta y + x), setZero. */
+DFM2G_API int dfm2g_vec_dot(const double *x, const double *y, size_t n, double *out, int mem);
+DFM2G_API int dfm2g_vec_axpy(double *y, double alpha, const double *x, size_t n, int mem);
+DFM2G_API int dfm2g_vec_scale_add(double *y, double beta, const double *x, size_t n, int mem);
+DFM2G_API int dfm2g_vec_set_zero(double *x, size_t n, int mem);
 
 /* ---- instrumentation ------------------------------------------------------- */
 /* Kernel classes timed when profiling is on (CUDA events around every launch

@@ -8,6 +8,9 @@
 //   Solve_PCG                  include/delfem2/lsitrsol.h:80-148
 // Storage is on the GPU; vectors passed by the caller are host memory (as in
 // the reference) unless a member says otherwise. Only 3x3 blocks.
+// Two ways to solve: Solve_PCG below runs the whole iteration on the device
+// (fast path); DeviceVectorView lets the reference's own Solve_PCG template
+// drive device vectors through the ADL primitives (compatibility path).
 #pragma once
 
 #include <climits>
@@ -150,6 +153,62 @@ inline std::vector<double> Solve_PCG(VectorView r_vec, VectorView x_vec, VectorV
   hist.resize(n < hist.size() ? n : hist.size());
   return hist;
 }
+
+// Compatibility path: a non-owning view of a device vector with the members
+// and ADL primitives the reference's generic Solve_PCG<MAT, VEC, PREC>
+// (lsitrsol.h:80-148) calls (view_vectorx.h:26-109), so that template runs
+// unchanged on GPU-resident vectors; each Dot returns to the host. Copy
+// construction copies the view, assignment copies the contents (as the
+// reference's `Pr_vec = r_vec`).
+struct DeviceVectorView {
+  double *p;
+  size_t n;
+  DeviceVectorView(double *p_, size_t n_) : p(p_), n(n_) {}
+  DeviceVectorView(const DeviceVectorView &) = default;
+  DeviceVectorView &operator=(const DeviceVectorView &o) {
+    if (o.n != n) throw Error(DFM2G_ERR_ARG, "DeviceVectorView: size mismatch");
+    if (o.p != p) check(dfm2g_dev_copy(p, o.p, sizeof(double) * n, DFM2G_COPY_D2D), "operator=");
+    return *this;
+  }
+  void setZero() { check(dfm2g_vec_set_zero(p, n, DFM2G_MEM_DEVICE), "setZero"); }
+};
+
+inline double Dot(const DeviceVectorView &x, const DeviceVectorView &y) {
+  double d = 0.0;
+  check(dfm2g_vec_dot(x.p, y.p, x.n, &d, DFM2G_MEM_DEVICE), "Dot");
+  return d;
+}
+inline void AddScaledVec(DeviceVectorView &y, double alpha, const DeviceVectorView &x) {
+  check(dfm2g_vec_axpy(y.p, alpha, x.p, y.n, DFM2G_MEM_DEVICE), "AddScaledVec");
+}
+inline void ScaleAndAddVec(DeviceVectorView &y, double beta, const DeviceVectorView &x) {
+  check(dfm2g_vec_scale_add(y.p, beta, x.p, y.n, DFM2G_MEM_DEVICE), "ScaleAndAddVec");
+}
+// lhs = scale_lhs * lhs + scale_rhs * mat * rhs
+inline void AddMatVec(DeviceVectorView &lhs, double scale_lhs, double scale_rhs, const CMatrixSparse<double> &mat,
+                      const DeviceVectorView &rhs) {
+  check(dfm2g_bsr_matvec(mat.handle(), DFM2G_F64, lhs.p, scale_rhs, rhs.p, scale_lhs, DFM2G_MEM_DEVICE),
+        "AddMatVec");
+}
+inline void SolvePrecond(DeviceVectorView &v, const CPreconditionerILU<double> &ilu) {
+  check(dfm2g_ilu_solve_precond(ilu.handle(), DFM2G_F64, v.p, DFM2G_MEM_DEVICE), "SolvePrecond");
+}
+
+// Owning device buffer for callers without CUDA of their own.
+class DeviceVector {
+ public:
+  explicit DeviceVector(size_t n) : n_(n) { check(dfm2g_dev_alloc((void **)&p_, sizeof(double) * n), "alloc"); }
+  DeviceVector(const DeviceVector &) = delete;
+  DeviceVector &operator=(const DeviceVector &) = delete;
+  ~DeviceVector() { dfm2g_dev_free(p_); }
+  DeviceVectorView view() { return DeviceVectorView(p_, n_); }
+  void upload(const double *h) { check(dfm2g_dev_copy(p_, h, sizeof(double) * n_, DFM2G_COPY_H2D), "upload"); }
+  void download(double *h) const { check(dfm2g_dev_copy(h, p_, sizeof(double) * n_, DFM2G_COPY_D2H), "download"); }
+
+ private:
+  double *p_ = nullptr;
+  size_t n_;
+};
 
 // The FP32-inner / FP64-refinement variant (no reference counterpart).
 inline dfm2g_solve_stats Solve_PCG_Mixed(const double *b, double *x, double tol, const CMatrixSparse<double> &mat,

@@ -43,6 +43,34 @@ static void emat_tet(const double P[4][3], double myu, double lam, double emat[4
   *vol_out = vol;
 }
 
+// A generic PCG written against the ADL primitives only (the call shapes of
+// the reference's Solve_PCG<MAT, VEC, PREC>): exercises the compatibility path
+// of dfm2g.hpp with device vectors. Returns the iteration count.
+template <class MAT, class VEC, class PREC>
+static unsigned generic_pcg(VEC &r, VEC &x, VEC &Pr, VEC &p, double tol, unsigned max_it, const MAT &K,
+                            const PREC &M) {
+  x.setZero();
+  const double rr0 = Dot(r, r);
+  Pr = r;
+  SolvePrecond(Pr, M);
+  p = Pr;
+  double rz = Dot(r, Pr);
+  for (unsigned it = 0; it < max_it; ++it) {
+    VEC &Ap = Pr;
+    AddMatVec(Ap, 0.0, 1.0, K, p);
+    const double alpha = rz / Dot(p, Ap);
+    AddScaledVec(r, -alpha, Ap);
+    AddScaledVec(x, alpha, p);
+    if (std::sqrt(Dot(r, r) / rr0) < tol) return it + 1;
+    Pr = r;
+    SolvePrecond(Pr, M);
+    const double rz1 = Dot(r, Pr);
+    ScaleAndAddVec(p, rz1 / rz, Pr);
+    rz = rz1;
+  }
+  return max_it;
+}
+
 int main(int argc, char **argv) {
   const unsigned n = argc > 1 ? (unsigned)atoi(argv[1]) : 8;
   const size_t np = (size_t)(n + 1) * (n + 1) * (n + 1), ntet = (size_t)n * n * n * 6;
@@ -101,6 +129,17 @@ int main(int argc, char **argv) {
     bb += b[i] * b[i];
     xs += x[i];
   }
-  std::printf("iterations %zu residual %.3e xsum %.17g\n", hist.size() - 1, std::sqrt(rr / bb), xs);
+  // the same solve through the compatibility path (device vectors + ADL primitives)
+  const size_t nd = b.size();
+  g::DeviceVector dr(nd), dx(nd), dPr(nd), dp(nd);
+  dr.upload(b.data());
+  g::DeviceVectorView vr = dr.view(), vx = dx.view(), vPr = dPr.view(), vp = dp.view();
+  const unsigned its2 = generic_pcg(vr, vx, vPr, vp, 1e-10, 1000, K, ilu);
+  std::vector<double> x2(nd);
+  dx.download(x2.data());
+  double xs2 = 0;
+  for (size_t i = 0; i < nd; ++i) xs2 += x2[i];
+  std::printf("iterations %zu residual %.3e xsum %.17g compat_iterations %u compat_xsum %.17g\n", hist.size() - 1,
+              std::sqrt(rr / bb), xs, its2, xs2);
   return 0;
 }

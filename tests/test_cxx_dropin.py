@@ -33,6 +33,11 @@ def test_dropin_caller_matches_oracle(exe, gpu, port):
     assert out.returncode == 0, out.stderr
     f = out.stdout.split()
     its, res, xsum = int(f[1]), float(f[3]), float(f[5])
+    its2, xsum2 = int(f[7]), float(f[9])
+    # the compatibility path (device vectors through the ADL primitives) takes
+    # the same iterations as the whole-loop device solve
+    assert abs(its2 - its) <= 1
+    assert abs(xsum2 - xsum) <= 1e-8 * abs(xsum)
     # the same problem through the oracle
     xyz, tet = port.voxel_tet_mesh(8, 8, 8, 1 / 8)
     np_ = xyz.size // 3
@@ -50,3 +55,19 @@ def test_dropin_caller_matches_oracle(exe, gpu, port):
     assert abs(its - (len(h) - 1)) <= 1
     assert res < 1e-9
     assert abs(xsum - x.sum()) <= 1e-8 * np.abs(x).sum()
+
+
+COMPAT = os.path.join(ROOT, "tests", "cxx", "compat_reference_pcg.cpp")
+REF_INCLUDE = "/root/reference/include"
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_INCLUDE, "delfem2")),
+                    reason="reference source tree not available")
+def test_reference_solve_pcg_template_accepts_device_views():
+    """The reference's own generic Solve_PCG (lsitrsol.h:80-148) instantiates
+    with delfem2::gb300::DeviceVectorView, CMatrixSparse<double> and
+    CPreconditionerILU<double>: the compatibility path is a type-level drop-in
+    (compile check, no GPU)."""
+    cmd = ["g++", "-std=c++17", "-fsyntax-only", "-I" + REF_INCLUDE, "-I" + os.path.join(ROOT, "include"), COMPAT]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
