@@ -556,12 +556,12 @@ double orc_dot(const double *a, const double *b, size_t n) {
 /* final entry when max_iter is exhausted. r is overwritten with the final   */
 /* residual. Returns the history length (entries past hist_cap are counted  */
 /* but not stored).                                                          */
-uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
-                       const double *vcrs, const double *vdia,
-                       const uint32_t *ilu_col, const uint32_t *dia_ind,
-                       const double *ilu_vcrs, const double *ilu_vdia,
-                       double *r, double *x, double tol, uint32_t max_iter,
-                       double *hist, uint32_t hist_cap) {
+uint32_t orc_solve_pcg_k(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                         const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                         const uint32_t *ilu_col, const uint32_t *dia_ind,
+                         const double *ilu_vcrs, const double *ilu_vdia,
+                         double *r, double *x, double tol, uint32_t max_iter,
+                         double *hist, uint32_t hist_cap) {
   const size_t n = (size_t)nblk * 3;
   uint32_t nh = 0;
 #define ORC_PUSH(v)                          \
@@ -577,8 +577,8 @@ uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t 
   double *Pr = (double *)malloc(n * sizeof(double));
   double *p = (double *)malloc(n * sizeof(double));
   memcpy(Pr, r, n * sizeof(double));
-  orc_ilu_forward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
-  orc_ilu_backward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
+  orc_ilu_forward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
+  orc_ilu_backward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
   memcpy(p, Pr, n * sizeof(double));
   double rPr = orc_dot(r, Pr, n);
   int converged = 0;
@@ -593,8 +593,8 @@ uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t 
     ORC_PUSH(sqrt(sq));
     if (sqrt(sq * inv_sq0) < tol) { converged = 1; break; }
     memcpy(Pr, r, n * sizeof(double));
-    orc_ilu_forward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
-    orc_ilu_backward(nblk, row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
+    orc_ilu_forward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
+    orc_ilu_backward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
     const double rPr1 = orc_dot(r, Pr, n);
     const double beta = rPr1 / rPr;
     rPr = rPr1;
@@ -605,6 +605,17 @@ uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t 
   free(Pr);
   free(p);
   return nh;
+}
+
+/* Solve_PCG with the ILU(0) factors (the ILU shares the matrix's row offsets). */
+uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                       const double *vcrs, const double *vdia,
+                       const uint32_t *ilu_col, const uint32_t *dia_ind,
+                       const double *ilu_vcrs, const double *ilu_vdia,
+                       double *r, double *x, double tol, uint32_t max_iter,
+                       double *hist, uint32_t hist_cap) {
+  return orc_solve_pcg_k(nblk, row_start, col, vcrs, vdia, row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, r, x,
+                         tol, max_iter, hist, hist_cap);
 }
 
 /* Solve_CG, include/delfem2/lsitrsol.h:35-74: history holds the relative   */
@@ -1127,4 +1138,123 @@ void orc_cloth_adjoint_terms(const double *xyz0, const double *xyz, const uint32
         xbar[(size_t)n[a] * 3 + i] -= h;
       }
   }
+}
+
+/* ---- ILU(k) --------------------------------------------------------------- */
+
+/* Initialize_ILUk(m, lev_fill), include/delfem2/ls_ilu_block_sparse.cpp:849-999: */
+/* level-of-fill symbolic factorisation, row by row. Row i starts as the      */
+/* sorted matrix row (level 0); for each k < i in it (ascending) with         */
+/* lev(i,k) + 1 <= lev_fill, each j in row k's upper part with               */
+/* lev(k,j) + 1 <= lev_fill and j != i that row i lacks is inserted with      */
+/* level max(lev(i,k), lev(k,j)) + 1 (existing entries keep their level).     */
+/* lev_fill == -1 takes every fill. Writes row_start_out (nblk+1) and, when   */
+/* cap is large enough, col_out and dia_ind; returns the pattern's size.      */
+size_t orc_ilu_pattern_k(uint32_t nblk, const uint32_t *row_start, const uint32_t *col_in, int lev_fill,
+                         uint32_t *row_start_out, uint32_t *col_out, size_t cap, uint32_t *dia_ind) {
+  /* rows kept as arrays of (col, lev), sorted by col */
+  size_t tot = 0, acap = (size_t)row_start[nblk] * 2 + 16;
+  uint32_t *acol = (uint32_t *)malloc(acap * sizeof(uint32_t));
+  uint32_t *alev = (uint32_t *)malloc(acap * sizeof(uint32_t));
+  uint32_t *rs = (uint32_t *)malloc(((size_t)nblk + 1) * sizeof(uint32_t));
+  uint32_t *dia = (uint32_t *)malloc(((size_t)nblk + 1) * sizeof(uint32_t));
+  size_t wcap = 64;
+  uint32_t *wc = (uint32_t *)malloc(wcap * sizeof(uint32_t)), *wl = (uint32_t *)malloc(wcap * sizeof(uint32_t));
+  rs[0] = 0;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    /* working row: sorted copy of the matrix row, level 0 */
+    size_t n = row_start[i + 1] - row_start[i];
+    if (n + 1 > wcap) {
+      wcap = 2 * (n + 1);
+      wc = (uint32_t *)realloc(wc, wcap * sizeof(uint32_t));
+      wl = (uint32_t *)realloc(wl, wcap * sizeof(uint32_t));
+    }
+    for (size_t t = 0; t < n; ++t) {
+      const uint32_t v = col_in[row_start[i] + t];
+      size_t b = t;
+      while (b > 0 && wc[b - 1] > v) {
+        wc[b] = wc[b - 1];
+        --b;
+      }
+      wc[b] = v;
+      wl[t] = 0;
+    }
+    /* walk k ascending over the (growing) row while k < i */
+    for (size_t kk = 0; kk < n; ++kk) {
+      const uint32_t k = wc[kk], lik = wl[kk];
+      if (lev_fill != -1 && (int)lik + 1 > lev_fill) continue;
+      if (k >= i) break;
+      size_t pos = kk; /* fills of this k are inserted after kk, in column order */
+      for (uint32_t s = dia[k]; s < rs[k + 1]; ++s) {
+        const uint32_t lkj = alev[s];
+        if (lev_fill != -1 && (int)lkj + 1 > lev_fill) continue;
+        const uint32_t j = acol[s];
+        if (j == i) continue;
+        while (pos + 1 < n && wc[pos + 1] < j) ++pos;
+        if (pos + 1 < n && wc[pos + 1] == j) continue; /* present: level unchanged */
+        if (n + 1 > wcap) {
+          wcap *= 2;
+          wc = (uint32_t *)realloc(wc, wcap * sizeof(uint32_t));
+          wl = (uint32_t *)realloc(wl, wcap * sizeof(uint32_t));
+        }
+        memmove(wc + pos + 2, wc + pos + 1, (n - pos - 1) * sizeof(uint32_t));
+        memmove(wl + pos + 2, wl + pos + 1, (n - pos - 1) * sizeof(uint32_t));
+        wc[pos + 1] = j;
+        wl[pos + 1] = (lik > lkj ? lik : lkj) + 1;
+        ++n;
+        ++pos;
+      }
+    }
+    if (tot + n > acap) {
+      while (tot + n > acap) acap *= 2;
+      acol = (uint32_t *)realloc(acol, acap * sizeof(uint32_t));
+      alev = (uint32_t *)realloc(alev, acap * sizeof(uint32_t));
+    }
+    memcpy(acol + tot, wc, n * sizeof(uint32_t));
+    memcpy(alev + tot, wl, n * sizeof(uint32_t));
+    dia[i] = (uint32_t)(tot + n);
+    for (size_t t = 0; t < n; ++t)
+      if (wc[t] > i) {
+        dia[i] = (uint32_t)(tot + t);
+        break;
+      }
+    tot += n;
+    rs[i + 1] = (uint32_t)tot;
+  }
+  memcpy(row_start_out, rs, ((size_t)nblk + 1) * sizeof(uint32_t));
+  if (col_out && cap >= tot) {
+    memcpy(col_out, acol, tot * sizeof(uint32_t));
+    memcpy(dia_ind, dia, (size_t)nblk * sizeof(uint32_t));
+  }
+  free(acol);
+  free(alev);
+  free(rs);
+  free(dia);
+  free(wc);
+  free(wl);
+  return tot;
+}
+
+/* CopyValue (ls_ilu_block_sparse.cpp:1009-1047) for an ILU pattern with its */
+/* own row offsets (fill-in): zero, scatter each matrix block into the slot  */
+/* with the same column, copy the diagonal. lev_fill names the pattern's     */
+/* fill level (the pattern itself is given).                                 */
+void orc_ilu_copy_value_k(uint32_t nblk, const uint32_t *mrow_start, const uint32_t *col_mat,
+                          const double *mat_vcrs, const double *mat_vdia, int lev_fill,
+                          const uint32_t *irow_start, const uint32_t *col_ilu, double *ilu_vcrs,
+                          double *ilu_vdia) {
+  (void)lev_fill;
+  memset(ilu_vcrs, 0, (size_t)irow_start[nblk] * 9 * sizeof(double));
+  int64_t *slot_of = (int64_t *)malloc((size_t)nblk * sizeof(int64_t));
+  for (uint32_t i = 0; i < nblk; ++i) slot_of[i] = -1;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    for (uint32_t s = irow_start[i]; s < irow_start[i + 1]; ++s) slot_of[col_ilu[s]] = s;
+    for (uint32_t s = mrow_start[i]; s < mrow_start[i + 1]; ++s) {
+      const int64_t t = slot_of[col_mat[s]];
+      if (t >= 0) memcpy(ilu_vcrs + (size_t)t * 9, mat_vcrs + (size_t)s * 9, 9 * sizeof(double));
+    }
+    for (uint32_t s = irow_start[i]; s < irow_start[i + 1]; ++s) slot_of[col_ilu[s]] = -1;
+  }
+  free(slot_of);
+  memcpy(ilu_vdia, mat_vdia, (size_t)nblk * 9 * sizeof(double));
 }

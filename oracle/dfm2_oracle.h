@@ -85,6 +85,12 @@ uint32_t orc_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t 
 uint32_t orc_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
                       const double *vcrs, const double *vdia, double *r, double *x,
                       double tol, uint32_t max_iter, double *hist, uint32_t hist_cap);
+uint32_t orc_solve_pcg_k(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                         const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                         const uint32_t *ilu_col, const uint32_t *dia_ind,
+                         const double *ilu_vcrs, const double *ilu_vdia,
+                         double *r, double *x, double tol, uint32_t max_iter,
+                         double *hist, uint32_t hist_cap);
 double orc_dot(const double *a, const double *b, size_t n);
 
 /* --- cloth ------------------------------------------------------------- */
@@ -102,6 +108,12 @@ uint32_t orc_cloth_step(uint32_t nblk, const uint32_t *row_start, const uint32_t
                         const double *xyz0, const int *bc, const uint32_t *tri, size_t ntri, const uint32_t *quad,
                         size_t nquad, const double *young_tri, double nu, double stiff_bend, const double g[3],
                         double mass, double dt, double tol, uint32_t max_iter);
+size_t orc_ilu_pattern_k(uint32_t nblk, const uint32_t *row_start, const uint32_t *col_in, int lev_fill,
+                         uint32_t *row_start_out, uint32_t *col_out, size_t cap, uint32_t *dia_ind);
+void orc_ilu_copy_value_k(uint32_t nblk, const uint32_t *mrow_start, const uint32_t *col_mat,
+                          const double *mat_vcrs, const double *mat_vdia, int lev_fill,
+                          const uint32_t *irow_start, const uint32_t *col_ilu, double *ilu_vcrs,
+                          double *ilu_vdia);
 void orc_pd_sim22_jac(const double s2[3], double J[3][3]);
 void orc_cloth_adjoint_terms(const double *xyz0, const double *xyz, const uint32_t *tri, size_t ntri,
                              const uint32_t *quad, size_t nquad, const double *young_tri, double nu,

@@ -155,6 +155,29 @@ class Oracle:
         f(nblk, row_start, _nz(col_ilu), vcrs, vdia, _nz(col_mat), _nz(mat_vcrs), mat_vdia)
         return vcrs[: mat_vcrs.size], vdia
 
+    def ilu_pattern_k(self, row_start, col_in, lev_fill):
+        """Initialize_ILUk's pattern: (row_start, col, dia_ind) of the ILU(k)."""
+        nblk = row_start.size - 1
+        f = self._f("ilu_pattern_k")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, C.c_int, _u32p, C.c_void_p, C.c_size_t, _u32p]
+        f.restype = C.c_size_t
+        rs = np.zeros(nblk + 1, np.uint32)
+        dia = np.zeros(max(nblk, 1), np.uint32)
+        n = f(nblk, row_start, _nz(col_in), int(lev_fill), rs, None, 0, dia)
+        col = np.zeros(max(n, 1), np.uint32)
+        f(nblk, row_start, _nz(col_in), int(lev_fill), rs, col.ctypes.data, col.size, dia)
+        return rs, col[:n], dia[:nblk]
+
+    def ilu_copy_value_k(self, mrow_start, col_mat, mat_vcrs, mat_vdia, lev_fill, irow_start, col_ilu):
+        nblk = mrow_start.size - 1
+        f = self._f("ilu_copy_value_k")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, C.c_int, _u32p, _u32p, _f64p, _f64p]
+        vcrs = np.zeros(max(col_ilu.size * 9, 9), np.float64)
+        vdia = np.zeros(nblk * 9, np.float64)
+        f(nblk, mrow_start, _nz(col_mat), _nz(mat_vcrs), mat_vdia, int(lev_fill), irow_start, _nz(col_ilu), vcrs,
+          vdia)
+        return vcrs[: col_ilu.size * 9], vdia
+
     def ilu_decompose(self, row_start, col, dia, vcrs, vdia):
         """In place; returns (status, n_singular) with status 0 on success."""
         nblk = row_start.size - 1
@@ -205,6 +228,22 @@ class Oracle:
         cap = max_iter + 2
         hist = np.zeros(cap, np.float64)
         nh = f(nblk, row_start, _nz(col), _nz(vcrs), vdia, _nz(ilu_col), dia, _nz(ilu_vcrs),
+               ilu_vdia, r, x, tol, max_iter, hist, cap)
+        return x, r, hist[:nh]
+
+    def solve_pcg_k(self, row_start, col, vcrs, vdia, ilu_row_start, ilu_col, dia, ilu_vcrs, ilu_vdia, r, tol,
+                    max_iter):
+        """Solve_PCG with an ILU whose pattern has its own row offsets (ILU(k))."""
+        nblk = row_start.size - 1
+        f = self._f("solve_pcg_k")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p,
+                      _f64p, C.c_double, C.c_uint32, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        r = np.array(r, np.float64)
+        x = np.zeros_like(r)
+        cap = max_iter + 2
+        hist = np.zeros(cap, np.float64)
+        nh = f(nblk, row_start, _nz(col), _nz(vcrs), vdia, ilu_row_start, _nz(ilu_col), dia, _nz(ilu_vcrs),
                ilu_vdia, r, x, tol, max_iter, hist, cap)
         return x, r, hist[:nh]
 

@@ -192,6 +192,38 @@ void ref_ilu_pattern0(uint32_t nblk, const uint32_t *row_start, const uint32_t *
   std::memcpy(dia_ind, ilu.m_diaInd.data(), sizeof(uint32_t) * nblk);
 }
 
+// Initialize_ILUk(m, lev_fill) itself; same contract as orc_ilu_pattern_k.
+size_t ref_ilu_pattern_k(uint32_t nblk, const uint32_t *row_start, const uint32_t *col_in, int lev_fill,
+                         uint32_t *row_start_out, uint32_t *col_out, size_t cap, uint32_t *dia_ind) {
+  auto m = make_matrix(nblk, row_start, col_in, nullptr, nullptr);
+  dfm2::CPreconditionerILU<double> ilu;
+  ilu.Initialize_ILUk(m, lev_fill);
+  std::memcpy(row_start_out, ilu.colInd.data(), sizeof(uint32_t) * (nblk + 1));
+  const size_t tot = ilu.rowPtr.size();
+  if (col_out && cap >= tot) {
+    std::memcpy(col_out, ilu.rowPtr.data(), sizeof(uint32_t) * tot);
+    std::memcpy(dia_ind, ilu.m_diaInd.data(), sizeof(uint32_t) * nblk);
+  }
+  return tot;
+}
+
+// CopyValue into the pattern Initialize_ILUk(m, lev_fill) builds (which the
+// caller passes as irow_start / col_ilu; nothing is written if they differ).
+void ref_ilu_copy_value_k(uint32_t nblk, const uint32_t *mrow_start, const uint32_t *col_mat,
+                          const double *mat_vcrs, const double *mat_vdia, int lev_fill,
+                          const uint32_t *irow_start, const uint32_t *col_ilu, double *ilu_vcrs,
+                          double *ilu_vdia) {
+  auto m = make_matrix(nblk, mrow_start, col_mat, mat_vcrs, mat_vdia);
+  dfm2::CPreconditionerILU<double> ilu;
+  ilu.Initialize_ILUk(m, lev_fill);
+  if (ilu.rowPtr.size() != irow_start[nblk]) return;
+  for (size_t s = 0; s < ilu.rowPtr.size(); ++s)
+    if (ilu.rowPtr[s] != col_ilu[s]) return;
+  ilu.CopyValue(m);
+  std::memcpy(ilu_vcrs, ilu.valCrs.data(), sizeof(double) * 9 * irow_start[nblk]);
+  std::memcpy(ilu_vdia, ilu.valDia.data(), sizeof(double) * 9 * nblk);
+}
+
 void ref_ilu_copy_value(uint32_t nblk, const uint32_t *row_start, const uint32_t *col_ilu,
                         double *ilu_vcrs, double *ilu_vdia, const uint32_t *col_mat,
                         const double *mat_vcrs, const double *mat_vdia) {
@@ -241,6 +273,23 @@ uint32_t ref_solve_pcg(uint32_t nblk, const uint32_t *row_start, const uint32_t 
   auto m = make_matrix(nblk, row_start, col, vcrs, vdia);
   dfm2::CPreconditionerILU<double> ilu;
   fill_ilu(ilu, nblk, row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia);
+  const size_t n = (size_t)nblk * 3;
+  std::vector<double> Pr(n), p(n);
+  auto h = dfm2::Solve_PCG(dfm2::ViewAsVectorXd(r, n), dfm2::ViewAsVectorXd(x, n),
+                           dfm2::ViewAsVectorXd(Pr), dfm2::ViewAsVectorXd(p), tol, max_iter, m,
+                           ilu);
+  for (size_t k = 0; k < h.size() && k < hist_cap; ++k) hist[k] = h[k];
+  return static_cast<uint32_t>(h.size());
+}
+
+uint32_t ref_solve_pcg_k(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
+                         const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                         const uint32_t *ilu_col, const uint32_t *dia_ind, const double *ilu_vcrs,
+                         const double *ilu_vdia, double *r, double *x, double tol, uint32_t max_iter,
+                         double *hist, uint32_t hist_cap) {
+  auto m = make_matrix(nblk, row_start, col, vcrs, vdia);
+  dfm2::CPreconditionerILU<double> ilu;
+  fill_ilu(ilu, nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia);
   const size_t n = (size_t)nblk * 3;
   std::vector<double> Pr(n), p(n);
   auto h = dfm2::Solve_PCG(dfm2::ViewAsVectorXd(r, n), dfm2::ViewAsVectorXd(x, n),

@@ -5,7 +5,7 @@ oracle/Makefile), so it only works where the reference source tree exists.
 The outputs are small .npz files committed next to this script; the tests
 read them on machines without the reference.
 
-  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth]
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk]
 """
 from __future__ import annotations
 
@@ -151,6 +151,28 @@ def make_cloth(R):
     print("cloth: rand-E iterations per step", out["step_rand_nhist"] - 1)
 
 
+def make_iluk(R):
+    """Initialize_ILUk patterns (k = 1, 2, 3 and full fill), the ILU(k) factors
+    and Solve_PCG with them on an 8^3 voxel block (per-tet E log-uniform
+    [0.1, 10], seed 9), from the reference."""
+    s = system(R, 8, 8, 8, 1.0 / 8, young_log_uniform(8 ** 3 * 6, 0.1, 10.0, 9))
+    out = {"young_seed": 9, "n": 8}
+    for k in (1, 2, 3, -1):
+        rs, col, dia = R.ilu_pattern_k(s["ind"], s["psup"], k)
+        ivc, ivd = R.ilu_copy_value_k(s["ind"], s["psup"], s["vc"], s["vd"], k, rs, col)
+        st, _ = R.ilu_decompose(rs, col, dia, ivc, ivd)
+        assert st == 0
+        x, _, hist = R.solve_pcg_k(s["ind"], s["psup"], s["vc"], s["vd"], rs, col, dia, ivc, ivd, s["b"], 1e-10, 1000)
+        tag = "full" if k == -1 else str(k)
+        si = sample_idx(ivc.size, 3000, seed=10 + k)
+        out.update({f"k{tag}_rs": rs, f"k{tag}_col": col, f"k{tag}_dia": dia, f"k{tag}_ivc_idx": si,
+                    f"k{tag}_ivc_sample": ivc[si], f"k{tag}_ivc_abs_sum": np.abs(ivc).sum(),
+                    f"k{tag}_ivd_abs_sum": np.abs(ivd).sum(), f"k{tag}_x": x.astype(np.float64),
+                    f"k{tag}_hist": np.array(hist)})
+        print(f"iluk: k={k} nnz={col.size} iterations={len(hist) - 1}")
+    np.savez_compressed(os.path.join(HERE, "iluk.npz"), **out)
+
+
 def main(which):
     build(quiet=True)
     R = reference()
@@ -169,6 +191,8 @@ def main(which):
         make_cfg(R, "cfg4", 48, 48, 48, 1 / 48, young_log_uniform(48 ** 3 * 6, 0.5, 2.0, 4), 1e-12, False)
     if "cloth" in which:
         make_cloth(R)
+    if "iluk" in which:
+        make_iluk(R)
 
 
 if __name__ == "__main__":
