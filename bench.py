@@ -245,6 +245,49 @@ def cloth_bench(dev, nsteps: int, cpu: bool):
     return out
 
 
+def iluk_bench(dev):
+    """ILU(k) (Initialize_ILUk) on the 64^3 voxel block (823,875 DOF, per-tet E log-uniform [0.1, 10], seed 2):
+    symbolic pattern (host), CopyValue + Decompose, and Solve_PCG to 1e-10 in FP64 and mixed precision."""
+    import torch
+    import delfem2_gb300 as D
+    a = D.voxel_problem_arrays(64, 64, 64, 1.0 / 64, seed=2, e_range=(0.1, 10.0))
+    P = D.StaticElasticProblem(a)
+    b = P.assemble(b=torch.zeros(a["np"] * 3, dtype=torch.float64, device=dev))
+    out = {"workload": f"64x64x64 voxels x 6 tets, {a['np'] * 3} DOF, Solve_PCG to 1e-10 with ILU(k) factors",
+           "matrix_blocks": int(a["psup"].size)}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in (0, 1, 2):
+        ilu = D.CPreconditionerILU()
+        t = time.perf_counter()
+        ilu.Initialize_ILUk(P.K, k)
+        torch.cuda.synchronize()
+        sym_s = time.perf_counter() - t
+        e0.record()
+        ilu.CopyValue(P.K)
+        assert ilu.Decompose()
+        e1.record()
+        torch.cuda.synchronize()
+        fac_ms = e0.elapsed_time(e1)
+        r, x = b.clone(), torch.zeros_like(b)
+        D.Solve_PCG(r.clone(), x, 1e-10, 20000, P.K, ilu)  # warm-up
+        r, x = b.clone(), torch.zeros_like(b)
+        e0.record()
+        hist = D.Solve_PCG(r, x, 1e-10, 20000, P.K, ilu)
+        e1.record()
+        torch.cuda.synchronize()
+        fp64_ms = e0.elapsed_time(e1)
+        xm = torch.zeros_like(b)
+        e0.record()
+        st = D.Solve_PCG_Mixed(b, xm, 1e-10, P.K, ilu, method=METHOD)
+        e1.record()
+        torch.cuda.synchronize()
+        out[f"k{k}"] = {"ilu_blocks": int(ilu.pattern()[0].size), "pattern_s": round(sym_s, 3),
+                        "factor_ms": round(fac_ms, 2), "fp64_iterations": len(hist) - 1,
+                        "fp64_ms": round(fp64_ms, 2), "mixed_iterations": st.iterations,
+                        "mixed_ms": round(e0.elapsed_time(e1), 2), "mixed_rel_residual": st.rel_residual}
+    return out
+
+
 def run_ours(args):
     import torch
     import delfem2_gb300 as D
@@ -427,6 +470,8 @@ def run_ours(args):
     }
     if args.cloth_steps > 0:
         out["cloth"] = cloth_bench(dev, args.cloth_steps, rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if not args.no_iluk:
+        out["ilu_k"] = iluk_bench(dev)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
@@ -502,6 +547,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="32x32x16 voxels instead of 128x128x64")
     ap.add_argument("--cpu-iters", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-iluk", action="store_true", help="skip the ILU(k) line")
     ap.add_argument("--cloth-steps", type=int, default=20,
                     help="steps of the 100-step cloth workload to time (0: skip the cloth line)")
     args = ap.parse_args()

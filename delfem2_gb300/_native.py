@@ -82,6 +82,7 @@ SIGNATURES = {
     "dfm2g_ilu_create": [C.POINTER(_vp)],
     "dfm2g_ilu_destroy": [_vp],
     "dfm2g_ilu_set_pattern0": [_vp, _vp],
+    "dfm2g_ilu_set_pattern_k": [_vp, _vp, _i],
     "dfm2g_ilu_copy_value": [_vp, _vp],
     "dfm2g_ilu_decompose": [_vp, _pi],
     "dfm2g_ilu_forward": [_vp, _i, _vp, _i],
@@ -91,6 +92,8 @@ SIGNATURES = {
     "dfm2g_ilu_set_sweep_mode": [_vp, _i],
     "dfm2g_ilu_get_sweep_mode": [_vp, _pi],
     "dfm2g_ilu_get_pattern": [_vp, _vp, _vp],
+    "dfm2g_ilu_info": [_vp, _pu, _psz],
+    "dfm2g_ilu_get_row_start": [_vp, _vp],
     "dfm2g_ilu_get_values": [_vp, _vp, _vp, _i],
     "dfm2g_ilu_get_levels": [_vp, _i, _vp, _vp, _vp, _pu],
     "dfm2g_solve_pcg": [_vp, _vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],

@@ -634,6 +634,91 @@ static int read_err(dfm2g_ilu_s *p) {
 
 using namespace dfm2g;
 
+// Level-of-fill symbolic ILU(k) on the host (Initialize_ILUk,
+// include/delfem2/ls_ilu_block_sparse.cpp:849-999). Row i starts as its sorted
+// matrix row (level 0); for each k < i of the row in ascending order with
+// lev(i,k) + 1 <= fill_level, every j of row k's upper part with
+// lev(k,j) + 1 <= fill_level and j != i that row i lacks is inserted with level
+// max(lev(i,k), lev(k,j)) + 1. An entry already present keeps its level (as the
+// reference does). fill_level == -1 keeps every fill.
+static int ilu_symbolic_k(unsigned n, const std::vector<unsigned> &mrs, const std::vector<unsigned> &mcol,
+                          int fill_level, std::vector<unsigned> &rs, std::vector<unsigned> &col) {
+  rs.assign((size_t)n + 1, 0u);
+  col.clear();
+  std::vector<unsigned> lev, dia(n);
+  std::vector<std::pair<unsigned, unsigned>> row;  // (column, level), ascending
+  auto too_deep = [fill_level](unsigned l) { return fill_level != -1 && (int)l + 1 > fill_level; };
+  for (unsigned i = 0; i < n; ++i) {
+    row.clear();
+    for (unsigned s = mrs[i]; s < mrs[i + 1]; ++s) row.emplace_back(mcol[s], 0u);
+    std::sort(row.begin(), row.end());
+    for (size_t kk = 0; kk < row.size(); ++kk) {
+      const unsigned k = row[kk].first, lik = row[kk].second;
+      if (too_deep(lik)) continue;
+      if (k >= i) break;
+      size_t pos = kk;
+      for (unsigned s = dia[k]; s < rs[k + 1]; ++s) {
+        const unsigned lkj = lev[s], j = col[s];
+        if (too_deep(lkj) || j == i) continue;
+        while (pos + 1 < row.size() && row[pos + 1].first < j) ++pos;
+        if (pos + 1 < row.size() && row[pos + 1].first == j) continue;
+        row.insert(row.begin() + (std::ptrdiff_t)pos + 1, std::make_pair(j, std::max(lik, lkj) + 1));
+        ++pos;
+      }
+    }
+    if (col.size() + row.size() > 0xFFFFFFF0ull)
+      return fail(DFM2G_ERR_UNSUPPORTED, "set_pattern_k: fill exceeds 32-bit offsets");
+    dia[i] = (unsigned)(col.size() + row.size());
+    for (size_t t = 0; t < row.size(); ++t) {
+      if (row[t].first > i && dia[i] == col.size() + row.size()) dia[i] = (unsigned)(col.size() + t);
+    }
+    for (const auto &e : row) {
+      col.push_back(e.first);
+      lev.push_back(e.second);
+    }
+    rs[i + 1] = (unsigned)col.size();
+  }
+  return DFM2G_OK;
+}
+
+// Installs an ILU pattern (row offsets and columns, rows sorted or not):
+// device copies, row sort + dia_ind, level sets and sweep schedules.
+static int ilu_install_pattern(dfm2g_ilu p, unsigned n, size_t nnz, const unsigned *rs_src, const unsigned *col_src,
+                               cudaMemcpyKind kind) {
+  p->nblk = n;
+  p->nnz = nnz;
+  p->has_pattern = p->has_factor = p->f32_valid = false;
+  DFM2G_TRY(p->row_start.resize(n + 1));
+  DFM2G_TRY(p->col.resize(nnz + 1));
+  DFM2G_TRY(p->dia_ind.resize(n + 1));
+  DFM2G_TRY(p->vcrs.resize(nnz * 9 + 4));
+  DFM2G_TRY(p->vdia.resize((size_t)n * 9 + 4));
+  DFM2G_CUDA(cudaMemcpyAsync(p->row_start.p, rs_src, sizeof(unsigned) * (n + 1), kind, stream()));
+  if (nnz) DFM2G_CUDA(cudaMemcpyAsync(p->col.p, col_src, sizeof(unsigned) * nnz, kind, stream()));
+  if (n) {
+    k_sort_rows_diaind<<<blocks_for(n, 128, ctx().num_sms * 16), 128, 0, stream()>>>(n, p->row_start.p, p->col.p,
+                                                                                    p->dia_ind.p);
+    DFM2G_LAUNCH_CHECK();
+  }
+  DFM2G_TRY(compute_levels(p, false));
+  DFM2G_TRY(compute_levels(p, true));
+  DFM2G_TRY(group_schedules_build(p));
+  DFM2G_TRY(part_schedules_build(p));
+  stream_schedules_reset(p);
+  // The blob schedule is correct but, with one CTA barrier per unit, a single
+  // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
+  // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
+  p->sweep_mode = DFM2G_SWEEP_SYNCFREE;
+  const size_t nvec = (size_t)n * 3 + 1;
+  DFM2G_TRY(p->tmp64a.resize(nvec));
+  DFM2G_TRY(p->tmp64b.resize(nvec));
+  DFM2G_TRY(p->tmp32a.resize(nvec));
+  DFM2G_TRY(p->tmp32b.resize(nvec));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  p->has_pattern = true;
+  return DFM2G_OK;
+}
+
 static int check_ilu(dfm2g_ilu p, bool pattern, bool factor) {
   if (!p) return fail(DFM2G_ERR_ARG, "null ILU handle");
   if (pattern && !p->has_pattern) return fail(DFM2G_ERR_STATE, "ILU has no pattern (call set_pattern0)");
@@ -665,41 +750,16 @@ int dfm2g_ilu_destroy(dfm2g_ilu p) {
 int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "set_pattern0: matrix has no pattern");
-  const unsigned n = m->nblk;
-  p->nblk = n;
-  p->nnz = m->nnz;
-  DFM2G_TRY(p->row_start.resize(n + 1));
-  DFM2G_TRY(p->col.resize(m->nnz + 1));
-  DFM2G_TRY(p->dia_ind.resize(n + 1));
-  DFM2G_TRY(p->vcrs.resize(m->nnz * 9 + 1));
-  DFM2G_TRY(p->vdia.resize((size_t)n * 9 + 1));
-  DFM2G_CUDA(cudaMemcpyAsync(p->row_start.p, m->row_start.p, sizeof(unsigned) * (n + 1), cudaMemcpyDeviceToDevice,
-                             stream()));
-  if (m->nnz)
-    DFM2G_CUDA(cudaMemcpyAsync(p->col.p, m->col.p, sizeof(unsigned) * m->nnz, cudaMemcpyDeviceToDevice, stream()));
-  if (n) {
-    k_sort_rows_diaind<<<blocks_for(n, 128, ctx().num_sms * 16), 128, 0, stream()>>>(n, p->row_start.p, p->col.p,
-                                                                                    p->dia_ind.p);
-    DFM2G_LAUNCH_CHECK();
-  }
-  DFM2G_TRY(compute_levels(p, false));
-  DFM2G_TRY(compute_levels(p, true));
-  DFM2G_TRY(group_schedules_build(p));
-  DFM2G_TRY(part_schedules_build(p));
-  stream_schedules_reset(p);
-  // The blob schedule is correct but, with one CTA barrier per unit, a single
-  // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
-  // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
-  p->sweep_mode = DFM2G_SWEEP_SYNCFREE;
-  const size_t nvec = (size_t)n * 3 + 1;
-  DFM2G_TRY(p->tmp64a.resize(nvec));
-  DFM2G_TRY(p->tmp64b.resize(nvec));
-  DFM2G_TRY(p->tmp32a.resize(nvec));
-  DFM2G_TRY(p->tmp32b.resize(nvec));
-  p->has_pattern = true;
-  p->has_factor = false;
-  p->f32_valid = false;
-  return DFM2G_OK;
+  return ilu_install_pattern(p, m->nblk, m->nnz, m->row_start.p, m->col.p, cudaMemcpyDeviceToDevice);
+}
+
+int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level) {
+  DFM2G_TRY(check_ilu(p, false, false));
+  if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "set_pattern_k: matrix has no pattern");
+  if (fill_level == 0) return dfm2g_ilu_set_pattern0(p, m);
+  std::vector<unsigned> rs, col;
+  DFM2G_TRY(ilu_symbolic_k(m->nblk, m->h_row_start, m->h_col, fill_level, rs, col));
+  return ilu_install_pattern(p, m->nblk, col.size(), rs.data(), col.data(), cudaMemcpyHostToDevice);
 }
 
 int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m) {
@@ -847,6 +907,22 @@ int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!mode) return fail(DFM2G_ERR_ARG, "get_sweep_mode: null out");
   *mode = p->sweep_mode;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_info(dfm2g_ilu p, unsigned *nblk, size_t *nnz) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  if (nblk) *nblk = p->nblk;
+  if (nnz) *nnz = p->nnz;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_get_row_start(dfm2g_ilu p, unsigned *row_start) {
+  DFM2G_TRY(check_ilu(p, true, false));
+  if (!row_start) return fail(DFM2G_ERR_ARG, "get_row_start: null out");
+  DFM2G_CUDA(cudaMemcpyAsync(row_start, p->row_start.p, sizeof(unsigned) * (p->nblk + 1), cudaMemcpyDeviceToHost,
+                             stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
 }
 

@@ -189,7 +189,7 @@ def setRHS_Zero(b, bc, iflag_nonzero: int = 0):
 
 # ---------------------------------------------------------------------------
 class CPreconditionerILU:
-    """Device-resident CPreconditionerILU<double> (ILU(0), 3x3 blocks)."""
+    """Device-resident CPreconditionerILU<double> (ILU(0) or ILU(k), 3x3 blocks)."""
 
     def __init__(self):
         h = C.c_void_p()
@@ -203,9 +203,13 @@ class CPreconditionerILU:
         self._nnz = mat.nnz
 
     def Initialize_ILUk(self, mat: CMatrixSparse, fill_level: int):
-        if fill_level != 0:
-            raise NotImplementedError("only ILU(0) (fill_level == 0) is supported")
-        self.SetPattern0(mat)
+        """Level-of-fill ILU(k) pattern (ls_ilu_block_sparse.cpp:849-999); 0 is
+        SetPattern0, -1 keeps every fill."""
+        N.call("dfm2g_ilu_set_pattern_k", self._h, mat._h, int(fill_level))
+        self.nblk = mat.nrowblk
+        nnz = C.c_size_t(0)
+        N.call("dfm2g_ilu_info", self._h, None, C.byref(nnz))
+        self._nnz = nnz.value
 
     def CopyValue(self, mat: CMatrixSparse):
         N.call("dfm2g_ilu_copy_value", self._h, mat._h)
@@ -238,6 +242,12 @@ class CPreconditionerILU:
         m = C.c_int(0)
         N.call("dfm2g_ilu_get_sweep_mode", self._h, C.byref(m))
         return m.value
+
+    def row_start(self):
+        """Row offsets of the ILU pattern (the matrix's for ILU(0))."""
+        rs = np.zeros(self.nblk + 1, np.uint32)
+        N.call("dfm2g_ilu_get_row_start", self._h, rs.ctypes.data)
+        return rs
 
     def pattern(self):
         col = np.zeros(max(self._nnz, 1), np.uint32)

@@ -146,6 +146,11 @@ DFM2G_API int dfm2g_ilu_destroy(dfm2g_ilu p);
  * 854-857: pattern copied and row-sorted on the device, dia_ind found, and the
  * forward/backward level sets computed on the device. */
 DFM2G_API int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m);
+/* Initialize_ILUk(m, fill_level), ls_ilu_block_sparse.cpp:849-999: the
+ * level-of-fill pattern of ILU(k) (fill_level 0: SetPattern0; -1: every fill),
+ * computed on the host from the matrix pattern; the numeric phases
+ * (CopyValue, Decompose, sweeps) then run on that pattern. */
+DFM2G_API int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level);
 /* CopyValue, ls_ilu_block_sparse.cpp:1009-1047. */
 DFM2G_API int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m);
 /* Decompose (3x3 branch), ls_ilu_block_sparse.cpp:152-160,286-356, level-
@@ -176,6 +181,10 @@ DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
  * room for nblk+1). */
+/* Size of the ILU pattern (nnz differs from the matrix's after fill-in) and its
+ * row offsets (nblk+1, host). */
+DFM2G_API int dfm2g_ilu_info(dfm2g_ilu p, unsigned *nblk, size_t *nnz);
+DFM2G_API int dfm2g_ilu_get_row_start(dfm2g_ilu p, unsigned *row_start);
 DFM2G_API int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_ind);
 DFM2G_API int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem);
 DFM2G_API int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, unsigned *order,

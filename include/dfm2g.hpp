@@ -105,8 +105,7 @@ class CPreconditionerILU<double> {
 
   void SetPattern0(const CMatrixSparse<double> &m) { check(dfm2g_ilu_set_pattern0(h_, m.handle()), "SetPattern0"); }
   void Initialize_ILUk(const CMatrixSparse<double> &m, int fill_level) {
-    if (fill_level != 0) throw Error(DFM2G_ERR_UNSUPPORTED, "Initialize_ILUk: only fill level 0");
-    SetPattern0(m);
+    check(dfm2g_ilu_set_pattern_k(h_, m.handle(), fill_level), "Initialize_ILUk");
   }
   void CopyValue(const CMatrixSparse<double> &m) { check(dfm2g_ilu_copy_value(h_, m.handle()), "CopyValue"); }
   bool Decompose() {
