@@ -296,7 +296,8 @@ struct dfm2g_ilu_s {
   dfm2g::DevBuf<float> tmp32a, tmp32b;
   dfm2g::DevBuf<int> err;
   dfm2g::DevBuf<int> nsing;
-  int coop_blocks64 = 0, coop_blocks32 = 0, coop_blocks64b = 0, coop_blocks32b = 0;
+  int coop_cache[2][2][2] = {};         // resident blocks of the sync-free kernel [f64][fwd][wide]
+  unsigned max_lower = 0, max_upper = 0; // longest triangle rows (blocks)
 };
 
 struct dfm2g_tetmesh_s {

@@ -409,17 +409,19 @@ __global__ void k_sweep_meta(unsigned n, const unsigned *__restrict__ order, con
   }
 }
 
-template <typename T>
+// R rounds (3R blocks of one triangle) in registers: 4 for ILU(0) patterns,
+// 8 for fill-in patterns whose longest triangle row has 13..24 blocks.
+template <typename T, unsigned R = 4>
 struct SweepRow {
-  static constexpr unsigned kRounds = 4;  // 12 blocks of one triangle in registers
+  static constexpr unsigned kRounds = R;
   RowFrag<T, kRounds> f;
   unsigned i, s0, s1;
   T in[3];  // lanes 0..2: the row's right-hand side
   T d[3];   // lanes 0..2: row `lane` of D_i^-1 (forward only)
 };
 
-template <typename T, bool FWD>
-__device__ __forceinline__ void sweep_load(SweepRow<T> &R, const RowLane &L, unsigned lane, uint4 m,
+template <typename T, bool FWD, unsigned NR>
+__device__ __forceinline__ void sweep_load(SweepRow<T, NR> &R, const RowLane &L, unsigned lane, uint4 m,
                                            const unsigned *__restrict__ col, const T *__restrict__ vcrs,
                                            const T *__restrict__ vdia, const T *in) {
   R.i = m.x;
@@ -436,12 +438,12 @@ __device__ __forceinline__ void sweep_load(SweepRow<T> &R, const RowLane &L, uns
   }
 }
 
-template <typename T, bool FWD, bool WAIT>
-__device__ __forceinline__ void sweep_finish(const SweepRow<T> &R, const RowLane &L, unsigned lane,
+template <typename T, bool FWD, bool WAIT, unsigned NR>
+__device__ __forceinline__ void sweep_finish(const SweepRow<T, NR> &R, const RowLane &L, unsigned lane,
                                              const unsigned *__restrict__ col, const T *__restrict__ vcrs, T *out,
                                              int *err, unsigned long long timeout_ns) {
   T acc;
-  if (R.f.nb <= 3 * SweepRow<T>::kRounds)
+  if (R.f.nb <= 3 * NR)
     acc = WAIT ? row_dot_wait(R.f, L, out, err, timeout_ns) : row_dot(R.f, L, out);
   else
     acc = WAIT ? row_dot_wait_long(L, R.s0, R.s1, col, vcrs, out, err, timeout_ns)
@@ -484,7 +486,7 @@ __global__ void __launch_bounds__(256) k_sweep_level(const uint4 *__restrict__ m
 // the earliest unfinished position can always proceed. Pipelined: the next
 // position's row is loaded before the current one's wait, and the metadata
 // of the one after that before the current row is finished.
-template <typename T, bool FWD>
+template <typename T, bool FWD, unsigned NR>
 __global__ void __launch_bounds__(256) k_sweep_syncfree(unsigned n, const uint4 *__restrict__ meta,
                                                         const unsigned *__restrict__ col,
                                                         const T *__restrict__ vcrs, const T *__restrict__ vdia,
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(256) k_sweep_syncfree(unsigned n, const uint4 
   const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
   unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= n) return;
-  SweepRow<T> cur, nxt;
+  SweepRow<T, NR> cur, nxt;
   sweep_load<T, FWD>(cur, L, lane, meta[q], col, vcrs, vdia, in);
   uint4 m1 = (q + nwarp < n) ? meta[q + nwarp] : make_uint4(0u, 0u, 0u, 0u);
   for (;;) {
@@ -574,9 +576,11 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     if (p->sweep_mode == DFM2G_SWEEP_GROUPS && gs.ok && gs.values_ok)
       return group_sweep(p, forward, (const float *)in, (float *)out, skip);
   }
-  void *kernel = forward ? (void *)k_sweep_syncfree<T, true> : (void *)k_sweep_syncfree<T, false>;
-  int *cache = sizeof(T) == 8 ? (forward ? &p->coop_blocks64 : &p->coop_blocks64b)
-                              : (forward ? &p->coop_blocks32 : &p->coop_blocks32b);
+  const unsigned longest = forward ? p->max_lower : p->max_upper;
+  const bool wide = longest > 12 && longest <= 24;
+  void *kernel = wide ? (forward ? (void *)k_sweep_syncfree<T, true, 8> : (void *)k_sweep_syncfree<T, false, 8>)
+                      : (forward ? (void *)k_sweep_syncfree<T, true, 4> : (void *)k_sweep_syncfree<T, false, 4>);
+  int *cache = &p->coop_cache[sizeof(T) == 8 ? 1 : 0][forward ? 1 : 0][wide ? 1 : 0];
   DFM2G_TRY(coop_blocks<T>(kernel, cache));
   const unsigned want = blocks_for((size_t)n * 32, 256);
   const unsigned blocks = std::min<unsigned>(want, (unsigned)*cache);
@@ -700,6 +704,23 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, size_t nnz, const unsign
                                                                                     p->dia_ind.p);
     DFM2G_LAUNCH_CHECK();
   }
+  {  // longest lower / upper triangle row (picks the sweep's register fragment)
+    std::vector<unsigned> hrs(n + 1), hdia(n);
+    if (n) {
+      DFM2G_CUDA(cudaMemcpyAsync(hrs.data(), p->row_start.p, sizeof(unsigned) * (n + 1), cudaMemcpyDeviceToHost,
+                                 stream()));
+      DFM2G_CUDA(cudaMemcpyAsync(hdia.data(), p->dia_ind.p, sizeof(unsigned) * n, cudaMemcpyDeviceToHost, stream()));
+      DFM2G_CUDA(cudaStreamSynchronize(stream()));
+    }
+    p->max_lower = p->max_upper = 0;
+    for (unsigned i = 0; i < n; ++i) {
+      p->max_lower = std::max(p->max_lower, hdia[i] - hrs[i]);
+      p->max_upper = std::max(p->max_upper, hrs[i + 1] - hdia[i]);
+    }
+  }
+  for (auto &a : p->coop_cache)
+    for (auto &b : a)
+      for (int &c : b) c = 0;
   DFM2G_TRY(compute_levels(p, false));
   DFM2G_TRY(compute_levels(p, true));
   DFM2G_TRY(group_schedules_build(p));
