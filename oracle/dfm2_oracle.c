@@ -1258,3 +1258,64 @@ void orc_ilu_copy_value_k(uint32_t nblk, const uint32_t *mrow_start, const uint3
   free(slot_of);
   memcpy(ilu_vdia, mat_vdia, (size_t)nblk * 9 * sizeof(double));
 }
+
+/* ---- Solve_PBiCGStab ------------------------------------------------------- */
+
+/* Solve_PBiCGStab, include/delfem2/vecxitrsol.h:350-437, with the ILU(0)    */
+/* preconditioner: x = 0; |r0|^2 < 1e-60 returns [|r0|]; r0* = r, p = r; for */
+/* iitr = 1 .. max_niter-1: Mp = M^-1 p, alpha = (r,r0*)/(A Mp, r0*),        */
+/* s = r - alpha A Mp, Ms = M^-1 s, omega = (s, A Ms)/(A Ms, A Ms),          */
+/* x += alpha Mp + omega Ms, r = s - omega A Ms, push |r|/|r0| (stop below   */
+/* tol), beta = (r,r0*) alpha / ((r,r0*)_old omega), p = beta p + r -        */
+/* beta omega A Mp. The history holds RELATIVE residuals, one per iteration. */
+uint32_t orc_solve_pbicgstab(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, const double *vcrs,
+                             const double *vdia, const uint32_t *ilu_row_start, const uint32_t *ilu_col,
+                             const uint32_t *dia_ind, const double *ilu_vcrs, const double *ilu_vdia, double *r,
+                             double *x, double tol, uint32_t max_iter, double *hist, uint32_t hist_cap) {
+  const size_t n = (size_t)nblk * 3;
+  uint32_t nh = 0;
+  for (size_t k = 0; k < n; ++k) x[k] = 0.0;
+  const double sq0 = orc_dot(r, r, n);
+  if (sq0 < 1.0e-60) {
+    if (hist_cap) hist[0] = sqrt(sq0);
+    return 1;
+  }
+  const double inv0 = 1.0 / sq0;
+  double *r0 = (double *)malloc(n * sizeof(double)), *p = (double *)malloc(n * sizeof(double));
+  double *s = (double *)malloc(n * sizeof(double)), *Mp = (double *)malloc(n * sizeof(double));
+  double *AMp = (double *)malloc(n * sizeof(double)), *Ms = (double *)malloc(n * sizeof(double));
+  double *AMs = (double *)malloc(n * sizeof(double));
+  memcpy(r0, r, n * sizeof(double));
+  memcpy(p, r, n * sizeof(double));
+  for (uint32_t it = 1; it < max_iter; ++it) {
+    memcpy(Mp, p, n * sizeof(double));
+    orc_ilu_forward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Mp);
+    orc_ilu_backward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Mp);
+    const double r_r2 = orc_dot(r, r0, n);
+    orc_bsr_matvec(nblk, row_start, col, vcrs, vdia, AMp, 1.0, Mp, 0.0);
+    const double alpha = r_r2 / orc_dot(AMp, r0, n);
+    for (size_t k = 0; k < n; ++k) s[k] = r[k] - alpha * AMp[k];
+    memcpy(Ms, s, n * sizeof(double));
+    orc_ilu_forward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Ms);
+    orc_ilu_backward(nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Ms);
+    orc_bsr_matvec(nblk, row_start, col, vcrs, vdia, AMs, 1.0, Ms, 0.0);
+    const double omega = orc_dot(s, AMs, n) / orc_dot(AMs, AMs, n);
+    for (size_t k = 0; k < n; ++k) x[k] += alpha * Mp[k];
+    for (size_t k = 0; k < n; ++k) x[k] += omega * Ms[k];
+    for (size_t k = 0; k < n; ++k) r[k] = s[k] - omega * AMs[k];
+    const double ratio = sqrt(orc_dot(r, r, n) * inv0);
+    if (nh < hist_cap) hist[nh] = ratio;
+    ++nh;
+    if (ratio < tol) break;
+    const double beta = orc_dot(r, r0, n) * alpha / (r_r2 * omega);
+    for (size_t k = 0; k < n; ++k) p[k] = beta * p[k] + r[k] - beta * omega * AMp[k];
+  }
+  free(r0);
+  free(p);
+  free(s);
+  free(Mp);
+  free(AMp);
+  free(Ms);
+  free(AMs);
+  return nh;
+}

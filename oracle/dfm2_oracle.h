@@ -91,6 +91,10 @@ uint32_t orc_solve_pcg_k(uint32_t nblk, const uint32_t *row_start, const uint32_
                          const double *ilu_vcrs, const double *ilu_vdia,
                          double *r, double *x, double tol, uint32_t max_iter,
                          double *hist, uint32_t hist_cap);
+uint32_t orc_solve_pbicgstab(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, const double *vcrs,
+                             const double *vdia, const uint32_t *ilu_row_start, const uint32_t *ilu_col,
+                             const uint32_t *dia_ind, const double *ilu_vcrs, const double *ilu_vdia, double *r,
+                             double *x, double tol, uint32_t max_iter, double *hist, uint32_t hist_cap);
 double orc_dot(const double *a, const double *b, size_t n);
 
 /* --- cloth ------------------------------------------------------------- */

@@ -247,6 +247,22 @@ class Oracle:
                ilu_vdia, r, x, tol, max_iter, hist, cap)
         return x, r, hist[:nh]
 
+    def solve_pbicgstab(self, row_start, col, vcrs, vdia, ilu_row_start, ilu_col, dia, ilu_vcrs, ilu_vdia, r,
+                        tol, max_iter):
+        """Returns (x, r_final, hist) for Solve_PBiCGStab on a copy of r (relative history)."""
+        nblk = row_start.size - 1
+        f = self._f("solve_pbicgstab")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p,
+                      _f64p, C.c_double, C.c_uint32, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        r = np.array(r, np.float64)
+        x = np.zeros_like(r)
+        cap = max_iter + 2
+        hist = np.zeros(cap, np.float64)
+        nh = f(nblk, row_start, _nz(col), _nz(vcrs), vdia, ilu_row_start, _nz(ilu_col), dia, _nz(ilu_vcrs),
+               ilu_vdia, r, x, tol, max_iter, hist, cap)
+        return x, r, hist[:nh]
+
     def solve_cg(self, row_start, col, vcrs, vdia, r, tol, max_iter):
         nblk = row_start.size - 1
         f = self._f("solve_cg")

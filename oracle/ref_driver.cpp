@@ -299,6 +299,19 @@ uint32_t ref_solve_pcg_k(uint32_t nblk, const uint32_t *row_start, const uint32_
   return static_cast<uint32_t>(h.size());
 }
 
+// Solve_PBiCGStab (vecxitrsol.h:350-437) itself, with CPreconditionerILU.
+uint32_t ref_solve_pbicgstab(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, const double *vcrs,
+                             const double *vdia, const uint32_t *ilu_row_start, const uint32_t *ilu_col,
+                             const uint32_t *dia_ind, const double *ilu_vcrs, const double *ilu_vdia, double *r,
+                             double *x, double tol, uint32_t max_iter, double *hist, uint32_t hist_cap) {
+  auto m = make_matrix(nblk, row_start, col, vcrs, vdia);
+  dfm2::CPreconditionerILU<double> ilu;
+  fill_ilu(ilu, nblk, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia);
+  auto h = dfm2::Solve_PBiCGStab(r, x, tol, max_iter, m, ilu);
+  for (size_t k = 0; k < h.size() && k < hist_cap; ++k) hist[k] = h[k];
+  return static_cast<uint32_t>(h.size());
+}
+
 uint32_t ref_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
                       const double *vcrs, const double *vdia, double *r, double *x, double tol,
                       uint32_t max_iter, double *hist, uint32_t hist_cap) {

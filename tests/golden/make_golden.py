@@ -5,7 +5,7 @@ oracle/Makefile), so it only works where the reference source tree exists.
 The outputs are small .npz files committed next to this script; the tests
 read them on machines without the reference.
 
-  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk]
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab]
 """
 from __future__ import annotations
 
@@ -173,6 +173,39 @@ def make_iluk(R):
     np.savez_compressed(os.path.join(HERE, "iluk.npz"), **out)
 
 
+def nonsymmetric(s, seed=11):
+    """K with each off-diagonal block scaled by a seeded factor in [0.7, 1.3]
+    (so block (i,j) is no longer block (j,i)^T), clamped again."""
+    rng = np.random.default_rng(seed)
+    vc = s["vc"] * (1.0 + 0.3 * rng.uniform(-1.0, 1.0, s["vc"].size // 9).repeat(9))
+    return vc, s["vd"].copy()
+
+
+def make_bicgstab(R):
+    """The reference's Solve_PBiCGStab with ILU(0) and ILU(1) on a non-symmetric
+    version of the 8^3 block (E seed 5), tol 1e-10 and 1e-6. The system is
+    assembled and factorised by the C restatement (pinned to the reference by
+    the other fixtures): BiCGStab amplifies 1e-16 differences in K or the
+    factors into different iteration counts, so the solver is pinned on
+    identical inputs."""
+    from oracle import port
+    P = port()
+    s = system(P, 8, 8, 8, 1.0 / 8, young_log_uniform(8 ** 3 * 6, 0.1, 10.0, 5))
+    vc, vd = nonsymmetric(s)
+    P.set_fixed_bc(s["ind"], s["psup"], vc, vd, s["bc"])
+    out = {}
+    for k in (0, 1):
+        rs, col, dia = P.ilu_pattern_k(s["ind"], s["psup"], k)
+        ivc, ivd = P.ilu_copy_value_k(s["ind"], s["psup"], vc, vd, k, rs, col)
+        assert P.ilu_decompose(rs, col, dia, ivc, ivd)[0] == 0
+        for tol in (1e-10, 1e-6):
+            x, r, hist = R.solve_pbicgstab(s["ind"], s["psup"], vc, vd, rs, col, dia, ivc, ivd, s["b"], tol, 1000)
+            tag = f"k{k}_t{int(-np.log10(tol))}"
+            out.update({f"{tag}_x": x, f"{tag}_r": r, f"{tag}_hist": np.array(hist)})
+            print(f"bicgstab: ILU({k}) tol {tol}: {len(hist)} iterations, last {hist[-1]:.3e}")
+    np.savez_compressed(os.path.join(HERE, "bicgstab.npz"), **out)
+
+
 def main(which):
     build(quiet=True)
     R = reference()
@@ -193,6 +226,8 @@ def main(which):
         make_cloth(R)
     if "iluk" in which:
         make_iluk(R)
+    if "bicgstab" in which:
+        make_bicgstab(R)
 
 
 if __name__ == "__main__":
