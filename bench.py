@@ -288,6 +288,45 @@ def iluk_bench(dev):
     return out
 
 
+def bicgstab_bench(dev, cpu: bool):
+    """Solve_PBiCGStab with ILU(0) on the 64^3 voxel block's elastic system to 1e-10, FP64 (the reference calls
+    BiCGStab on this kind of 3x3-block elastic system, 603_Fem3DStiffwarp/main.cpp:218); the C restatement timed
+    per iteration on the host."""
+    import torch
+    import delfem2_gb300 as D
+    a = D.voxel_problem_arrays(64, 64, 64, 1.0 / 64, seed=2, e_range=(0.1, 10.0))
+    P = D.StaticElasticProblem(a)
+    b = P.assemble()
+    assert P.factor()
+    bd = torch.tensor(b, device=dev)
+    r, x = bd.clone(), torch.zeros_like(bd)
+    D.Solve_PBiCGStab(r, x, 1e-10, 5000, P.K, P.ilu)  # warm-up
+    r, x = bd.clone(), torch.zeros_like(bd)
+    st = D.SolveStats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    hist = D.Solve_PBiCGStab(r, x, 1e-10, 5000, P.K, P.ilu, st)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"workload": f"64x64x64 voxel block, {a['np'] * 3} DOF, ILU(0)-BiCGStab to 1e-10 (FP64)",
+           "ms": round(ms, 2), "iterations": len(hist), "rel_residual": st.rel_residual}
+    if cpu:
+        from oracle import port
+        O = port()
+        vc, vd = P.K.get_values()
+        col, dia = P.ilu.pattern()
+        ivc, ivd = P.ilu.values()
+        its = 3
+        t = time.perf_counter()
+        O.solve_pbicgstab(a["psup_ind"], a["psup"], vc, vd, a["psup_ind"], col, dia, ivc, ivd, b, 1e-300, its + 1)
+        per = (time.perf_counter() - t) * 1e3 / its
+        out["cpu_baseline"] = {"value": round(per * len(hist), 1), "unit": "ms", "cores": 1, "kind": "port",
+                               "sample": f"{its} BiCGStab iterations of the C restatement ({per:.1f} ms each) "
+                                         f"scaled to the GPU's {len(hist)} iterations"}
+    return out
+
+
 def run_ours(args):
     import torch
     import delfem2_gb300 as D
@@ -472,6 +511,7 @@ def run_ours(args):
         out["cloth"] = cloth_bench(dev, args.cloth_steps, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if not args.no_iluk:
         out["ilu_k"] = iluk_bench(dev)
+        out["bicgstab"] = bicgstab_bench(dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:

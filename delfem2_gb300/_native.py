@@ -98,6 +98,7 @@ SIGNATURES = {
     "dfm2g_ilu_get_levels": [_vp, _i, _vp, _vp, _vp, _pu],
     "dfm2g_solve_pcg": [_vp, _vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
     "dfm2g_solve_cg": [_vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
+    "dfm2g_solve_pbicgstab": [_vp, _vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
     "dfm2g_solve_pcg_mixed": [_vp, _vp, _vp, _vp, _d, _d, _u, _u, _i, _pstats],
     "dfm2g_solve_pcg_mixed_reliable": [_vp, _vp, _vp, _vp, _d, _d, _u, _i, _pstats],
     "dfm2g_tetmesh_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz],

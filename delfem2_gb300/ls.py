@@ -309,6 +309,21 @@ def Solve_CG(r_vec, u_vec, conv_ratio_tol: float, max_iteration: int, mat: CMatr
     return list(hist[: min(nh.value, cap)])
 
 
+def Solve_PBiCGStab(r_vec, x_vec, conv_ratio_tol: float, max_niter: int, mat: CMatrixSparse,
+                    ilu: CPreconditionerILU, stats: N.SolveStats | None = None):
+    """Solve_PBiCGStab (vecxitrsol.h:350-437): x = 0, r overwritten with the final
+    residual; returns the RELATIVE residual history (one entry per iteration)."""
+    pr, mr, kr = _vec(r_vec, np.float64, True)
+    px, mx, kx = _vec(x_vec, np.float64, True)
+    cap = int(max_niter) + 2
+    hist = np.zeros(cap, np.float64)
+    nh = C.c_uint(0)
+    N.call("dfm2g_solve_pbicgstab", mat._h, ilu._h, pr, px, float(conv_ratio_tol), int(max_niter),
+           hist.ctypes.data, cap, C.byref(nh), _same_mem(mr, mx), C.byref(stats) if stats is not None else None,
+           allow=(N.ERR_NOT_CONVERGED,))
+    return list(hist[: min(nh.value, cap)])
+
+
 RELIABLE_REFRESH = 0.1  # |r| drop between FP64 residual refreshes of the reliable-update solver
 
 

@@ -223,6 +223,16 @@ DFM2G_API int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const dou
                                              double tol, double delta, unsigned max_iter, int mem,
                                              dfm2g_solve_stats *stats);
 
+/* Solve_PBiCGStab, include/delfem2/vecxitrsol.h:350-437, FP64, for
+ * non-symmetric K: x = 0, r overwritten with the final residual; hist receives
+ * the RELATIVE residual after each iteration (iterations 1 .. max_iter-1, the
+ * reference's loop); |r0|^2 < 1e-60 returns [|r0|]. Not converging returns
+ * DFM2G_ERR_NOT_CONVERGED with x valid; a NaN/Inf residual stops with
+ * DFM2G_ERR_NONFINITE. */
+DFM2G_API int dfm2g_solve_pbicgstab(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol,
+                                    unsigned max_iter, double *hist, unsigned hist_cap,
+                                    unsigned *n_hist, int mem, dfm2g_solve_stats *stats);
+
 /* ---- linear-tet elasticity ------------------------------------------------- */
 /* Builds, for mesh (xyz: 3*np, tet: 4*ntet, host arrays) against the pattern
  * of K: the element->slot map (device) and a greedy element colouring (no two

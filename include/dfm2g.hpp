@@ -153,6 +153,20 @@ inline std::vector<double> Solve_PCG(VectorView r_vec, VectorView x_vec, VectorV
   return hist;
 }
 
+// Solve_PBiCGStab(r, x, tol, max_niter, K, ilu), vecxitrsol.h:350-437: same
+// arguments and result (RELATIVE residual per iteration); runs on the GPU.
+inline std::vector<double> Solve_PBiCGStab(double *r_vec, double *x_vec, double conv_ratio_tol,
+                                           unsigned int max_niter, const CMatrixSparse<double> &mat,
+                                           const CPreconditionerILU<double> &ilu) {
+  std::vector<double> hist(max_niter + 2);
+  unsigned n = 0;
+  const int s = dfm2g_solve_pbicgstab(mat.handle(), ilu.handle(), r_vec, x_vec, conv_ratio_tol, max_niter,
+                                      hist.data(), (unsigned)hist.size(), &n, DFM2G_MEM_HOST, nullptr);
+  if (s != DFM2G_ERR_NOT_CONVERGED) check(s, "Solve_PBiCGStab");
+  hist.resize(n < hist.size() ? n : hist.size());
+  return hist;
+}
+
 // Compatibility path: a non-owning view of a device vector with the members
 // and ADL primitives the reference's generic Solve_PCG<MAT, VEC, PREC>
 // (lsitrsol.h:80-148) calls (view_vectorx.h:26-109), so that template runs

@@ -1281,10 +1281,12 @@ uint32_t orc_solve_pbicgstab(uint32_t nblk, const uint32_t *row_start, const uin
     return 1;
   }
   const double inv0 = 1.0 / sq0;
-  double *r0 = (double *)malloc(n * sizeof(double)), *p = (double *)malloc(n * sizeof(double));
-  double *s = (double *)malloc(n * sizeof(double)), *Mp = (double *)malloc(n * sizeof(double));
-  double *AMp = (double *)malloc(n * sizeof(double)), *Ms = (double *)malloc(n * sizeof(double));
-  double *AMs = (double *)malloc(n * sizeof(double));
+  /* zero-initialised like the reference's std::vector buffers: MatVec scales  */
+  /* y by beta = 0 first, which keeps a NaN an uninitialised y might hold     */
+  double *r0 = (double *)calloc(n, sizeof(double)), *p = (double *)calloc(n, sizeof(double));
+  double *s = (double *)calloc(n, sizeof(double)), *Mp = (double *)calloc(n, sizeof(double));
+  double *AMp = (double *)calloc(n, sizeof(double)), *Ms = (double *)calloc(n, sizeof(double));
+  double *AMs = (double *)calloc(n, sizeof(double));
   memcpy(r0, r, n * sizeof(double));
   memcpy(p, r, n * sizeof(double));
   for (uint32_t it = 1; it < max_iter; ++it) {

@@ -1,0 +1,81 @@
+"""Solve_PBiCGStab on the GPU against the reference fixture (non-symmetric 8^3
+system: each off-diagonal block of K scaled by a seeded factor in [0.7, 1.3]).
+
+BiCGStab turns 1e-16 differences (summation order, the GPU's own assembly)
+into different iteration paths, so the bars are on the result: converged
+below tol, true residual within 10 tol, x within 1e-6 relative of the
+reference's x at tol 1e-10, iteration count within 30% of the reference's.
+Semantics (early return, exhaustion length) are exact."""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(gpu_lib):
+    import delfem2_gb300 as D
+    a = D.voxel_problem_arrays(8, 8, 8, 1.0 / 8, seed=5, e_range=(0.1, 10.0))
+    P = D.StaticElasticProblem(a)
+    b = P.assemble()
+    vc, vd = P.K.get_values()
+    rng = np.random.default_rng(11)
+    vc = vc * (1.0 + 0.3 * rng.uniform(-1.0, 1.0, vc.size // 9).repeat(9))
+    P.K.set_values(vc, vd)
+    P.K.SetFixedBC(a["bc"])
+    return a, P, b
+
+
+@pytest.mark.parametrize("k", [0, 1])
+@pytest.mark.parametrize("tol", [1e-10, 1e-6])
+def test_bicgstab_matches_reference(gpu, k, tol):
+    import delfem2_gb300 as D
+    G = golden("bicgstab")
+    a, P, b = _system(gpu)
+    ilu = D.CPreconditionerILU()
+    ilu.Initialize_ILUk(P.K, k)
+    ilu.CopyValue(P.K)
+    assert ilu.Decompose()
+    r, x = b.copy(), np.zeros_like(b)
+    st = D.SolveStats()
+    hist = D.Solve_PBiCGStab(r, x, tol, 1000, P.K, ilu, st)
+    tag = f"k{k}_t{int(-np.log10(tol))}"
+    gh = G[f"{tag}_hist"]
+    assert hist[-1] < tol and all(h >= tol for h in hist[:-1])
+    assert abs(len(hist) - len(gh)) <= 0.3 * len(gh)
+    assert st.rel_residual < 10 * tol
+    if tol == 1e-10:
+        assert rel_err(x, G[f"{tag}_x"]) < 1e-6
+    # r holds the final residual b - A x (recursively updated)
+    assert np.linalg.norm(r) / np.linalg.norm(b) == pytest.approx(hist[-1], rel=1e-6)
+
+
+def test_bicgstab_semantics(gpu):
+    import delfem2_gb300 as D
+    a, P, b = _system(gpu)
+    ilu = D.CPreconditionerILU()
+    ilu.SetPattern0(P.K)
+    ilu.CopyValue(P.K)
+    assert ilu.Decompose()
+    x = np.ones_like(b)
+    hist = D.Solve_PBiCGStab(np.zeros_like(b), x, 1e-10, 100, P.K, ilu)
+    assert hist == [0.0] and not x.any()  # |r0|^2 < 1e-60: x = 0, history [|r0|]
+    hist = D.Solve_PBiCGStab(b.copy(), x, 1e-30, 7, P.K, ilu)
+    assert len(hist) == 6  # iterations 1 .. max_niter-1, no extra entry on exhaustion
+
+
+def test_bicgstab_on_device_tensors(gpu):
+    import torch
+    import delfem2_gb300 as D
+    a, P, b = _system(gpu)
+    ilu = D.CPreconditionerILU()
+    ilu.SetPattern0(P.K)
+    ilu.CopyValue(P.K)
+    assert ilu.Decompose()
+    rh, xh = b.copy(), np.zeros_like(b)
+    hh = D.Solve_PBiCGStab(rh, xh, 1e-10, 1000, P.K, ilu)
+    rd = torch.tensor(b, device="cuda")
+    xd = torch.zeros_like(rd)
+    hd = D.Solve_PBiCGStab(rd, xd, 1e-10, 1000, P.K, ilu)
+    assert hd == hh and np.array_equal(xd.cpu().numpy(), xh)  # deterministic reductions
