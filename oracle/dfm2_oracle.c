@@ -177,9 +177,11 @@ void orc_bsr_matvec_f32(uint32_t nblk, const uint32_t *row_start, const uint32_t
 /* ---------------------------------------------------------------------- */
 /* Merge<nno,nno,3,3,double>, include/delfem2/ls_block_sparse.h:260-310:    */
 /* for each element row, mark the row's columns with their slots in          */
-/* merge_buffer, add the (irow,jcol) 3x3 block to the diagonal (same node)  */
-/* or to the marked slot, then reset the marks. Returns 0, or 1 on a         */
-/* missing slot (the reference returns false there).                         */
+/* merge_buffer, add the (irow,jcol) 3x3 block to the marked slot, or, when  */
+/* both nodes are the same block, the (irow,irow) block to the diagonal (as */
+/* the reference does; it differs only for an element that repeats a node), */
+/* then reset the marks. Returns 0, or 1 on a missing slot (the reference    */
+/* returns false there).                                                     */
 int orc_merge(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
               double *vcrs, double *vdia, uint32_t nnoel, const uint32_t *nodes,
               const double *emat, uint32_t *merge_buffer) {
@@ -189,7 +191,7 @@ int orc_merge(uint32_t nblk, const uint32_t *row_start, const uint32_t *col,
     for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) merge_buffer[col[s]] = s;
     for (uint32_t b = 0; b < nnoel; ++b) {
       const uint32_t j = nodes[b];
-      const double *src = emat + ((size_t)a * nnoel + b) * 9;
+      const double *src = emat + ((size_t)a * nnoel + (i == j ? a : b)) * 9;
       double *dst;
       if (i == j) {
         dst = vdia + (size_t)i * 9;
@@ -1320,4 +1322,498 @@ uint32_t orc_solve_pbicgstab(uint32_t nblk, const uint32_t *row_start, const uin
   free(Ms);
   free(AMs);
   return nh;
+}
+
+/* ====================================================================== */
+/* Scalar (ndim 1) and 2x2 (ndim 2) blocks. Every function below takes     */
+/* ndim in {1, 2, 3}; ndim 3 runs the 3x3 functions above. Values are      */
+/* row-major ndim x ndim blocks, vectors ndim entries per block row.       */
+
+/* y = alpha*A*x + beta*y, include/delfem2/ls_block_sparse.cpp:213-224 (y   */
+/* scaled by beta first) with MatVec_MatSparseCRS_Blk11 (59-78) and          */
+/* MatVec_MatSparseCRS_Blk22 (80-101), in their expression order.            */
+void orc_nd_matvec(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                   const double *vcrs, const double *vdia, double *y, double alpha, const double *x,
+                   double beta) {
+  if (ndim == 3) {
+    orc_bsr_matvec(nblk, row_start, col, vcrs, vdia, y, alpha, x, beta);
+    return;
+  }
+  for (size_t i = 0; i < (size_t)nblk * ndim; ++i) y[i] *= beta;
+  if (ndim == 1) {
+    for (uint32_t i = 0; i < nblk; ++i) {
+      for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) y[i] += alpha * vcrs[s] * x[col[s]];
+      y[i] += alpha * vdia[i] * x[i];
+    }
+    return;
+  }
+  for (uint32_t i = 0; i < nblk; ++i) {
+    double *yi = y + (size_t)i * 2;
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const double *a = vcrs + (size_t)s * 4, *xj = x + (size_t)col[s] * 2;
+      yi[0] += alpha * (a[0] * xj[0] + a[1] * xj[1]);
+      yi[1] += alpha * (a[2] * xj[0] + a[3] * xj[1]);
+    }
+    const double *d = vdia + (size_t)i * 4, *xi = x + (size_t)i * 2;
+    yi[0] += alpha * (d[0] * xi[0] + d[1] * xi[1]);
+    yi[1] += alpha * (d[2] * xi[0] + d[3] * xi[1]);
+  }
+}
+
+/* Mearge / Merge<nrow,ncol,ndimrow,ndimcol> and Merge<nrow,ncol>,           */
+/* include/delfem2/ls_block_sparse.h:209-358, with the same diagonal rule as */
+/* orc_merge: a (irow, jcol) pair on one block adds the (irow, irow) block.  */
+int orc_nd_merge(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                 double *vdia, uint32_t nnoel, const uint32_t *nodes, const double *emat, uint32_t *merge_buffer) {
+  (void)nblk;
+  const size_t bb = (size_t)ndim * ndim;
+  for (uint32_t a = 0; a < nnoel; ++a) {
+    const uint32_t i = nodes[a];
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) merge_buffer[col[s]] = s;
+    for (uint32_t b = 0; b < nnoel; ++b) {
+      const uint32_t j = nodes[b];
+      double *dst;
+      if (i == j) {
+        dst = vdia + (size_t)i * bb;
+      } else {
+        if (merge_buffer[j] == ORC_UNSET) return 1;
+        dst = vcrs + (size_t)merge_buffer[j] * bb;
+      }
+      const double *src = emat + ((size_t)a * nnoel + (i == j ? a : b)) * bb;
+      for (size_t k = 0; k < bb; ++k) dst[k] += src[k];
+    }
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) merge_buffer[col[s]] = ORC_UNSET;
+  }
+  return 0;
+}
+
+/* SetFixedBC (Dia(1), Row, Col), include/delfem2/ls_block_sparse.cpp:397-472 */
+/* for any block size.                                                        */
+void orc_nd_set_fixed_bc(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                         double *vcrs, double *vdia, const int *bc) {
+  const size_t bb = (size_t)ndim * ndim;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    double *d = vdia + (size_t)i * bb;
+    for (uint32_t a = 0; a < ndim; ++a) {
+      if (bc[(size_t)i * ndim + a] == 0) continue;
+      for (uint32_t b = 0; b < ndim; ++b) { d[a * ndim + b] = 0.0; d[b * ndim + a] = 0.0; }
+      d[a * ndim + a] = 1.0;
+    }
+  }
+  for (uint32_t i = 0; i < nblk; ++i)
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s)
+      for (uint32_t a = 0; a < ndim; ++a) {
+        if (bc[(size_t)i * ndim + a] == 0) continue;
+        for (uint32_t b = 0; b < ndim; ++b) vcrs[(size_t)s * bb + a * ndim + b] = 0.0;
+      }
+  for (uint32_t i = 0; i < nblk; ++i)
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) {
+      const uint32_t j = col[s];
+      for (uint32_t b = 0; b < ndim; ++b) {
+        if (bc[(size_t)j * ndim + b] == 0) continue;
+        for (uint32_t a = 0; a < ndim; ++a) vcrs[(size_t)s * bb + a * ndim + b] = 0.0;
+      }
+    }
+}
+
+/* CopyValue, ls_ilu_block_sparse.cpp:1009-1047, any block size, for an ILU  */
+/* pattern with its own row offsets (lev_fill names the pattern's fill       */
+/* level; the pattern itself is given).                                       */
+void orc_nd_ilu_copy_value(uint32_t nblk, uint32_t ndim, const uint32_t *mrow_start, const uint32_t *col_mat,
+                           const double *mat_vcrs, const double *mat_vdia, int lev_fill,
+                           const uint32_t *irow_start, const uint32_t *col_ilu, double *ilu_vcrs,
+                           double *ilu_vdia) {
+  (void)lev_fill;
+  const size_t bb = (size_t)ndim * ndim;
+  memset(ilu_vcrs, 0, (size_t)irow_start[nblk] * bb * sizeof(double));
+  int64_t *slot_of = (int64_t *)malloc((size_t)nblk * sizeof(int64_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) slot_of[i] = -1;
+  for (uint32_t i = 0; i < nblk; ++i) {
+    for (uint32_t s = irow_start[i]; s < irow_start[i + 1]; ++s) slot_of[col_ilu[s]] = s;
+    for (uint32_t s = mrow_start[i]; s < mrow_start[i + 1]; ++s) {
+      const int64_t t = slot_of[col_mat[s]];
+      if (t >= 0) memcpy(ilu_vcrs + (size_t)t * bb, mat_vcrs + (size_t)s * bb, bb * sizeof(double));
+    }
+    for (uint32_t s = irow_start[i]; s < irow_start[i + 1]; ++s) slot_of[col_ilu[s]] = -1;
+  }
+  free(slot_of);
+  memcpy(ilu_vdia, mat_vdia, (size_t)nblk * bb * sizeof(double));
+}
+
+/* Decompose, ls_ilu_block_sparse.cpp:168-213 (ndim 1) and 214-285 (ndim 2): */
+/* as orc_ilu_decompose with A_ij -= A_ik A_kj on 1x1 / 2x2 blocks; the      */
+/* pivot is inverted when |d| (ndim 1) or |det| (ndim 2) exceeds 1e-30,      */
+/* else counted and left (more than 10 stop with failure); then             */
+/* U_ij <- D_i^-1 U_ij.                                                      */
+int orc_nd_ilu_decompose(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                         const uint32_t *dia_ind, double *vcrs, double *vdia, int *n_singular) {
+  if (ndim == 3) return orc_ilu_decompose(nblk, row_start, col, dia_ind, vcrs, vdia, n_singular);
+  const size_t bb = (size_t)ndim * ndim;
+  int64_t *slot_of = (int64_t *)malloc((size_t)nblk * sizeof(int64_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) slot_of[i] = -1;
+  int nsing = 0, status = 0;
+  for (uint32_t i = 0; i < nblk && status == 0; ++i) {
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) slot_of[col[s]] = s;
+    for (uint32_t sk = row_start[i]; sk < dia_ind[i]; ++sk) {
+      const uint32_t k = col[sk];
+      const double *aik = vcrs + (size_t)sk * bb;
+      for (uint32_t sj = dia_ind[k]; sj < row_start[k + 1]; ++sj) {
+        const uint32_t j = col[sj];
+        double *aij;
+        if (j != i) {
+          if (slot_of[j] < 0) continue;
+          aij = vcrs + (size_t)slot_of[j] * bb;
+        } else {
+          aij = vdia + (size_t)i * bb;
+        }
+        const double *akj = vcrs + (size_t)sj * bb;
+        if (ndim == 1) {
+          aij[0] -= aik[0] * akj[0];
+        } else {
+          aij[0] -= aik[0] * akj[0] + aik[1] * akj[2];
+          aij[1] -= aik[0] * akj[1] + aik[1] * akj[3];
+          aij[2] -= aik[2] * akj[0] + aik[3] * akj[2];
+          aij[3] -= aik[2] * akj[1] + aik[3] * akj[3];
+        }
+      }
+    }
+    double *dii = vdia + (size_t)i * bb;
+    if (ndim == 1) {
+      if (fabs(dii[0]) > 1.0e-30) {
+        dii[0] = 1.0 / dii[0];
+      } else if (++nsing > 10) {
+        status = 1;
+      }
+    } else {
+      const double det = dii[0] * dii[3] - dii[1] * dii[2];
+      if (fabs(det) > 1.0e-30) {
+        const double inv_det = 1.0 / det, d0 = dii[0];
+        dii[0] = inv_det * dii[3];
+        dii[1] = -inv_det * dii[1];
+        dii[2] = -inv_det * dii[2];
+        dii[3] = inv_det * d0;
+      } else if (++nsing > 10) {
+        status = 1;
+      }
+    }
+    if (status == 0) {
+      for (uint32_t s = dia_ind[i]; s < row_start[i + 1]; ++s) {
+        double *u = vcrs + (size_t)s * bb;
+        if (ndim == 1) {
+          u[0] = u[0] * dii[0];
+        } else {
+          const double t[4] = {u[0], u[1], u[2], u[3]};
+          u[0] = dii[0] * t[0] + dii[1] * t[2];
+          u[1] = dii[0] * t[1] + dii[1] * t[3];
+          u[2] = dii[2] * t[0] + dii[3] * t[2];
+          u[3] = dii[2] * t[1] + dii[3] * t[3];
+        }
+      }
+    }
+    for (uint32_t s = row_start[i]; s < row_start[i + 1]; ++s) slot_of[col[s]] = -1;
+  }
+  free(slot_of);
+  if (n_singular) *n_singular = nsing;
+  return status;
+}
+
+/* ForwardSubstitution, ls_ilu_block_sparse.cpp:502-543 (ndim 1 and 2), in  */
+/* place: v_i <- D_i^-1 (v_i - sum_{j<i} L_ij v_j), ascending rows.          */
+void orc_nd_ilu_forward(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                        const uint32_t *dia_ind, const double *vcrs, const double *vdia, double *vec) {
+  if (ndim == 3) {
+    orc_ilu_forward(nblk, row_start, col, dia_ind, vcrs, vdia, vec);
+    return;
+  }
+  for (uint32_t i = 0; i < nblk; ++i) {
+    if (ndim == 1) {
+      double t = vec[i];
+      for (uint32_t s = row_start[i]; s < dia_ind[i]; ++s) t -= vcrs[s] * vec[col[s]];
+      vec[i] = vdia[i] * t;
+    } else {
+      double t0 = vec[(size_t)i * 2], t1 = vec[(size_t)i * 2 + 1];
+      for (uint32_t s = row_start[i]; s < dia_ind[i]; ++s) {
+        const double *a = vcrs + (size_t)s * 4;
+        const double v0 = vec[(size_t)col[s] * 2], v1 = vec[(size_t)col[s] * 2 + 1];
+        t0 -= a[0] * v0 + a[1] * v1;
+        t1 -= a[2] * v0 + a[3] * v1;
+      }
+      const double *d = vdia + (size_t)i * 4;
+      vec[(size_t)i * 2] = d[0] * t0 + d[1] * t1;
+      vec[(size_t)i * 2 + 1] = d[2] * t0 + d[3] * t1;
+    }
+  }
+}
+
+/* BackwardSubstitution, ls_ilu_block_sparse.cpp:680-720 (ndim 1 and 2), in */
+/* place: v_i <- v_i - sum_{j>i} U'_ij v_j, descending rows.                 */
+void orc_nd_ilu_backward(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                         const uint32_t *dia_ind, const double *vcrs, double *vec) {
+  if (ndim == 3) {
+    orc_ilu_backward(nblk, row_start, col, dia_ind, vcrs, vec);
+    return;
+  }
+  for (uint32_t ii = nblk; ii-- > 0;) {
+    if (ndim == 1) {
+      double t = vec[ii];
+      for (uint32_t s = dia_ind[ii]; s < row_start[ii + 1]; ++s) t -= vcrs[s] * vec[col[s]];
+      vec[ii] = t;
+    } else {
+      double t0 = vec[(size_t)ii * 2], t1 = vec[(size_t)ii * 2 + 1];
+      for (uint32_t s = dia_ind[ii]; s < row_start[ii + 1]; ++s) {
+        const double *a = vcrs + (size_t)s * 4;
+        const double v0 = vec[(size_t)col[s] * 2], v1 = vec[(size_t)col[s] * 2 + 1];
+        t0 -= a[0] * v0 + a[1] * v1;
+        t1 -= a[2] * v0 + a[3] * v1;
+      }
+      vec[(size_t)ii * 2] = t0;
+      vec[(size_t)ii * 2 + 1] = t1;
+    }
+  }
+}
+
+/* Solve_PCG (lsitrsol.h:80-148, the semantics of orc_solve_pcg_k) for any  */
+/* block size.                                                               */
+uint32_t orc_nd_solve_pcg(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                          const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                          const uint32_t *ilu_col, const uint32_t *dia_ind, const double *ilu_vcrs,
+                          const double *ilu_vdia, double *r, double *x, double tol, uint32_t max_iter,
+                          double *hist, uint32_t hist_cap) {
+  const size_t n = (size_t)nblk * ndim;
+  uint32_t nh = 0;
+#define ORC_PUSH(v)                    \
+  do {                                 \
+    if (nh < hist_cap) hist[nh] = (v); \
+    ++nh;                              \
+  } while (0)
+  for (size_t k = 0; k < n; ++k) x[k] = 0.0;
+  const double sq0 = orc_dot(r, r, n);
+  ORC_PUSH(sqrt(sq0));
+  if (sq0 < 1.0e-30) return nh;
+  const double inv_sq0 = 1.0 / sq0;
+  double *Pr = (double *)malloc(n * sizeof(double) + 1);
+  double *p = (double *)malloc(n * sizeof(double) + 1);
+  memcpy(Pr, r, n * sizeof(double));
+  orc_nd_ilu_forward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
+  orc_nd_ilu_backward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
+  memcpy(p, Pr, n * sizeof(double));
+  double rPr = orc_dot(r, Pr, n);
+  int converged = 0;
+  for (uint32_t it = 0; it < max_iter; ++it) {
+    double *Ap = Pr;
+    orc_nd_matvec(nblk, ndim, row_start, col, vcrs, vdia, Ap, 1.0, p, 0.0);
+    const double alpha = rPr / orc_dot(p, Ap, n);
+    for (size_t k = 0; k < n; ++k) r[k] += -alpha * Ap[k];
+    for (size_t k = 0; k < n; ++k) x[k] += alpha * p[k];
+    const double sq = orc_dot(r, r, n);
+    ORC_PUSH(sqrt(sq));
+    if (sqrt(sq * inv_sq0) < tol) { converged = 1; break; }
+    memcpy(Pr, r, n * sizeof(double));
+    orc_nd_ilu_forward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Pr);
+    orc_nd_ilu_backward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Pr);
+    const double rPr1 = orc_dot(r, Pr, n);
+    const double beta = rPr1 / rPr;
+    rPr = rPr1;
+    for (size_t k = 0; k < n; ++k) p[k] = beta * p[k] + Pr[k];
+  }
+  if (!converged) ORC_PUSH(sqrt(orc_dot(r, r, n)));
+#undef ORC_PUSH
+  free(Pr);
+  free(p);
+  return nh;
+}
+
+/* Solve_PBiCGStab (vecxitrsol.h:350-437, the semantics of                  */
+/* orc_solve_pbicgstab) for any block size.                                 */
+uint32_t orc_nd_solve_pbicgstab(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                                const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                                const uint32_t *ilu_col, const uint32_t *dia_ind, const double *ilu_vcrs,
+                                const double *ilu_vdia, double *r, double *x, double tol, uint32_t max_iter,
+                                double *hist, uint32_t hist_cap) {
+  const size_t n = (size_t)nblk * ndim;
+  uint32_t nh = 0;
+  for (size_t k = 0; k < n; ++k) x[k] = 0.0;
+  const double sq0 = orc_dot(r, r, n);
+  if (sq0 < 1.0e-60) {
+    if (hist_cap) hist[0] = sqrt(sq0);
+    return 1;
+  }
+  const double inv0 = 1.0 / sq0;
+  double *r0 = (double *)calloc(n + 1, sizeof(double)), *p = (double *)calloc(n + 1, sizeof(double));
+  double *s = (double *)calloc(n + 1, sizeof(double)), *Mp = (double *)calloc(n + 1, sizeof(double));
+  double *AMp = (double *)calloc(n + 1, sizeof(double)), *Ms = (double *)calloc(n + 1, sizeof(double));
+  double *AMs = (double *)calloc(n + 1, sizeof(double));
+  memcpy(r0, r, n * sizeof(double));
+  memcpy(p, r, n * sizeof(double));
+  for (uint32_t it = 1; it < max_iter; ++it) {
+    memcpy(Mp, p, n * sizeof(double));
+    orc_nd_ilu_forward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Mp);
+    orc_nd_ilu_backward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Mp);
+    const double r_r2 = orc_dot(r, r0, n);
+    orc_nd_matvec(nblk, ndim, row_start, col, vcrs, vdia, AMp, 1.0, Mp, 0.0);
+    const double alpha = r_r2 / orc_dot(AMp, r0, n);
+    for (size_t k = 0; k < n; ++k) s[k] = r[k] - alpha * AMp[k];
+    memcpy(Ms, s, n * sizeof(double));
+    orc_nd_ilu_forward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, ilu_vdia, Ms);
+    orc_nd_ilu_backward(nblk, ndim, ilu_row_start, ilu_col, dia_ind, ilu_vcrs, Ms);
+    orc_nd_matvec(nblk, ndim, row_start, col, vcrs, vdia, AMs, 1.0, Ms, 0.0);
+    const double omega = orc_dot(s, AMs, n) / orc_dot(AMs, AMs, n);
+    for (size_t k = 0; k < n; ++k) x[k] += alpha * Mp[k];
+    for (size_t k = 0; k < n; ++k) x[k] += omega * Ms[k];
+    for (size_t k = 0; k < n; ++k) r[k] = s[k] - omega * AMs[k];
+    const double ratio = sqrt(orc_dot(r, r, n) * inv0);
+    if (nh < hist_cap) hist[nh] = ratio;
+    ++nh;
+    if (ratio < tol) break;
+    const double beta = orc_dot(r, r0, n) * alpha / (r_r2 * omega);
+    for (size_t k = 0; k < n; ++k) p[k] = beta * p[k] + r[k] - beta * omega * AMp[k];
+  }
+  free(r0);
+  free(p);
+  free(s);
+  free(Mp);
+  free(AMp);
+  free(Ms);
+  free(AMs);
+  return nh;
+}
+
+/* ---- scalar and 2-D element assembly ----------------------------------- */
+
+/* EMat_Poisson_Tet3D, include/delfem2/fem_poisson.cpp:163-194:              */
+/*   K_e[i][j] = alpha vol (dN_i . dN_j),                                   */
+/*   r_e[i] = source vol / 4 - sum_j K_e[i][j] value_j.                      */
+void orc_emat_poisson_tet(const double P[4][3], double alpha, double source, const double value[4],
+                          double emat[4][4], double eres[4]) {
+  const double vol = orc_tet_volume(P[0], P[1], P[2], P[3]);
+  double dN[4][3];
+  orc_tet_grad(P, vol, dN);
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j)
+      emat[i][j] = alpha * vol * (dN[i][0] * dN[j][0] + dN[i][1] * dN[j][1] + dN[i][2] * dN[j][2]);
+  for (int i = 0; i < 4; ++i) eres[i] = source * vol * 0.25;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) eres[i] -= emat[i][j] * value[j];
+}
+
+/* MergeLinSys_Poission_MeshTet3D, include/delfem2/fem_poisson.h:128-162:   */
+/* per tet b[node] += r_e and Merge<4,4> of K_e (scalar blocks). Returns 0,  */
+/* or 1 when an element block is missing from the pattern.                   */
+int orc_assemble_poisson_tet(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                             double *vdia, double *b, double alpha, double source, const double *xyz,
+                             const uint32_t *tet, size_t ntet, const double *val) {
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  int status = 0;
+  for (size_t e = 0; e < ntet && status == 0; ++e) {
+    const uint32_t *ip = tet + e * 4;
+    double P[4][3], value[4], emat[4][4], eres[4];
+    for (int a = 0; a < 4; ++a) {
+      for (int k = 0; k < 3; ++k) P[a][k] = xyz[(size_t)ip[a] * 3 + k];
+      value[a] = val ? val[ip[a]] : 0.0;
+    }
+    orc_emat_poisson_tet(P, alpha, source, value, emat, eres);
+    for (int a = 0; a < 4; ++a) b[ip[a]] += eres[a];
+    status = orc_nd_merge(nblk, 1, row_start, col, vcrs, vdia, 4, ip, &emat[0][0], buf);
+  }
+  free(buf);
+  return status;
+}
+
+/* TriArea2D (femutil.cpp:16-21) and TriDlDx (femutil.cpp:177-197).         */
+static double orc_tri_area2(const double *p0, const double *p1, const double *p2) {
+  return 0.5 * ((p1[0] - p0[0]) * (p2[1] - p0[1]) - (p2[0] - p0[0]) * (p1[1] - p0[1]));
+}
+
+static void orc_tri_dldx2(const double P[3][2], double area, double dldx[3][2]) {
+  const double t = 0.5 / area;
+  dldx[0][0] = t * (P[1][1] - P[2][1]);
+  dldx[1][0] = t * (P[2][1] - P[0][1]);
+  dldx[2][0] = t * (P[0][1] - P[1][1]);
+  dldx[0][1] = t * (P[2][0] - P[1][0]);
+  dldx[1][1] = t * (P[0][0] - P[2][0]);
+  dldx[2][1] = t * (P[1][0] - P[0][0]);
+}
+
+/* EMat_Poisson_Tri2D, include/delfem2/fem_poisson.cpp:15-46:                */
+/*   K_e[i][j] = alpha area (dN_i . dN_j), r_e[i] = source area / 3 - K_e v. */
+void orc_emat_poisson_tri2(const double P[3][2], double alpha, double source, const double value[3],
+                           double emat[3][3], double eres[3]) {
+  const double area = orc_tri_area2(P[0], P[1], P[2]);
+  double d[3][2];
+  orc_tri_dldx2(P, area, d);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) emat[i][j] = alpha * area * (d[i][0] * d[j][0] + d[i][1] * d[j][1]);
+  for (int i = 0; i < 3; ++i) eres[i] = source * area * 0.33333333333333333;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) eres[i] -= emat[i][j] * value[j];
+}
+
+/* EMat_SolidStaticLinear_Tri2D, include/delfem2/fem_solidlinear.cpp:89-124  */
+/* with SetEmat_LinearSolid2<3> (fem_solidlinear.cpp:35-53):                  */
+/*   K_e[i][j] = area (lambda dN_i dN_j^T + myu dN_j dN_i^T                   */
+/*                     + myu (dN_i . dN_j) I),                                */
+/*   r_e[i] = area rho g / 3 - sum_j K_e[i][j] u_j.                           */
+void orc_emat_solid_tri2(const double P[3][2], double myu, double lambda, double rho, double gx, double gy,
+                         const double disp[3][2], double emat[3][3][2][2], double eres[3][2]) {
+  const double area = orc_tri_area2(P[0], P[1], P[2]);
+  double d[3][2];
+  orc_tri_dldx2(P, area, d);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      emat[i][j][0][0] = area * (lambda + myu) * d[i][0] * d[j][0];
+      emat[i][j][0][1] = area * (lambda * d[i][0] * d[j][1] + myu * d[j][0] * d[i][1]);
+      emat[i][j][1][0] = area * (lambda * d[i][1] * d[j][0] + myu * d[j][1] * d[i][0]);
+      emat[i][j][1][1] = area * (lambda + myu) * d[i][1] * d[j][1];
+      const double t = area * myu * (d[i][1] * d[j][1] + d[i][0] * d[j][0]);
+      emat[i][j][0][0] += t;
+      emat[i][j][1][1] += t;
+    }
+  for (int i = 0; i < 3; ++i) {
+    eres[i][0] = area * rho * gx * 0.33333333333333333;
+    eres[i][1] = area * rho * gy * 0.33333333333333333;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      eres[i][0] -= emat[i][j][0][0] * disp[j][0] + emat[i][j][0][1] * disp[j][1];
+      eres[i][1] -= emat[i][j][1][0] * disp[j][0] + emat[i][j][1][1] * disp[j][1];
+    }
+}
+
+/* MergeLinSys_Poission_MeshTri2D (fem_poisson.h:92-127, ndim 1) and         */
+/* MergeLinSys_SolidLinear_Static_MeshTri2D (fem_solidlinear.h:155-187,      */
+/* ndim 2): per triangle b += r_e and Merge<3,3(,2,2)> of K_e. `val` is the  */
+/* nodal value (ndim 1) or displacement (ndim 2), or NULL for zero. Returns  */
+/* 0, or 1 when an element block is missing from the pattern.                */
+int orc_assemble_tri2(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                      double *vdia, double *b, const double *param, const double *xy, const uint32_t *tri,
+                      size_t ntri, const double *val) {
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  int status = 0;
+  for (size_t e = 0; e < ntri && status == 0; ++e) {
+    const uint32_t *ip = tri + e * 3;
+    double P[3][2];
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < 2; ++k) P[a][k] = xy[(size_t)ip[a] * 2 + k];
+    if (ndim == 1) { /* param: alpha, source */
+      double value[3], emat[3][3], eres[3];
+      for (int a = 0; a < 3; ++a) value[a] = val ? val[ip[a]] : 0.0;
+      orc_emat_poisson_tri2(P, param[0], param[1], value, emat, eres);
+      for (int a = 0; a < 3; ++a) b[ip[a]] += eres[a];
+      status = orc_nd_merge(nblk, 1, row_start, col, vcrs, vdia, 3, ip, &emat[0][0], buf);
+    } else { /* param: myu, lambda, rho, gx, gy */
+      double disp[3][2], emat[3][3][2][2], eres[3][2];
+      for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < 2; ++k) disp[a][k] = val ? val[(size_t)ip[a] * 2 + k] : 0.0;
+      orc_emat_solid_tri2(P, param[0], param[1], param[2], param[3], param[4], disp, emat, eres);
+      for (int a = 0; a < 3; ++a) {
+        b[(size_t)ip[a] * 2] += eres[a][0];
+        b[(size_t)ip[a] * 2 + 1] += eres[a][1];
+      }
+      status = orc_nd_merge(nblk, 2, row_start, col, vcrs, vdia, 3, ip, &emat[0][0][0][0], buf);
+    }
+  }
+  free(buf);
+  return status;
 }

@@ -123,6 +123,47 @@ void orc_cloth_adjoint_terms(const double *xyz0, const double *xyz, const uint32
                              const uint32_t *quad, size_t nquad, const double *young_tri, double nu,
                              double stiff_bend, const double *mu, const double *dx, double *xbar, double *Ebar);
 
+/* --- scalar (ndim 1) and 2x2 (ndim 2) blocks; ndim 3 runs the 3x3 code ---- */
+void orc_nd_matvec(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                   const double *vcrs, const double *vdia, double *y, double alpha, const double *x,
+                   double beta);
+int orc_nd_merge(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                 double *vdia, uint32_t nnoel, const uint32_t *nodes, const double *emat, uint32_t *merge_buffer);
+void orc_nd_set_fixed_bc(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                         double *vcrs, double *vdia, const int *bc);
+void orc_nd_ilu_copy_value(uint32_t nblk, uint32_t ndim, const uint32_t *mrow_start, const uint32_t *col_mat,
+                           const double *mat_vcrs, const double *mat_vdia, int lev_fill,
+                           const uint32_t *irow_start, const uint32_t *col_ilu, double *ilu_vcrs,
+                           double *ilu_vdia);
+int orc_nd_ilu_decompose(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                         const uint32_t *dia_ind, double *vcrs, double *vdia, int *n_singular);
+void orc_nd_ilu_forward(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                        const uint32_t *dia_ind, const double *vcrs, const double *vdia, double *vec);
+void orc_nd_ilu_backward(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                         const uint32_t *dia_ind, const double *vcrs, double *vec);
+uint32_t orc_nd_solve_pcg(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                          const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                          const uint32_t *ilu_col, const uint32_t *dia_ind, const double *ilu_vcrs,
+                          const double *ilu_vdia, double *r, double *x, double tol, uint32_t max_iter,
+                          double *hist, uint32_t hist_cap);
+uint32_t orc_nd_solve_pbicgstab(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col,
+                                const double *vcrs, const double *vdia, const uint32_t *ilu_row_start,
+                                const uint32_t *ilu_col, const uint32_t *dia_ind, const double *ilu_vcrs,
+                                const double *ilu_vdia, double *r, double *x, double tol, uint32_t max_iter,
+                                double *hist, uint32_t hist_cap);
+void orc_emat_poisson_tet(const double P[4][3], double alpha, double source, const double value[4],
+                          double emat[4][4], double eres[4]);
+int orc_assemble_poisson_tet(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                             double *vdia, double *b, double alpha, double source, const double *xyz,
+                             const uint32_t *tet, size_t ntet, const double *val);
+void orc_emat_poisson_tri2(const double P[3][2], double alpha, double source, const double value[3],
+                           double emat[3][3], double eres[3]);
+void orc_emat_solid_tri2(const double P[3][2], double myu, double lambda, double rho, double gx, double gy,
+                         const double disp[3][2], double emat[3][3][2][2], double eres[3][2]);
+int orc_assemble_tri2(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                      double *vdia, double *b, const double *param, const double *xy, const uint32_t *tri,
+                      size_t ntri, const double *val);
+
 #ifdef __cplusplus
 }
 #endif

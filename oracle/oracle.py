@@ -276,6 +276,131 @@ class Oracle:
         return x, r, hist[:nh]
 
 
+    # ---- scalar (ndim 1) and 2x2 (ndim 2) blocks; ndim 3 runs the 3x3 code --------
+    def nd_matvec(self, ndim, row_start, col, vcrs, vdia, y, alpha, x, beta):
+        nblk = row_start.size - 1
+        f = self._f("nd_matvec")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, C.c_double, _f64p, C.c_double]
+        y = np.array(y, np.float64)
+        f(nblk, ndim, row_start, _nz(col), _nz(vcrs), vdia, y, alpha, np.ascontiguousarray(x, np.float64), beta)
+        return y
+
+    def nd_merge(self, ndim, row_start, col, vcrs, vdia, nodes, emat):
+        """Merges one element in place; returns 0, or 1 on a missing slot."""
+        nblk = row_start.size - 1
+        f = self._f("nd_merge")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _f64p, _f64p, C.c_uint32, _u32p, _f64p, _u32p]
+        f.restype = C.c_int
+        buf = np.full(nblk, 0xFFFFFFFF, np.uint32)
+        nodes = np.ascontiguousarray(nodes, np.uint32)
+        return f(nblk, ndim, row_start, _nz(col), _nz(vcrs), vdia, nodes.size, nodes,
+                 np.ascontiguousarray(emat, np.float64).ravel(), buf)
+
+    def nd_set_fixed_bc(self, ndim, row_start, col, vcrs, vdia, bc):
+        nblk = row_start.size - 1
+        f = self._f("nd_set_fixed_bc")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _f64p, _f64p, _i32p]
+        f(nblk, ndim, row_start, _nz(col), _nz(vcrs), vdia, np.ascontiguousarray(bc, np.int32))
+
+    def nd_ilu_copy_value(self, ndim, mrow_start, col_mat, mat_vcrs, mat_vdia, lev_fill, irow_start, col_ilu):
+        """CopyValue into the given ILU pattern; returns (ilu_vcrs, ilu_vdia)."""
+        nblk = mrow_start.size - 1
+        bb = ndim * ndim
+        f = self._f("nd_ilu_copy_value")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _f64p, _f64p, C.c_int, _u32p, _u32p, _f64p, _f64p]
+        vc = np.zeros(max(int(irow_start[-1]) * bb, 1), np.float64)
+        vd = np.zeros(max(nblk * bb, 1), np.float64)
+        f(nblk, ndim, mrow_start, _nz(col_mat), _nz(mat_vcrs), _nz(mat_vdia), int(lev_fill), irow_start,
+          _nz(col_ilu), vc, vd)
+        return vc[: int(irow_start[-1]) * bb], vd[: nblk * bb]
+
+    def nd_ilu_decompose(self, ndim, row_start, col, dia_ind, vcrs, vdia):
+        """Returns (status, vcrs, vdia) of Decompose on copies of the values."""
+        nblk = row_start.size - 1
+        f = self._f("nd_ilu_decompose")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p, C.POINTER(C.c_int)]
+        f.restype = C.c_int
+        vc, vd = np.array(vcrs, np.float64), np.array(vdia, np.float64)
+        ns = C.c_int(0)
+        st = f(nblk, ndim, row_start, _nz(col), _nz(dia_ind), _nz(vc), _nz(vd), C.byref(ns))
+        return st, vc, vd
+
+    def nd_ilu_forward(self, ndim, row_start, col, dia_ind, vcrs, vdia, vec):
+        nblk = row_start.size - 1
+        f = self._f("nd_ilu_forward")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p]
+        v = np.array(vec, np.float64)
+        f(nblk, ndim, row_start, _nz(col), _nz(dia_ind), _nz(vcrs), _nz(vdia), _nz(v))
+        return v
+
+    def nd_ilu_backward(self, ndim, row_start, col, dia_ind, vcrs, vec):
+        nblk = row_start.size - 1
+        f = self._f("nd_ilu_backward")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _u32p, _f64p, _f64p]
+        v = np.array(vec, np.float64)
+        f(nblk, ndim, row_start, _nz(col), _nz(dia_ind), _nz(vcrs), _nz(v))
+        return v
+
+    def _nd_solve(self, name, ndim, row_start, col, vcrs, vdia, ilu_row_start, ilu_col, dia, ilu_vcrs, ilu_vdia, r,
+                  tol, max_iter):
+        nblk = row_start.size - 1
+        f = self._f(name)
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _f64p, _f64p, _u32p, _u32p, _u32p, _f64p, _f64p, _f64p,
+                      _f64p, C.c_double, C.c_uint32, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        r = np.array(r, np.float64)
+        x = np.zeros_like(r)
+        hist = np.zeros(max_iter + 2, np.float64)
+        nh = f(nblk, ndim, row_start, _nz(col), _nz(vcrs), vdia, ilu_row_start, _nz(ilu_col), _nz(dia),
+               _nz(ilu_vcrs), ilu_vdia, r, x, tol, max_iter, hist, hist.size)
+        return x, r, hist[:nh]
+
+    def nd_solve_pcg(self, ndim, *args):
+        """(row_start, col, vcrs, vdia, ilu_row_start, ilu_col, dia, ilu_vcrs, ilu_vdia, r, tol, max_iter)
+        -> (x, r_final, hist): Solve_PCG (absolute history)."""
+        return self._nd_solve("nd_solve_pcg", ndim, *args)
+
+    def nd_solve_pbicgstab(self, ndim, *args):
+        """Same arguments as nd_solve_pcg -> (x, r_final, hist): Solve_PBiCGStab (relative history)."""
+        return self._nd_solve("nd_solve_pbicgstab", ndim, *args)
+
+    def assemble_poisson_tet(self, row_start, col, xyz, tet, alpha, source, val=None):
+        """MergeLinSys_Poission_MeshTet3D into a zeroed scalar matrix: (vcrs, vdia, b)."""
+        nblk = row_start.size - 1
+        f = self._f("assemble_poisson_tet")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, C.c_double, C.c_double, _f64p, _u32p,
+                      C.c_size_t, C.c_void_p]
+        f.restype = C.c_int
+        vc = np.zeros(max(col.size, 1), np.float64)
+        vd = np.zeros(nblk, np.float64)
+        b = np.zeros(nblk, np.float64)
+        tet = np.ascontiguousarray(tet, np.uint32)
+        v = None if val is None else np.ascontiguousarray(val, np.float64)
+        st = f(nblk, row_start, _nz(col), vc, vd, b, alpha, source, np.ascontiguousarray(xyz, np.float64), tet,
+               tet.size // 4, _optr(v))
+        assert st == 0, "element block missing from the pattern"
+        return vc[: col.size], vd, b
+
+    def assemble_tri2(self, ndim, row_start, col, xy, tri, param, val=None):
+        """Scalar Poisson (ndim 1, param = (alpha, source)) or 2-D linear solid (ndim 2, param = (myu, lambda,
+        rho, gx, gy)) over a 2-D triangle mesh into a zeroed matrix: (vcrs, vdia, b)."""
+        nblk = row_start.size - 1
+        bb = ndim * ndim
+        f = self._f("assemble_tri2")
+        f.argtypes = [C.c_uint32, C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, _f64p, _f64p, _u32p, C.c_size_t,
+                      C.c_void_p]
+        f.restype = C.c_int
+        vc = np.zeros(max(col.size * bb, 1), np.float64)
+        vd = np.zeros(nblk * bb, np.float64)
+        b = np.zeros(nblk * ndim, np.float64)
+        tri = np.ascontiguousarray(tri, np.uint32)
+        v = None if val is None else np.ascontiguousarray(val, np.float64)
+        st = f(nblk, ndim, row_start, _nz(col), vc, vd, b, np.ascontiguousarray(param, np.float64),
+               np.ascontiguousarray(xy, np.float64), tri, tri.size // 3, _optr(v))
+        assert st == 0, "element block missing from the pattern"
+        return vc[: col.size * bb], vd, b
+
+
 def _nz(a):
     """Never hand a zero-length array to C (its data pointer may be NULL)."""
     if a.size == 0:

@@ -324,4 +324,29 @@ uint32_t ref_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *
   return static_cast<uint32_t>(h.size());
 }
 
+int ref_poisson_tri2(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs, double *vdia,
+                     double *b, double alpha, double source, const double *xy, const uint32_t *tri, size_t ntri,
+                     const double *val);  // ref_driver_nd.cpp
+
+// MergeLinSys_SolidLinear_Static_MeshTri2D (fem_solidlinear.h:155-187,
+// ndim 2, param = {myu, lambda, rho, gx, gy}) or, for ndim 1,
+// MergeLinSys_Poission_MeshTri2D (param = {alpha, source}); the contract of
+// orc_assemble_tri2.
+int ref_assemble_tri2(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                      double *vdia, double *b, const double *param, const double *xy, const uint32_t *tri,
+                      size_t ntri, const double *val) {
+  if (ndim == 1) return ref_poisson_tri2(nblk, row_start, col, vcrs, vdia, b, param[0], param[1], xy, tri, ntri, val);
+  dfm2::CMatrixSparse<double> m;
+  m.Initialize(nblk, 2, true);
+  m.SetPattern(row_start, nblk + 1, col, row_start[nblk]);
+  std::memcpy(m.val_crs_.data(), vcrs, sizeof(double) * 4 * row_start[nblk]);
+  std::memcpy(m.val_dia_.data(), vdia, sizeof(double) * 4 * nblk);
+  std::vector<double> zero((size_t)nblk * 2, 0.0);
+  dfm2::MergeLinSys_SolidLinear_Static_MeshTri2D(m, b, param[0], param[1], param[2], param[3], param[4], xy, nblk,
+                                                 tri, ntri, val ? val : zero.data());
+  std::memcpy(vcrs, m.val_crs_.data(), sizeof(double) * 4 * row_start[nblk]);
+  std::memcpy(vdia, m.val_dia_.data(), sizeof(double) * 4 * nblk);
+  return 0;
+}
+
 }  // extern "C"

@@ -5,7 +5,7 @@ oracle/Makefile), so it only works where the reference source tree exists.
 The outputs are small .npz files committed next to this script; the tests
 read them on machines without the reference.
 
-  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab]
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab nd]
 """
 from __future__ import annotations
 
@@ -206,6 +206,51 @@ def make_bicgstab(R):
     np.savez_compressed(os.path.join(HERE, "bicgstab.npz"), **out)
 
 
+def make_nd(R):
+    """Scalar (ndim 1) and 2x2 (ndim 2) systems of tests/nd_systems.py, all from
+    the reference: assembly (MergeLinSys_Poission_MeshTet3D,
+    MergeLinSys_Poission_MeshTri2D, MergeLinSys_SolidLinear_Static_MeshTri2D),
+    SetFixedBC, MatVec of a seeded vector, ILU(0) / ILU(1) factors, one forward
+    and backward sweep, Solve_PCG and Solve_PBiCGStab to 1e-10; plus a Merge of
+    an element that repeats a node, for ndim 1, 2 and 3."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import nd_systems as S
+    out = {}
+    for name, make in S.SYSTEMS.items():
+        s = make(R)
+        nd, n = s["ndim"], s["b"].size
+        out.update({f"{name}_{k}": s[k] for k in ("ind", "psup", "vc", "vd", "b", "bc", "elem")})
+        rng = np.random.default_rng(7)
+        x, y = rng.standard_normal(n), rng.standard_normal(n)
+        out[f"{name}_mv_x"], out[f"{name}_mv_y"] = x, y
+        out[f"{name}_mv"] = R.nd_matvec(nd, s["ind"], s["psup"], s["vc"], s["vd"], y, 1.5, x, 0.5)
+        for k in (0, 1):
+            rs, col, dia, ivc, ivd = S.factor(R, s, k)
+            t = f"{name}_k{k}"
+            out.update({f"{t}_rs": rs, f"{t}_col": col, f"{t}_dia": dia, f"{t}_vc": ivc, f"{t}_vd": ivd})
+            out[f"{t}_fwd"] = R.nd_ilu_forward(nd, rs, col, dia, ivc, ivd, x)
+            out[f"{t}_bwd"] = R.nd_ilu_backward(nd, rs, col, dia, ivc, x)
+            for solver in ("pcg", "pbicgstab"):
+                f = R.nd_solve_pcg if solver == "pcg" else R.nd_solve_pbicgstab
+                xs, _, hist = f(nd, s["ind"], s["psup"], s["vc"], s["vd"], rs, col, dia, ivc, ivd, s["b"], 1e-10, 1000)
+                out[f"{t}_{solver}_x"], out[f"{t}_{solver}_hist"] = xs, np.array(hist)
+                print(f"nd {name} ILU({k}) {solver}: {len(hist)} entries, last {hist[-1]:.3e}")
+    # Merge of one element whose nodes 0 and 2 coincide (diagonal rule of the reference)
+    for nd in (1, 2, 3):
+        ind = np.array([0, 2, 4, 6], np.uint32)
+        psup = np.array([1, 2, 0, 2, 0, 1], np.uint32)
+        rng = np.random.default_rng(20 + nd)
+        vc = rng.standard_normal(6 * nd * nd)
+        vd = rng.standard_normal(3 * nd * nd)
+        nodes = np.array([0, 1, 0, 2], np.uint32)
+        emat = rng.standard_normal(16 * nd * nd)
+        out[f"merge{nd}_vc0"], out[f"merge{nd}_vd0"], out[f"merge{nd}_emat"] = vc.copy(), vd.copy(), emat
+        st = R.nd_merge(nd, ind, psup, vc, vd, nodes, emat) if nd < 3 else R.merge(ind, psup, vc, vd, nodes, emat)
+        assert st == 0
+        out[f"merge{nd}_vc"], out[f"merge{nd}_vd"] = vc, vd
+    np.savez_compressed(os.path.join(HERE, "nd.npz"), **out)
+
+
 def main(which):
     build(quiet=True)
     R = reference()
@@ -228,6 +273,8 @@ def main(which):
         make_iluk(R)
     if "bicgstab" in which:
         make_bicgstab(R)
+    if "nd" in which:
+        make_nd(R)
 
 
 if __name__ == "__main__":
