@@ -69,6 +69,7 @@ SIGNATURES = {
     "dfm2g_bsr_create": [C.POINTER(_vp), _u, _u],
     "dfm2g_bsr_destroy": [_vp],
     "dfm2g_bsr_set_pattern": [_vp, _vp, _sz, _vp, _sz],
+    "dfm2g_bsr_ndim": [_vp, _pu],
     "dfm2g_bsr_info": [_vp, _pu, _psz],
     "dfm2g_bsr_set_zero": [_vp],
     "dfm2g_bsr_set_values": [_vp, _vp, _vp, _i],
@@ -106,6 +107,11 @@ SIGNATURES = {
     "dfm2g_tetmesh_info": [_vp, _pu, _psz],
     "dfm2g_tetmesh_assemble_linear": [_vp, _vp, _vp, _d, _d, _vp, _vp, _vp, _i],
     "dfm2g_tetmesh_dLdE": [_vp, _vp, _d, _vp, _vp, _vp, _i],
+    "dfm2g_tetmesh_assemble_poisson": [_vp, _vp, _d, _d, _vp, _vp, _i],
+    "dfm2g_trimesh2_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz],
+    "dfm2g_trimesh2_destroy": [_vp],
+    "dfm2g_trimesh2_assemble_poisson": [_vp, _vp, _d, _d, _vp, _vp, _i],
+    "dfm2g_trimesh2_assemble_solid_linear": [_vp, _vp, _d, _d, _d, _d, _d, _vp, _vp, _i],
     "dfm2g_cloth_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz, _vp, _sz],
     "dfm2g_cloth_destroy": [_vp],
     "dfm2g_cloth_info": [_vp, _pu, _pu],

@@ -138,9 +138,10 @@ int dfm2g_solve_pbicgstab(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "solve_pbicgstab: matrix has no pattern");
   if (!p || !p->has_factor || p->nblk != m->nblk)
     return fail(DFM2G_ERR_STATE, "solve_pbicgstab: preconditioner not decomposed for this matrix");
+  if (p->ndim != m->ndim) return fail(DFM2G_ERR_ARG, "solve_pbicgstab: preconditioner and matrix block sizes differ");
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_pbicgstab: null vector");
   DFM2G_TRY(ensure_context());
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   auto &W = g_bi;
   const unsigned grid = (unsigned)ctx().num_sms * 4;
   DFM2G_TRY(W.st.ensure(1));

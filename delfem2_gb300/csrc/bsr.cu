@@ -1,17 +1,40 @@
-// CMatrixSparse<double> (3x3 blocks) on the device: pattern, values, fixed
-// boundary conditions, MatVec, and the colour-scheduled Merge.
+// CMatrixSparse<double> on the device: pattern, values, fixed boundary
+// conditions, MatVec, and the colour-scheduled Merge, for 3x3 blocks (the
+// tuned path) and for 1x1 / 2x2 blocks (nd.cuh).
 //
 // Device layout: row_start[nblk+1] and col[nnz] (u32, the reference's
-// col_ind_ / row_ptr_), vcrs[9*nnz] and vdia[9*nblk] (f64, row-major 3x3), plus
-// an FP32 mirror vcrs32/vdia32 used by the mixed-precision solver.
+// col_ind_ / row_ptr_), vcrs[B*B*nnz] and vdia[B*B*nblk] (f64, row-major
+// B x B, B = ndim), plus an FP32 mirror vcrs32/vdia32 used by the
+// mixed-precision solver.
 #include <algorithm>
 #include <cstring>
 
 #include "common.cuh"
+#include "nd.cuh"
 #include "rowkern.cuh"
 #include "spmv_tma.cuh"
 
 namespace dfm2g {
+
+int require_3x3(const dfm2g_bsr_s *m, const char *what) {
+  if (m && m->ndim != 3) return fail(DFM2G_ERR_UNSUPPORTED, "%s: needs 3x3 blocks (matrix has ndim %u)", what, m->ndim);
+  return DFM2G_OK;
+}
+
+// y = alpha*K*x + beta*y for 1x1 and 2x2 blocks, one warp per block row.
+template <typename T, int B>
+__global__ void __launch_bounds__(256) k_nd_spmv(unsigned nblk, const unsigned *__restrict__ row_start,
+                                                 const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                                 const T *__restrict__ vdia, T *__restrict__ y, T alpha,
+                                                 const T *__restrict__ x, T beta) {
+  const unsigned lane = threadIdx.x & 31;
+  nd_spmv_rows<T, B>(nblk, row_start, col, vcrs, vdia, x, [&](unsigned row, const T s[B]) {
+    if (lane < (unsigned)B) {
+      T *py = y + (size_t)row * B + lane;
+      *py = beta * *py + alpha * nd_pick<T, B>(s, lane);
+    }
+  });
+}
 
 // ---------------------------------------------------------------------------
 // SpMV y = alpha*K*x + beta*y, one warp per block row (rows w, w+W, ...), in
@@ -111,7 +134,29 @@ int bsr_check_err(dfm2g_bsr_s *m) {
   return DFM2G_OK;
 }
 
+template <typename T>
+static void nd_spmv_launch(dfm2g_bsr_s *m, const T *vcrs, const T *vdia, T *y, T alpha, const T *x, T beta) {
+  const unsigned blocks = blocks_for((size_t)m->nblk * 32, 256, (unsigned)ctx().num_sms * 16);
+  if (m->ndim == 1)
+    k_nd_spmv<T, 1><<<blocks, 256, 0, stream()>>>(m->nblk, m->row_start.p, m->col.p, vcrs, vdia, y, alpha, x, beta);
+  else
+    k_nd_spmv<T, 2><<<blocks, 256, 0, stream()>>>(m->nblk, m->row_start.p, m->col.p, vcrs, vdia, y, alpha, x, beta);
+}
+
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta) {
+  if (m->ndim != 3) {
+    if (prec == DFM2G_F64) {
+      nd_spmv_launch<double>(m, m->vcrs.p, m->vdia.p, (double *)y, alpha, (const double *)x, beta);
+    } else if (prec == DFM2G_F32) {
+      DFM2G_TRY(bsr_ensure_f32(m));
+      nd_spmv_launch<float>(m, m->vcrs32.p, m->vdia32.p, (float *)y, (float)alpha, (const float *)x, (float)beta);
+    } else {
+      return fail(DFM2G_ERR_ARG, "matvec: prec must be DFM2G_F64 or DFM2G_F32");
+    }
+    note_launches(1);
+    DFM2G_LAUNCH_CHECK();
+    return DFM2G_OK;
+  }
   if (m->tiles_ok && (prec == DFM2G_F64 || prec == DFM2G_F32)) {
     const unsigned long long timeout = kWaitTimeoutNs;
     if (prec == DFM2G_F64) {
@@ -160,14 +205,15 @@ void to_f32(size_t n, const double *in, float *out) {
 int bsr_ensure_f32(dfm2g_bsr_s *m) {
   if (m->f32_valid) return DFM2G_OK;
   // +8 floats: bulk copies round their byte range up to 16 B past the last element
-  DFM2G_TRY(m->vcrs32.ensure(m->nnz * 9 + 8));
-  DFM2G_TRY(m->vdia32.ensure((size_t)m->nblk * 9 + 8));
+  const size_t bb = (size_t)m->ndim * m->ndim;
+  DFM2G_TRY(m->vcrs32.ensure(m->nnz * bb + 8));
+  DFM2G_TRY(m->vdia32.ensure((size_t)m->nblk * bb + 8));
   const unsigned cap = (unsigned)ctx().num_sms * 8;
   if (m->nnz)
-    k_to_f32<<<blocks_for(m->nnz * 9, 256, cap), 256, 0, stream()>>>(m->nnz * 9, m->vcrs.p, m->vcrs32.p);
+    k_to_f32<<<blocks_for(m->nnz * bb, 256, cap), 256, 0, stream()>>>(m->nnz * bb, m->vcrs.p, m->vcrs32.p);
   if (m->nblk)
-    k_to_f32<<<blocks_for((size_t)m->nblk * 9, 256, cap), 256, 0, stream()>>>((size_t)m->nblk * 9, m->vdia.p,
-                                                                            m->vdia32.p);
+    k_to_f32<<<blocks_for((size_t)m->nblk * bb, 256, cap), 256, 0, stream()>>>((size_t)m->nblk * bb, m->vdia.p,
+                                                                             m->vdia32.p);
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = true;
   return DFM2G_OK;
@@ -203,12 +249,34 @@ __global__ void k_bsr_fixed_bc(unsigned nblk, const unsigned *__restrict__ row_s
   }
 }
 
-__global__ void k_add_dia(unsigned nblk, double *vdia, double eps) {
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x) {
-    vdia[(size_t)i * 9 + 0] += eps;
-    vdia[(size_t)i * 9 + 4] += eps;
-    vdia[(size_t)i * 9 + 8] += eps;
+// The same for B x B blocks with B = ndim in {1, 2}.
+__global__ void k_nd_fixed_bc(unsigned nblk, unsigned B, const unsigned *__restrict__ row_start,
+                              const unsigned *__restrict__ col, double *__restrict__ vcrs, double *__restrict__ vdia,
+                              const int *__restrict__ bc) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
+  const unsigned bb = B * B;
+  for (unsigned row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nblk; row += nwarp) {
+    const unsigned s0 = row_start[row], s1 = row_start[row + 1];
+    for (unsigned s = s0 + lane; s < s1; s += 32) {
+      const unsigned j = col[s];
+      double *a = vcrs + (size_t)s * bb;
+      for (unsigned r = 0; r < B; ++r)
+        for (unsigned c = 0; c < B; ++c)
+          if (bc[(size_t)row * B + r] != 0 || bc[(size_t)j * B + c] != 0) a[r * B + c] = 0.0;
+    }
+    if (lane < bb) {
+      const unsigned r = lane / B, c = lane % B;
+      if (bc[(size_t)row * B + r] != 0 || bc[(size_t)row * B + c] != 0)
+        vdia[(size_t)row * bb + lane] = (r == c) ? 1.0 : 0.0;
+    }
   }
+}
+
+// vdia_i += eps I for B x B blocks.
+__global__ void k_add_dia(unsigned nblk, unsigned B, double *vdia, double eps) {
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < nblk; i += gridDim.x * blockDim.x)
+    for (unsigned r = 0; r < B; ++r) vdia[(size_t)i * B * B + r * (B + 1)] += eps;
 }
 
 __global__ void k_zero_bc(size_t n, double *__restrict__ b, const int *__restrict__ bc) {
@@ -241,22 +309,35 @@ __global__ void k_slot_map(size_t nelem, unsigned nno, const unsigned *__restric
   }
 }
 
+// One thread per (element of this colour, local node a) adds block row a of
+// the element matrix. As in the reference's Merge
+// (include/delfem2/ls_block_sparse.h:209-358), a pair (a, b) whose nodes are
+// the same block adds the (a, a) block to the diagonal; this differs from
+// (a, b) only for an element that repeats a node. The rows of a repeated node
+// all go to one block row, so the thread of its first occurrence adds them,
+// in the reference's (a, b) order, and the other occurrences' threads add
+// nothing.
 __global__ void k_merge_color(unsigned n, const unsigned *__restrict__ list, unsigned nno,
                               const unsigned *__restrict__ elem, const unsigned *__restrict__ slot,
-                              const double *__restrict__ emat, double *__restrict__ vcrs,
+                              const double *__restrict__ emat, unsigned bb, double *__restrict__ vcrs,
                               double *__restrict__ vdia) {
   const size_t total = (size_t)n * nno;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
     const size_t e = list[t / nno];
     const unsigned a = (unsigned)(t % nno);
     const unsigned i = elem[e * nno + a];
-    for (unsigned b = 0; b < nno; ++b) {
-      const size_t k = (e * nno + a) * nno + b;
-      const unsigned s = slot[k];
-      double *dst = (s == kDiag) ? vdia + (size_t)i * 9 : vcrs + (size_t)s * 9;
-      const double *src = emat + k * 9;
-#pragma unroll
-      for (int q = 0; q < 9; ++q) dst[q] += src[q];
+    bool first = true;
+    for (unsigned a0 = 0; a0 < a; ++a0) first = first && elem[e * nno + a0] != i;
+    if (!first) continue;
+    for (unsigned a2 = a; a2 < nno; ++a2) {
+      if (elem[e * nno + a2] != i) continue;
+      for (unsigned b = 0; b < nno; ++b) {
+        const size_t k = (e * nno + a2) * nno + b;
+        const unsigned s = slot[k];
+        double *dst = (s == kDiag) ? vdia + (size_t)i * bb : vcrs + (size_t)s * bb;
+        const double *src = emat + ((s == kDiag) ? (e * nno + a2) * nno + a2 : k) * bb;
+        for (unsigned q = 0; q < bb; ++q) dst[q] += src[q];
+      }
     }
   }
 }
@@ -323,10 +404,11 @@ extern "C" {
 
 int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim) {
   if (!out) return fail(DFM2G_ERR_ARG, "bsr_create: null out");
-  if (ndim != 3) return fail(DFM2G_ERR_UNSUPPORTED, "only 3x3 blocks are supported (ndim=%u)", ndim);
+  if (ndim < 1 || ndim > 3) return fail(DFM2G_ERR_UNSUPPORTED, "block size ndim=%u (1, 2 or 3 supported)", ndim);
   DFM2G_TRY(ensure_context());
   auto *m = new dfm2g_bsr_s();
   m->nblk = nblk;
+  m->ndim = ndim;
   *out = m;
   return DFM2G_OK;
 }
@@ -364,19 +446,21 @@ int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_s
   m->h_col.assign(col, col + ncol);
   DFM2G_TRY(m->row_start.resize(m->nblk + 1));
   // slack past the last element: bulk copies round their byte range up to 16 B
+  const size_t bb = (size_t)m->ndim * m->ndim;
   DFM2G_TRY(m->col.resize(ncol + 8));
-  DFM2G_TRY(m->vcrs.resize(ncol * 9 + 4));
-  DFM2G_TRY(m->vdia.resize((size_t)m->nblk * 9 + 4));
+  DFM2G_TRY(m->vcrs.resize(ncol * bb + 4));
+  DFM2G_TRY(m->vdia.resize((size_t)m->nblk * bb + 4));
   DFM2G_CUDA(cudaMemcpyAsync(m->row_start.p, row_start, sizeof(unsigned) * (m->nblk + 1), cudaMemcpyHostToDevice,
                              stream()));
   if (ncol) DFM2G_CUDA(cudaMemcpyAsync(m->col.p, col, sizeof(unsigned) * ncol, cudaMemcpyHostToDevice, stream()));
-  DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * (ncol * 9 + 1), stream()));
-  DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * ((size_t)m->nblk * 9 + 1), stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * (ncol * bb + 1), stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * ((size_t)m->nblk * bb + 1), stream()));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   m->has_pattern = true;
   m->f32_valid = false;
   m->pattern_version++;
-  DFM2G_TRY(bsr_tiles_build(m));
+  m->tiles_ok = false;
+  if (m->ndim == 3) DFM2G_TRY(bsr_tiles_build(m));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
 }
@@ -388,10 +472,18 @@ int dfm2g_bsr_info(dfm2g_bsr m, unsigned *nblk, size_t *nnz) {
   return DFM2G_OK;
 }
 
+int dfm2g_bsr_ndim(dfm2g_bsr m, unsigned *ndim) {
+  DFM2G_TRY(check_bsr(m, false));
+  if (!ndim) return fail(DFM2G_ERR_ARG, "bsr_ndim: null out");
+  *ndim = m->ndim;
+  return DFM2G_OK;
+}
+
 int dfm2g_bsr_set_zero(dfm2g_bsr m) {
   DFM2G_TRY(check_bsr(m));
-  DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * m->nnz * 9, stream()));
-  DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * m->nblk * 9, stream()));
+  const size_t bb = (size_t)m->ndim * m->ndim;
+  DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * m->nnz * bb, stream()));
+  DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * m->nblk * bb, stream()));
   m->f32_valid = false;
   return DFM2G_OK;
 }
@@ -399,8 +491,9 @@ int dfm2g_bsr_set_zero(dfm2g_bsr m) {
 int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, int mem) {
   DFM2G_TRY(check_bsr(m));
   const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  if (vcrs && m->nnz) DFM2G_CUDA(cudaMemcpyAsync(m->vcrs.p, vcrs, sizeof(double) * 9 * m->nnz, k, stream()));
-  if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(m->vdia.p, vdia, sizeof(double) * 9 * m->nblk, k, stream()));
+  const size_t bb = (size_t)m->ndim * m->ndim;
+  if (vcrs && m->nnz) DFM2G_CUDA(cudaMemcpyAsync(m->vcrs.p, vcrs, sizeof(double) * bb * m->nnz, k, stream()));
+  if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(m->vdia.p, vdia, sizeof(double) * bb * m->nblk, k, stream()));
   if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   m->f32_valid = false;
   return DFM2G_OK;
@@ -409,8 +502,9 @@ int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, in
 int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem) {
   DFM2G_TRY(check_bsr(m));
   const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  if (vcrs && m->nnz) DFM2G_CUDA(cudaMemcpyAsync(vcrs, m->vcrs.p, sizeof(double) * 9 * m->nnz, k, stream()));
-  if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, m->vdia.p, sizeof(double) * 9 * m->nblk, k, stream()));
+  const size_t bb = (size_t)m->ndim * m->ndim;
+  if (vcrs && m->nnz) DFM2G_CUDA(cudaMemcpyAsync(vcrs, m->vcrs.p, sizeof(double) * bb * m->nnz, k, stream()));
+  if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, m->vdia.p, sizeof(double) * bb * m->nblk, k, stream()));
   if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
 }
@@ -419,9 +513,13 @@ int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem) {
   DFM2G_TRY(check_bsr(m));
   if (!bc) return fail(DFM2G_ERR_ARG, "set_fixed_bc: null bc");
   VecArg<int> a;
-  DFM2G_TRY(a.in(bc, (size_t)m->nblk * 3, mem, true));
-  k_bsr_fixed_bc<<<blocks_for((size_t)m->nblk * 32, 256, ctx().num_sms * 16), 256, 0, stream()>>>(
-      m->nblk, m->row_start.p, m->col.p, m->vcrs.p, m->vdia.p, a.dev());
+  DFM2G_TRY(a.in(bc, (size_t)m->nblk * m->ndim, mem, true));
+  const unsigned blocks = blocks_for((size_t)m->nblk * 32, 256, ctx().num_sms * 16);
+  if (m->ndim == 3)
+    k_bsr_fixed_bc<<<blocks, 256, 0, stream()>>>(m->nblk, m->row_start.p, m->col.p, m->vcrs.p, m->vdia.p, a.dev());
+  else
+    k_nd_fixed_bc<<<blocks, 256, 0, stream()>>>(m->nblk, m->ndim, m->row_start.p, m->col.p, m->vcrs.p, m->vdia.p,
+                                                a.dev());
   DFM2G_LAUNCH_CHECK();
   if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   m->f32_valid = false;
@@ -430,7 +528,7 @@ int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem) {
 
 int dfm2g_bsr_add_dia(dfm2g_bsr m, double eps) {
   DFM2G_TRY(check_bsr(m));
-  k_add_dia<<<blocks_for(m->nblk, 256, ctx().num_sms * 8), 256, 0, stream()>>>(m->nblk, m->vdia.p, eps);
+  k_add_dia<<<blocks_for(m->nblk, 256, ctx().num_sms * 8), 256, 0, stream()>>>(m->nblk, m->ndim, m->vdia.p, eps);
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return DFM2G_OK;
@@ -445,7 +543,7 @@ int dfm2g_bsr_update_f32(dfm2g_bsr m) {
 int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x, double beta, int mem) {
   DFM2G_TRY(check_bsr(m));
   if (!y || !x) return fail(DFM2G_ERR_ARG, "matvec: null vector");
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   if (prec == DFM2G_F64) {
     VecArg<double> ay, ax;
     DFM2G_TRY(ay.in((double *)y, n, mem, true));
@@ -504,8 +602,9 @@ int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned 
   DFM2G_CUDA(cudaMemcpyAsync(d_list.p, by_color.data(), nelem * sizeof(unsigned), cudaMemcpyHostToDevice,
                              stream()));
   DFM2G_CUDA(cudaMemsetAsync(d_missing.p, 0, sizeof(int), stream()));
+  const unsigned bb = m->ndim * m->ndim;
   VecArg<double> a_emat;
-  DFM2G_TRY(a_emat.in(emat, (size_t)nelem * nnoel * nnoel * 9, mem, true));
+  DFM2G_TRY(a_emat.in(emat, (size_t)nelem * nnoel * nnoel * bb, mem, true));
   const size_t nslot = (size_t)nelem * nnoel * nnoel;
   k_slot_map<<<blocks_for(nslot, 256, ctx().num_sms * 16), 256, 0, stream()>>>(
       nelem, nnoel, d_elem.p, m->row_start.p, m->col.p, d_slot.p, d_missing.p);
@@ -517,7 +616,7 @@ int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned 
   for (size_t c = 0; c + 1 < color_start.size(); ++c) {
     const unsigned n = color_start[c + 1] - color_start[c];
     k_merge_color<<<blocks_for((size_t)n * nnoel, 128, ctx().num_sms * 16), 128, 0, stream()>>>(
-        n, d_list.p + color_start[c], nnoel, d_elem.p, d_slot.p, a_emat.dev(), m->vcrs.p, m->vdia.p);
+        n, d_list.p + color_start[c], nnoel, d_elem.p, d_slot.p, a_emat.dev(), bb, m->vcrs.p, m->vdia.p);
     DFM2G_LAUNCH_CHECK();
   }
   DFM2G_CUDA(cudaStreamSynchronize(stream()));

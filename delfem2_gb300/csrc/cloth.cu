@@ -498,6 +498,7 @@ __global__ void k_quad_adjoint(unsigned n, const unsigned *__restrict__ list, co
 
 static int check_cloth(dfm2g_cloth c, dfm2g_bsr m) {
   if (!c || !m) return fail(DFM2G_ERR_ARG, "cloth: null handle");
+  DFM2G_TRY(require_3x3(m, "cloth"));
   if (m != c->bsr || m->pattern_version != c->pattern_version)
     return fail(DFM2G_ERR_STATE, "cloth: matrix pattern differs from the one the mesh was mapped to");
   return DFM2G_OK;
@@ -631,6 +632,7 @@ int dfm2g_cloth_create(dfm2g_cloth *out, dfm2g_bsr m, const double *xyz0, size_t
                        size_t ntri, const unsigned *quad, size_t nquad) {
   if (!out) return fail(DFM2G_ERR_ARG, "cloth_create: null out");
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "cloth_create: matrix has no pattern");
+  DFM2G_TRY(require_3x3(m, "cloth_create"));
   if (np != m->nblk) return fail(DFM2G_ERR_ARG, "cloth_create: np (%zu) != matrix blocks (%u)", np, m->nblk);
   if ((ntri && !tri) || (nquad && !quad) || (np && !xyz0)) return fail(DFM2G_ERR_ARG, "cloth_create: null array");
   if (ntri > 0xFFFFFFFFull / 9 || nquad > 0xFFFFFFFFull / 16) return fail(DFM2G_ERR_ARG, "cloth_create: too large");

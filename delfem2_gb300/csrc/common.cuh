@@ -217,6 +217,7 @@ __device__ __forceinline__ bool grid_sum_last(double partial, double *partials,
 // ---- handle layouts -----------------------------------------------------------------
 struct dfm2g_bsr_s {
   unsigned nblk = 0;
+  unsigned ndim = 3;  // block size: 3x3 (TMA SpMV, every sweep schedule), 1x1 or 2x2 (nd.cuh kernels)
   size_t nnz = 0;
   bool has_pattern = false;
   std::vector<unsigned> h_row_start, h_col;  // host copy of the pattern
@@ -270,6 +271,7 @@ struct StreamSched {
 
 struct dfm2g_ilu_s {
   unsigned nblk = 0;
+  unsigned ndim = 3;  // block size of the matrix the pattern was taken from
   size_t nnz = 0;
   bool has_pattern = false, has_factor = false, f32_valid = false;
   int sweep_mode = DFM2G_SWEEP_SYNCFREE;
@@ -332,6 +334,9 @@ template <typename T>
 int part_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout);
 int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, double beta);
+// Fails with DFM2G_ERR_UNSUPPORTED unless the matrix has 3x3 blocks (entry
+// points whose kernels are written for 3x3 blocks call it first).
+int require_3x3(const dfm2g_bsr_s *m, const char *what);
 int bsr_tiles_build(dfm2g_bsr_s *m);
 int bsr_check_err(dfm2g_bsr_s *m);
 int ilu_ensure_f32(dfm2g_ilu_s *p);

@@ -1,5 +1,6 @@
-// Linear-tet elasticity on the device: colour-scheduled, atomic-free assembly
-// of K and b (per-tet Young's modulus) and the adjoint element term dL/dE.
+// Linear tets on the device: colour-scheduled, atomic-free assembly of the
+// elasticity K and b (3x3 blocks, per-tet Young's modulus), the adjoint element
+// term dL/dE, and the scalar Poisson K and b (1x1 blocks).
 //
 // Layout: tet[4*ntet] node ids, slot[16*ntet] with slot[16e + 4a + b] the
 // val_crs_ slot of block (tet[e][a], tet[e][b]) (0xffffffff on the diagonal),
@@ -91,6 +92,49 @@ __global__ void __launch_bounds__(128) k_tet_assemble(unsigned n, const unsigned
   for (int r = 0; r < 3; ++r) rhs[(size_t)i * 3 + r] += res[r];
 }
 
+// One thread per (tet of this colour, local node a): row a of the scalar
+// element matrix of EMat_Poisson_Tet3D (include/delfem2/fem_poisson.cpp:
+// 163-194), K_e[a][b] = alpha vol (dN_a . dN_b), added to the diagonal (the
+// (a, a) entry when both nodes are one block, as the reference's Merge does)
+// or to the mapped slot; b_i += source vol / 4 - sum_b K_ab val_b.
+__global__ void __launch_bounds__(128) k_tet_poisson(unsigned n, const unsigned *__restrict__ list,
+                                                     const unsigned *__restrict__ tet,
+                                                     const unsigned *__restrict__ slot,
+                                                     const double *__restrict__ xyz, double alpha, double source,
+                                                     const double *__restrict__ val, double *vcrs, double *vdia,
+                                                     double *rhs) {
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * 4u) return;
+  const unsigned e = list[t >> 2], a = t & 3u;
+  unsigned nd[4];
+  double P[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    nd[k] = tet[(size_t)e * 4 + k];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) P[k][d] = xyz[(size_t)nd[k] * 3 + d];
+  }
+  double dN[4][3];
+  const double vol = tet_geometry(P, dN);
+  double da[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) da[d] = (a == 0) ? dN[0][d] : (a == 1) ? dN[1][d] : (a == 2) ? dN[2][d] : dN[3][d];
+  const double kaa = alpha * vol * (da[0] * da[0] + da[1] * da[1] + da[2] * da[2]);
+  const unsigned i = nd[a];
+  double res = source * vol * 0.25;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const double k = alpha * vol * (da[0] * dN[b][0] + da[1] * dN[b][1] + da[2] * dN[b][2]);
+    if (val) res -= k * val[nd[b]];
+    const unsigned s = slot[(size_t)e * 16 + a * 4 + b];
+    if (s == kDiagSlot)
+      vdia[i] += kaa;
+    else
+      vcrs[s] += k;
+  }
+  rhs[i] += res;
+}
+
 // dL/dE_e = -lam_e^T (K_e / E_e) u_e with G(v)[r][c] = sum_k v_k[r] dN_k[c]:
 // lam^T K_e u = vol (lambda1 tr(GL) tr(GU) + myu1 (tr(GL GU) + GL:GU)),
 // lambda1 = nu/((1+nu)(1-2nu)), myu1 = 1/(2(1+nu)) (the moduli at E = 1).
@@ -144,6 +188,7 @@ int dfm2g_tetmesh_create(dfm2g_tetmesh *out, dfm2g_bsr m, const double *xyz, siz
                          size_t ntet) {
   if (!out) return fail(DFM2G_ERR_ARG, "tetmesh_create: null out");
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "tetmesh_create: matrix has no pattern");
+  if (m->ndim == 2) return fail(DFM2G_ERR_UNSUPPORTED, "tetmesh_create: 2x2 blocks (tets take 1x1 or 3x3)");
   if (np != m->nblk) return fail(DFM2G_ERR_ARG, "tetmesh_create: np (%zu) != matrix blocks (%u)", np, m->nblk);
   if ((ntet && !tet) || (np && !xyz)) return fail(DFM2G_ERR_ARG, "tetmesh_create: null mesh array");
   if (ntet > 0xFFFFFFFFull / 16) return fail(DFM2G_ERR_ARG, "tetmesh_create: too many tets");
@@ -197,6 +242,7 @@ int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const double *yo
   if (!t || !m) return fail(DFM2G_ERR_ARG, "assemble: null handle");
   if (m != t->bsr || m->pattern_version != t->pattern_version)
     return fail(DFM2G_ERR_STATE, "assemble: matrix pattern differs from the one the mesh was mapped to");
+  DFM2G_TRY(require_3x3(m, "tetmesh_assemble_linear"));
   if (!young || !g || !b) return fail(DFM2G_ERR_ARG, "assemble: null argument");
   VecArg<double> ay, ad, ab;
   DFM2G_TRY(ay.in(young, t->ntet, mem, true));
@@ -208,6 +254,28 @@ int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const double *yo
         n, t->by_color.p + t->color_start[c], t->tet.p, t->slot.p, t->xyz.p, ay.dev(), nu, rho, g[0], g[1], g[2],
         disp ? ad.dev() : nullptr, m->vcrs.p, m->vdia.p, ab.dev());
   }
+  DFM2G_LAUNCH_CHECK();
+  m->f32_valid = false;
+  return ab.copy_back();
+}
+
+int dfm2g_tetmesh_assemble_poisson(dfm2g_tetmesh t, dfm2g_bsr m, double alpha, double source, const double *val,
+                                   double *b, int mem) {
+  if (!t || !m) return fail(DFM2G_ERR_ARG, "assemble_poisson: null handle");
+  if (m != t->bsr || m->pattern_version != t->pattern_version)
+    return fail(DFM2G_ERR_STATE, "assemble_poisson: matrix pattern differs from the one the mesh was mapped to");
+  if (m->ndim != 1) return fail(DFM2G_ERR_UNSUPPORTED, "assemble_poisson: needs a scalar (ndim 1) matrix");
+  if (!b) return fail(DFM2G_ERR_ARG, "assemble_poisson: null b");
+  VecArg<double> av, ab;
+  if (val) DFM2G_TRY(av.in(val, t->np, mem, true));
+  DFM2G_TRY(ab.in(b, t->np, mem, true));
+  for (size_t c = 0; c + 1 < t->color_start.size(); ++c) {
+    const unsigned n = t->color_start[c + 1] - t->color_start[c];
+    k_tet_poisson<<<blocks_for((size_t)n * 4, 128), 128, 0, stream()>>>(
+        n, t->by_color.p + t->color_start[c], t->tet.p, t->slot.p, t->xyz.p, alpha, source, val ? av.dev() : nullptr,
+        m->vcrs.p, m->vdia.p, ab.dev());
+  }
+  note_launches((unsigned)(t->color_start.empty() ? 0 : t->color_start.size() - 1));
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return ab.copy_back();

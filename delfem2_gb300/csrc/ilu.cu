@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "nd.cuh"
 #include "rowkern.cuh"
 
 namespace dfm2g {
@@ -286,6 +287,7 @@ static int compute_levels(dfm2g_ilu_s *p, bool backward) {
 // ---------------------------------------------------------------------------
 // CopyValue: every matrix block goes to the ILU slot of the same column (binary
 // search in the sorted ILU row); blocks without a slot are dropped.
+template <unsigned BB>
 __global__ void k_ilu_copy(unsigned nblk, const unsigned *__restrict__ m_row_start,
                            const unsigned *__restrict__ m_col, const double *__restrict__ m_vcrs,
                            const unsigned *__restrict__ p_row_start, const unsigned *__restrict__ p_col,
@@ -302,7 +304,7 @@ __global__ void k_ilu_copy(unsigned nblk, const unsigned *__restrict__ m_row_sta
       }
       if (lo < q1 && p_col[lo] == j) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) p_vcrs[(size_t)lo * 9 + k] = m_vcrs[(size_t)s * 9 + k];
+        for (unsigned k = 0; k < BB; ++k) p_vcrs[(size_t)lo * BB + k] = m_vcrs[(size_t)s * BB + k];
       }
     }
   }
@@ -387,6 +389,96 @@ __global__ void __launch_bounds__(256) k_ilu_factor_level(const unsigned *__rest
 #pragma unroll
       for (int c = 0; c < 3; ++c)
         u[r * 3 + c] = v[r * 3 + 0] * t[0 * 3 + c] + v[r * 3 + 1] * t[1 * 3 + c] + v[r * 3 + 2] * t[2 * 3 + c];
+  }
+}
+
+// The same for 1x1 and 2x2 blocks, in the reference's arithmetic
+// (ls_ilu_block_sparse.cpp:168-285): every product and sum is rounded on its
+// own (no fused multiply-add), in the reference's order, so the factors equal
+// the reference's bit for bit. A_ij -= A_ik A_kj; the pivot is inverted when
+// |d| (1x1) or |det| (2x2) exceeds 1e-30, else counted and left; then
+// U_ij <- D_i^-1 U_ij.
+template <int B>
+__global__ void __launch_bounds__(256) k_ilu_factor_level_nd(const unsigned *__restrict__ rows, unsigned nrows,
+                                                             const unsigned *__restrict__ row_start,
+                                                             const unsigned *__restrict__ col,
+                                                             const unsigned *__restrict__ dia_ind, double *vcrs,
+                                                             double *vdia, int *nsing) {
+  constexpr unsigned BB = B * B;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nrows) return;
+  const unsigned i = rows[w];
+  const unsigned s0 = row_start[i], s1 = row_start[i + 1], sd = dia_ind[i];
+  for (unsigned sk = s0; sk < sd; ++sk) {
+    const unsigned k = col[sk];
+    double aik[BB];
+#pragma unroll
+    for (unsigned q = 0; q < BB; ++q) aik[q] = vcrs[(size_t)sk * BB + q];
+    const unsigned u0 = dia_ind[k], u1 = row_start[k + 1];
+    const unsigned ntask = (u1 - u0) * BB;
+    for (unsigned t = lane; t < ntask; t += 32) {
+      const unsigned uu = t / BB, e = t - uu * BB, r = e / B, c = e - r * B;
+      const unsigned sj = u0 + uu;
+      const unsigned j = col[sj];
+      double *dst;
+      if (j == i) {
+        dst = vdia + (size_t)i * BB;
+      } else {
+        unsigned lo = s0, hi = s1;
+        while (lo < hi) {
+          const unsigned mid = (lo + hi) >> 1;
+          if (col[mid] < j) lo = mid + 1; else hi = mid;
+        }
+        if (lo >= s1 || col[lo] != j) continue;
+        dst = vcrs + (size_t)lo * BB;
+      }
+      const double *akj = vcrs + (size_t)sj * BB;
+      double sum = __dmul_rn(aik[r * B], akj[c]);
+#pragma unroll
+      for (int q = 1; q < B; ++q) sum = __dadd_rn(sum, __dmul_rn(aik[r * B + q], akj[q * B + c]));
+      dst[e] = __dsub_rn(dst[e], sum);
+    }
+    __syncwarp();
+  }
+  double d[BB], v[BB];
+#pragma unroll
+  for (unsigned q = 0; q < BB; ++q) v[q] = d[q] = vdia[(size_t)i * BB + q];  // a singular pivot stays as it is
+  bool singular;
+  if constexpr (B == 1) {
+    singular = !(fabs(d[0]) > 1.0e-30);
+    if (!singular) v[0] = 1.0 / d[0];
+  } else {
+    const double det = __dsub_rn(__dmul_rn(d[0], d[3]), __dmul_rn(d[1], d[2]));
+    singular = !(fabs(det) > 1.0e-30);
+    if (!singular) {
+      const double inv_det = 1.0 / det;
+      v[0] = __dmul_rn(inv_det, d[3]);
+      v[1] = __dmul_rn(-inv_det, d[1]);
+      v[2] = __dmul_rn(-inv_det, d[2]);
+      v[3] = __dmul_rn(inv_det, d[0]);
+    }
+  }
+  if (singular && lane == 0) atomicAdd(nsing, 1);
+  __syncwarp();
+  if (lane < BB) {
+    double o = v[0];
+#pragma unroll
+    for (unsigned q = 1; q < BB; ++q)
+      if (q == lane) o = v[q];
+    vdia[(size_t)i * BB + lane] = o;
+  }
+  for (unsigned s = sd + lane; s < s1; s += 32) {
+    double *u = vcrs + (size_t)s * BB;
+    if constexpr (B == 1) {
+      u[0] = __dmul_rn(u[0], v[0]);
+    } else {
+      const double t0 = u[0], t1 = u[1], t2 = u[2], t3 = u[3];
+      u[0] = __dadd_rn(__dmul_rn(v[0], t0), __dmul_rn(v[1], t2));
+      u[1] = __dadd_rn(__dmul_rn(v[0], t1), __dmul_rn(v[1], t3));
+      u[2] = __dadd_rn(__dmul_rn(v[2], t0), __dmul_rn(v[3], t2));
+      u[3] = __dadd_rn(__dmul_rn(v[2], t1), __dmul_rn(v[3], t3));
+    }
   }
 }
 
@@ -514,6 +606,64 @@ __global__ void __launch_bounds__(256) k_sweep_syncfree(unsigned n, const uint4 
   }
 }
 
+// Sweeps for 1x1 and 2x2 blocks (nd.cuh): one warp per row, the lanes over
+// the row's triangle blocks. The level kernel works in place on `out` (rows of
+// one level are independent); the sync-free kernel is the same co-resident
+// grid as k_sweep_syncfree, waiting (bounded) on each needed out_j.
+template <typename T, bool FWD, int B>
+__device__ __forceinline__ T nd_sweep_value(const uint4 m, unsigned lane, const T t[B], const T *__restrict__ vdia) {
+  if constexpr (FWD) {
+    const T *d = vdia + (size_t)m.x * (B * B) + (size_t)lane * B;
+    T z = d[0] * t[0];
+#pragma unroll
+    for (int c = 1; c < B; ++c) z += d[c] * t[c];
+    return z;
+  } else {
+    return nd_pick<T, B>(t, lane);
+  }
+}
+
+template <typename T, bool FWD, int B>
+__global__ void __launch_bounds__(256) k_sweep_level_nd(const uint4 *__restrict__ meta, unsigned nrows,
+                                                        const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                                        const T *__restrict__ vdia, T *out, const int *skip) {
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nrows || (skip && *skip)) return;
+  const uint4 m = meta[w];
+  T t[B];
+#pragma unroll
+  for (int r = 0; r < B; ++r) t[r] = out[(size_t)m.x * B + r];
+  T acc[B];
+  nd_row_sum<T, B, false>(lane, m.y, m.z, col, vcrs, out, acc, nullptr, 0);
+#pragma unroll
+  for (int r = 0; r < B; ++r) t[r] -= acc[r];
+  __syncwarp();  // every lane has read row m.x's input before it is overwritten
+  if (lane < (unsigned)B) out[(size_t)m.x * B + lane] = nd_sweep_value<T, FWD, B>(m, lane, t, vdia);
+}
+
+template <typename T, bool FWD, int B>
+__global__ void __launch_bounds__(256) k_sweep_syncfree_nd(unsigned n, const uint4 *__restrict__ meta,
+                                                           const unsigned *__restrict__ col,
+                                                           const T *__restrict__ vcrs, const T *__restrict__ vdia,
+                                                           const T *in, T *out, int *err,
+                                                           unsigned long long timeout_ns, const int *skip) {
+  if (skip && *skip) return;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n; q += nwarp) {
+    const uint4 m = meta[q];
+    T acc[B];
+    nd_row_sum<T, B, true>(lane, m.y, m.z, col, vcrs, out, acc, err, timeout_ns);
+    if (lane < (unsigned)B) {
+      T t[B];
+#pragma unroll
+      for (int r = 0; r < B; ++r) t[r] = in[(size_t)m.x * B + r] - acc[r];
+      st_relaxed(out + (size_t)m.x * B + lane, nd_sweep_value<T, FWD, B>(m, lane, t, vdia));
+    }
+  }
+}
+
 template <typename T>
 __global__ void k_copy_guarded(size_t n, const T *__restrict__ in, T *__restrict__ out, const int *skip) {
   if (skip && *skip) return;
@@ -531,11 +681,56 @@ static int coop_blocks(const void *kernel, int *cache) {
   return DFM2G_OK;
 }
 
+template <typename T, int B>
+static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia,
+                         const int *skip, bool prefilled) {
+  const unsigned n = p->nblk;
+  const uint4 *meta = forward ? p->meta_f.p : p->meta_b.p;
+  if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
+    if (in != out) {
+      k_copy_guarded<T><<<blocks_for((size_t)n * B, 256, ctx().num_sms * 4), 256, 0, stream()>>>((size_t)n * B, in,
+                                                                                                 out, skip);
+      DFM2G_LAUNCH_CHECK();
+    }
+    const std::vector<unsigned> &ls = forward ? p->h_lstart_f : p->h_lstart_b;
+    for (size_t l = 0; l + 1 < ls.size(); ++l) {
+      const unsigned nrows = ls[l + 1] - ls[l];
+      const unsigned blocks = blocks_for((size_t)nrows * 32, 256);
+      if (forward)
+        k_sweep_level_nd<T, true, B><<<blocks, 256, 0, stream()>>>(meta + ls[l], nrows, p->col.p, vcrs, vdia, out,
+                                                                  skip);
+      else
+        k_sweep_level_nd<T, false, B><<<blocks, 256, 0, stream()>>>(meta + ls[l], nrows, p->col.p, vcrs, vdia, out,
+                                                                   skip);
+    }
+    note_launches((unsigned)(ls.size() - 1) + (in != out ? 1u : 0u));
+    DFM2G_LAUNCH_CHECK();
+    return DFM2G_OK;
+  }
+  if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
+  if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * B, stream()));
+  void *kernel = forward ? (void *)k_sweep_syncfree_nd<T, true, B> : (void *)k_sweep_syncfree_nd<T, false, B>;
+  int *cache = &p->coop_cache[sizeof(T) == 8 ? 1 : 0][forward ? 1 : 0][0];
+  DFM2G_TRY(coop_blocks<T>(kernel, cache));
+  const unsigned want = blocks_for((size_t)n * 32, 256);
+  const unsigned blocks = std::min<unsigned>(want, (unsigned)*cache);
+  const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+  unsigned long long timeout = kWaitTimeoutNs + 20000ull * nlev;
+  int *err = p->err.p;
+  void *args[] = {(void *)&n, (void *)&meta, (void *)&p->col.p, (void *)&vcrs, (void *)&vdia, (void *)&in,
+                  (void *)&out, (void *)&err, (void *)&timeout, (void *)&skip};
+  DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(256), args, 0, stream()));
+  note_launches(1);
+  return DFM2G_OK;
+}
+
 template <typename T>
 static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia,
                       const int *skip, bool prefilled) {
   const unsigned n = p->nblk;
   if (n == 0) return DFM2G_OK;
+  if (p->ndim == 1) return nd_sweep_impl<T, 1>(p, forward, in, out, vcrs, vdia, skip, prefilled);
+  if (p->ndim == 2) return nd_sweep_impl<T, 2>(p, forward, in, out, vcrs, vdia, skip, prefilled);
   if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
     // levels in order; rows of one level are independent (in == out allowed)
     if (in != out) {
@@ -613,10 +808,11 @@ int ilu_sweep_guarded(dfm2g_ilu_s *p, int prec, bool forward, const void *in, vo
 int ilu_ensure_f32(dfm2g_ilu_s *p) {
   if (p->f32_valid) return DFM2G_OK;
   if (!p->has_factor) return fail(DFM2G_ERR_STATE, "ILU not decomposed");
-  DFM2G_TRY(p->vcrs32.ensure(p->nnz * 9 + 1));
-  DFM2G_TRY(p->vdia32.ensure((size_t)p->nblk * 9 + 1));
-  to_f32(p->nnz * 9, p->vcrs.p, p->vcrs32.p);
-  to_f32((size_t)p->nblk * 9, p->vdia.p, p->vdia32.p);
+  const size_t bb = (size_t)p->ndim * p->ndim;
+  DFM2G_TRY(p->vcrs32.ensure(p->nnz * bb + 1));
+  DFM2G_TRY(p->vdia32.ensure((size_t)p->nblk * bb + 1));
+  to_f32(p->nnz * bb, p->vcrs.p, p->vcrs32.p);
+  to_f32((size_t)p->nblk * bb, p->vdia.p, p->vdia32.p);
   DFM2G_LAUNCH_CHECK();
   DFM2G_TRY(group_values_fill(p));
   p->f32_valid = true;
@@ -687,16 +883,18 @@ static int ilu_symbolic_k(unsigned n, const std::vector<unsigned> &mrs, const st
 
 // Installs an ILU pattern (row offsets and columns, rows sorted or not):
 // device copies, row sort + dia_ind, level sets and sweep schedules.
-static int ilu_install_pattern(dfm2g_ilu p, unsigned n, size_t nnz, const unsigned *rs_src, const unsigned *col_src,
-                               cudaMemcpyKind kind) {
+static int ilu_install_pattern(dfm2g_ilu p, unsigned n, unsigned ndim, size_t nnz, const unsigned *rs_src,
+                               const unsigned *col_src, cudaMemcpyKind kind) {
   p->nblk = n;
+  p->ndim = ndim;
   p->nnz = nnz;
   p->has_pattern = p->has_factor = p->f32_valid = false;
+  const size_t bb = (size_t)ndim * ndim;
   DFM2G_TRY(p->row_start.resize(n + 1));
   DFM2G_TRY(p->col.resize(nnz + 1));
   DFM2G_TRY(p->dia_ind.resize(n + 1));
-  DFM2G_TRY(p->vcrs.resize(nnz * 9 + 4));
-  DFM2G_TRY(p->vdia.resize((size_t)n * 9 + 4));
+  DFM2G_TRY(p->vcrs.resize(nnz * bb + 4));
+  DFM2G_TRY(p->vdia.resize((size_t)n * bb + 4));
   DFM2G_CUDA(cudaMemcpyAsync(p->row_start.p, rs_src, sizeof(unsigned) * (n + 1), kind, stream()));
   if (nnz) DFM2G_CUDA(cudaMemcpyAsync(p->col.p, col_src, sizeof(unsigned) * nnz, kind, stream()));
   if (n) {
@@ -723,14 +921,19 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, size_t nnz, const unsign
       for (int &c : b) c = 0;
   DFM2G_TRY(compute_levels(p, false));
   DFM2G_TRY(compute_levels(p, true));
-  DFM2G_TRY(group_schedules_build(p));
-  DFM2G_TRY(part_schedules_build(p));
   stream_schedules_reset(p);
+  if (ndim == 3) {  // the blob and row-range schedules are written for 3x3 blocks
+    DFM2G_TRY(group_schedules_build(p));
+    DFM2G_TRY(part_schedules_build(p));
+  } else {
+    p->gs_f.ok = p->gs_b.ok = false;
+    p->parts_ok = false;
+  }
   // The blob schedule is correct but, with one CTA barrier per unit, a single
   // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
   // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
   p->sweep_mode = DFM2G_SWEEP_SYNCFREE;
-  const size_t nvec = (size_t)n * 3 + 1;
+  const size_t nvec = (size_t)n * ndim + 1;
   DFM2G_TRY(p->tmp64a.resize(nvec));
   DFM2G_TRY(p->tmp64b.resize(nvec));
   DFM2G_TRY(p->tmp32a.resize(nvec));
@@ -771,7 +974,7 @@ int dfm2g_ilu_destroy(dfm2g_ilu p) {
 int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "set_pattern0: matrix has no pattern");
-  return ilu_install_pattern(p, m->nblk, m->nnz, m->row_start.p, m->col.p, cudaMemcpyDeviceToDevice);
+  return ilu_install_pattern(p, m->nblk, m->ndim, m->nnz, m->row_start.p, m->col.p, cudaMemcpyDeviceToDevice);
 }
 
 int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level) {
@@ -780,18 +983,30 @@ int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level) {
   if (fill_level == 0) return dfm2g_ilu_set_pattern0(p, m);
   std::vector<unsigned> rs, col;
   DFM2G_TRY(ilu_symbolic_k(m->nblk, m->h_row_start, m->h_col, fill_level, rs, col));
-  return ilu_install_pattern(p, m->nblk, col.size(), rs.data(), col.data(), cudaMemcpyHostToDevice);
+  return ilu_install_pattern(p, m->nblk, m->ndim, col.size(), rs.data(), col.data(), cudaMemcpyHostToDevice);
 }
 
 int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m) {
   DFM2G_TRY(check_ilu(p, true, false));
   if (!m || !m->has_pattern || m->nblk != p->nblk) return fail(DFM2G_ERR_ARG, "copy_value: matrix size mismatch");
-  DFM2G_CUDA(cudaMemsetAsync(p->vcrs.p, 0, sizeof(double) * p->nnz * 9, stream()));
+  if (m->ndim != p->ndim)
+    return fail(DFM2G_ERR_ARG, "copy_value: matrix blocks are %ux%u, the pattern's %ux%u", m->ndim, m->ndim, p->ndim,
+                p->ndim);
+  const size_t bb = (size_t)p->ndim * p->ndim;
+  DFM2G_CUDA(cudaMemsetAsync(p->vcrs.p, 0, sizeof(double) * p->nnz * bb, stream()));
   if (p->nblk) {
-    k_ilu_copy<<<blocks_for((size_t)p->nblk * 32, 256, ctx().num_sms * 16), 256, 0, stream()>>>(
-        p->nblk, m->row_start.p, m->col.p, m->vcrs.p, p->row_start.p, p->col.p, p->vcrs.p);
+    const unsigned blocks = blocks_for((size_t)p->nblk * 32, 256, ctx().num_sms * 16);
+    if (p->ndim == 3)
+      k_ilu_copy<9><<<blocks, 256, 0, stream()>>>(p->nblk, m->row_start.p, m->col.p, m->vcrs.p, p->row_start.p,
+                                                  p->col.p, p->vcrs.p);
+    else if (p->ndim == 2)
+      k_ilu_copy<4><<<blocks, 256, 0, stream()>>>(p->nblk, m->row_start.p, m->col.p, m->vcrs.p, p->row_start.p,
+                                                  p->col.p, p->vcrs.p);
+    else
+      k_ilu_copy<1><<<blocks, 256, 0, stream()>>>(p->nblk, m->row_start.p, m->col.p, m->vcrs.p, p->row_start.p,
+                                                  p->col.p, p->vcrs.p);
     DFM2G_LAUNCH_CHECK();
-    DFM2G_CUDA(cudaMemcpyAsync(p->vdia.p, m->vdia.p, sizeof(double) * 9 * p->nblk, cudaMemcpyDeviceToDevice,
+    DFM2G_CUDA(cudaMemcpyAsync(p->vdia.p, m->vdia.p, sizeof(double) * bb * p->nblk, cudaMemcpyDeviceToDevice,
                                stream()));
   }
   p->has_factor = false;
@@ -805,8 +1020,16 @@ int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular) {
   const std::vector<unsigned> &ls = p->h_lstart_f;
   for (size_t l = 0; l + 1 < ls.size(); ++l) {
     const unsigned nrows = ls[l + 1] - ls[l];
-    k_ilu_factor_level<<<blocks_for((size_t)nrows * 32, 256), 256, 0, stream()>>>(
-        p->order_f.p + ls[l], nrows, p->row_start.p, p->col.p, p->dia_ind.p, p->vcrs.p, p->vdia.p, p->nsing.p);
+    const unsigned blocks = blocks_for((size_t)nrows * 32, 256);
+    if (p->ndim == 3)
+      k_ilu_factor_level<<<blocks, 256, 0, stream()>>>(p->order_f.p + ls[l], nrows, p->row_start.p, p->col.p,
+                                                       p->dia_ind.p, p->vcrs.p, p->vdia.p, p->nsing.p);
+    else if (p->ndim == 2)
+      k_ilu_factor_level_nd<2><<<blocks, 256, 0, stream()>>>(p->order_f.p + ls[l], nrows, p->row_start.p, p->col.p,
+                                                             p->dia_ind.p, p->vcrs.p, p->vdia.p, p->nsing.p);
+    else
+      k_ilu_factor_level_nd<1><<<blocks, 256, 0, stream()>>>(p->order_f.p + ls[l], nrows, p->row_start.p, p->col.p,
+                                                             p->dia_ind.p, p->vcrs.p, p->vdia.p, p->nsing.p);
   }
   DFM2G_LAUNCH_CHECK();
   int ns = 0;
@@ -824,7 +1047,7 @@ static int precond_host(dfm2g_ilu p, int prec, void *vec, int mem, int which /*1
   DFM2G_TRY(check_ilu(p, true, true));
   if (!vec) return fail(DFM2G_ERR_ARG, "null vector");
   if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "prec must be F64 or F32");
-  const size_t n = (size_t)p->nblk * 3;
+  const size_t n = (size_t)p->nblk * p->ndim;
   const size_t es = prec == DFM2G_F64 ? 8 : 4;
   void *a = prec == DFM2G_F64 ? (void *)p->tmp64a.p : (void *)p->tmp32a.p;
   void *b = prec == DFM2G_F64 ? (void *)p->tmp64b.p : (void *)p->tmp32b.p;
@@ -885,12 +1108,12 @@ int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec) {
   DFM2G_TRY(check_ilu(p, true, true));
   if (!vec) return fail(DFM2G_ERR_ARG, "solve_precond_noalloc: null vector");
   if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "prec must be F64 or F32");
-  const size_t n = (size_t)p->nblk * 3;
+  const size_t n = (size_t)p->nblk * p->ndim;
   if (n > kNoAllocMaxScalars)
     return fail(DFM2G_ERR_ARG,
-                "solve_precond_noalloc: %zu unknowns exceed the fixed scratch of %zu (at most %zu 3x3 block rows); "
+                "solve_precond_noalloc: %zu unknowns exceed the fixed scratch of %zu (at most %zu %ux%u block rows); "
                 "use dfm2g_ilu_solve_precond for larger systems",
-                n, kNoAllocMaxScalars, kNoAllocMaxScalars / 3);
+                n, kNoAllocMaxScalars, kNoAllocMaxScalars / p->ndim, p->ndim, p->ndim);
   if (prec == DFM2G_F32 && !p->f32_valid)
     return fail(DFM2G_ERR_STATE,
                 "solve_precond_noalloc: no FP32 factors yet (creating them allocates); call "
@@ -916,6 +1139,8 @@ int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
       mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
+  if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS)
+    return fail(DFM2G_ERR_UNSUPPORTED, "sweep mode %d needs 3x3 blocks (the pattern has ndim %u)", mode, p->ndim);
   if (mode == DFM2G_SWEEP_PARTS && !p->parts_ok)
     return fail(DFM2G_ERR_UNSUPPORTED, "row-range partition unavailable for this pattern");
   if (mode == DFM2G_SWEEP_GROUPS && !(p->gs_f.ok && p->gs_b.ok))
@@ -959,8 +1184,9 @@ int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_ind) {
 int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem) {
   DFM2G_TRY(check_ilu(p, true, false));
   const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  if (vcrs && p->nnz) DFM2G_CUDA(cudaMemcpyAsync(vcrs, p->vcrs.p, sizeof(double) * 9 * p->nnz, k, stream()));
-  if (vdia && p->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, p->vdia.p, sizeof(double) * 9 * p->nblk, k, stream()));
+  const size_t bb = (size_t)p->ndim * p->ndim;
+  if (vcrs && p->nnz) DFM2G_CUDA(cudaMemcpyAsync(vcrs, p->vcrs.p, sizeof(double) * bb * p->nnz, k, stream()));
+  if (vdia && p->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, p->vdia.p, sizeof(double) * bb * p->nblk, k, stream()));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
 }

@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "nd.cuh"
 #include "rowkern.cuh"
 #include "spmv_tma.cuh"
 
@@ -103,10 +104,40 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_spmv_pAp_tma(IterState *st, 
   }
 }
 
+// The same for 1x1 and 2x2 blocks (nd.cuh).
+template <typename T, int B>
+__global__ void __launch_bounds__(kThreads) k_spmv_pAp_nd(IterState *st, unsigned nblk,
+                                                          const unsigned *__restrict__ row_start,
+                                                          const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                                          const T *__restrict__ vdia, const T *__restrict__ p,
+                                                          T *__restrict__ Ap, double *partials) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  const unsigned lane = threadIdx.x & 31;
+  double dot = 0.0;
+  nd_spmv_rows<T, B>(nblk, row_start, col, vcrs, vdia, p, [&](unsigned row, const T s[B]) {
+    if (lane < (unsigned)B) {
+      const T v = nd_pick<T, B>(s, lane);
+      Ap[(size_t)row * B + lane] = v;
+      dot += (double)(v * p[(size_t)row * B + lane]);
+    }
+  });
+  double total;
+  if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
+    st->alpha = st->rPr / total;
+  }
+}
+
 template <typename T>
 static int launch_spmv_pAp(dfm2g_bsr_s *m, IterState *st, const T *vcrs, const T *vdia, const T *pv, T *Ap,
                            double *partials, unsigned spmv_blocks) {
-  if (m->tiles_ok) {
+  if (m->ndim == 1) {
+    k_spmv_pAp_nd<T, 1><<<spmv_blocks, kThreads, 0, stream()>>>(st, m->nblk, m->row_start.p, m->col.p, vcrs, vdia, pv,
+                                                               Ap, partials);
+  } else if (m->ndim == 2) {
+    k_spmv_pAp_nd<T, 2><<<spmv_blocks, kThreads, 0, stream()>>>(st, m->nblk, m->row_start.p, m->col.p, vcrs, vdia, pv,
+                                                               Ap, partials);
+  } else if (m->tiles_ok) {
     static int attr_device = -1;  // per instantiation, once per device
     if (attr_device != ctx().device) {
       DFM2G_CUDA(cudaFuncSetAttribute(k_spmv_pAp_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -136,6 +167,8 @@ __global__ void k_flush_x(const IterState *st, size_t n, double *__restrict__ x6
 
 // Reliable update, part 2: r64 = b - K64 x64 in FP64, r32 = (float) r64, and
 // |r64| decides convergence (|r64| < tol |b|) or the next refresh threshold.
+// B = 3 runs the 3x3 row product of rowkern.cuh, B = 1, 2 that of nd.cuh.
+template <int B>
 __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsigned nblk,
                                                             const unsigned *__restrict__ row_start,
                                                             const unsigned *__restrict__ col,
@@ -150,16 +183,20 @@ __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsig
   const unsigned lane = threadIdx.x & 31;
   const double sc = st->scale_next, inv_old = 1.0 / st->scale;
   double rr = 0.0, dd = 0.0;
-  spmv_rows(nblk, row_start, col, vcrs, vdia, x64, [&](unsigned row, const double s[3]) {
-    if (lane < 3) {
-      const size_t k = (size_t)row * 3 + lane;
-      const double r = b[k] - pick3(s, lane);
+  auto row_done = [&](unsigned row, const double s[B]) {
+    if (lane < (unsigned)B) {
+      const size_t k = (size_t)row * B + lane;
+      const double r = b[k] - (B == 3 ? pick3(s, lane) : nd_pick<double, B>(s, lane));
       const double gap = r - (double)r32[k] * inv_old;  // true minus recursive residual
       r32[k] = (float)(r * sc);
       rr += r * r;
       dd += gap * gap;
     }
-  });
+  };
+  if constexpr (B == 3)
+    spmv_rows(nblk, row_start, col, vcrs, vdia, x64, row_done);
+  else
+    nd_spmv_rows<double, B>(nblk, row_start, col, vcrs, vdia, x64, row_done);
   // |true - recursive|^2: block sums go to partials[gridDim.x + block] (written
   // before grid_sum_last's fence), the last block adds them in block order
   dd = block_sum(dd, sh2);
@@ -440,7 +477,7 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
                     const Refine &rf = Refine()) {
   const int prec = sizeof(T) == 8 ? DFM2G_F64 : DFM2G_F32;
   const unsigned nblk = m->nblk;
-  const size_t n = (size_t)nblk * 3;
+  const size_t n = (size_t)nblk * m->ndim;
   const T *vcrs = sizeof(T) == 8 ? (const T *)m->vcrs.p : (const T *)m->vcrs32.p;
   const T *vdia = sizeof(T) == 8 ? (const T *)m->vdia.p : (const T *)m->vdia32.p;
   if (mode == 2 && sizeof(T) != 4) return fail(DFM2G_ERR_ARG, "reliable-update PCG runs in FP32");
@@ -491,9 +528,18 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
         if (mode == 2) {
           ProfScope ps(DFM2G_PROF_OUTER, 2);
           k_flush_x<<<vec_blocks, kThreads, 0, stream()>>>(st, n, rf.x64, (float *)x);
-          k_true_residual<<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p, m->vcrs.p,
-                                                                  m->vdia.p, rf.x64, rf.b64, (float *)r,
-                                                                  g_ws.partials.p);
+          if (m->ndim == 3)
+            k_true_residual<3><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p,
+                                                                       m->vcrs.p, m->vdia.p, rf.x64, rf.b64,
+                                                                       (float *)r, g_ws.partials.p);
+          else if (m->ndim == 2)
+            k_true_residual<2><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p,
+                                                                       m->vcrs.p, m->vdia.p, rf.x64, rf.b64,
+                                                                       (float *)r, g_ws.partials.p);
+          else
+            k_true_residual<1><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p,
+                                                                       m->vcrs.p, m->vdia.p, rf.x64, rf.b64,
+                                                                       (float *)r, g_ws.partials.p);
         }
       }
       if (mode != 1) {
@@ -544,11 +590,14 @@ static int check_pair(dfm2g_bsr m, dfm2g_ilu p) {
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "matrix has no pattern");
   if (p && (!p->has_factor || p->nblk != m->nblk))
     return fail(DFM2G_ERR_STATE, "preconditioner not decomposed for this matrix");
+  if (p && p->ndim != m->ndim)
+    return fail(DFM2G_ERR_ARG, "preconditioner blocks are %ux%u, the matrix's %ux%u", p->ndim, p->ndim, m->ndim,
+                m->ndim);
   return DFM2G_OK;
 }
 
 static int true_residual(dfm2g_bsr_s *m, const double *b, const double *x, double *res, double *rel) {
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   DFM2G_CUDA(cudaMemcpyAsync(res, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, stream()));
   DFM2G_TRY(bsr_spmv(m, DFM2G_F64, res, -1.0, x, 1.0));
   double rr = 0, bb = 0;
@@ -569,7 +618,7 @@ int dfm2g_solve_pcg(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol, 
   DFM2G_TRY(check_pair(m, p));
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg: null preconditioner");
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_pcg: null vector");
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   DFM2G_TRY(ws_prepare(n, max_iter + 2, false));
   VecArg<double> ar, ax;
   DFM2G_TRY(ar.in(r, n, mem, true));
@@ -606,7 +655,7 @@ int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_i
                    unsigned *n_hist, int mem, dfm2g_solve_stats *stats) {
   DFM2G_TRY(check_pair(m, nullptr));
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_cg: null vector");
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   DFM2G_TRY(ws_prepare(n, max_iter + 2, false));
   VecArg<double> ar, ax;
   DFM2G_TRY(ar.in(r, n, mem, true));
@@ -645,7 +694,7 @@ int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const double *b, do
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null preconditioner");
   if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null vector");
   if (!(delta > 0 && delta < 1)) return fail(DFM2G_ERR_ARG, "delta must be in (0,1)");
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   DFM2G_TRY(ws_prepare(n, max_iter + 4, true));
   DFM2G_TRY(bsr_ensure_f32(m));
   DFM2G_TRY(ilu_ensure_f32(p));
@@ -697,7 +746,7 @@ int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, 
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null preconditioner");
   if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null vector");
   if (!(inner_tol > 0 && inner_tol < 1)) return fail(DFM2G_ERR_ARG, "inner_tol must be in (0,1)");
-  const size_t n = (size_t)m->nblk * 3;
+  const size_t n = (size_t)m->nblk * m->ndim;
   DFM2G_TRY(ws_prepare(n, 4, true));
   DFM2G_TRY(bsr_ensure_f32(m));
   DFM2G_TRY(ilu_ensure_f32(p));

@@ -1,8 +1,13 @@
-"""Linear-tet elasticity on the device (assembly and the adjoint element term).
+"""Element assembly on the device: linear tets (elasticity with the adjoint
+element term, 3x3 blocks; scalar Poisson, 1x1 blocks) and 2-D linear
+triangles (scalar Poisson, 1x1 blocks; static linear solid, 2x2 blocks).
 
-TetMesh mirrors the per-element loop of MergeLinSys_SolidLinear_Static_MeshTet3D
-(include/delfem2/fem_solidlinear.h:192-237) with a per-tet Young's modulus;
-the assembly runs as colour-scheduled, atomic-free CUDA kernels.
+TetMesh mirrors the per-element loops of MergeLinSys_SolidLinear_Static_MeshTet3D
+(include/delfem2/fem_solidlinear.h:192-237, per-tet Young's modulus) and
+MergeLinSys_Poission_MeshTet3D (include/delfem2/fem_poisson.h:128-162);
+TriMesh2 those of MergeLinSys_Poission_MeshTri2D (fem_poisson.h:92-127) and
+MergeLinSys_SolidLinear_Static_MeshTri2D (fem_solidlinear.h:155-187). The
+assembly runs as colour-scheduled, atomic-free CUDA kernels.
 """
 from __future__ import annotations
 
@@ -48,6 +53,13 @@ class TetMesh:
         N.call("dfm2g_tetmesh_assemble_linear", self._h, self.mat._h, py, float(nu), float(rho), g3, pd, pb,
                _same_mem(my, mb, md))
 
+    def assemble_poisson(self, alpha: float, source: float, b, val=None):
+        """Scalar K += K_e, b += source vol/4 - K_e val_e (b in place; the matrix has 1x1 blocks)."""
+        pb, mb, kb = _vec(b, np.float64, True)
+        pv, mv, kv = _vec(val, np.float64, False) if val is not None else (None, None, None)
+        N.call("dfm2g_tetmesh_assemble_poisson", self._h, self.mat._h, float(alpha), float(source), pv, pb,
+               _same_mem(mb, mv))
+
     def dLdE(self, nu: float, u, lam, out):
         """out[e] = -lam_e^T (dK_e/dE_e) u_e."""
         pu, mu, ku = _vec(u, np.float64, False)
@@ -59,6 +71,43 @@ class TetMesh:
         try:
             if self._h is not None:
                 N.load().dfm2g_tetmesh_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class TriMesh2:
+    """Element->slot map and colouring of a 2-D triangle mesh against the pattern of a 1x1- or 2x2-block matrix."""
+
+    def __init__(self, mat: CMatrixSparse, xy, tri):
+        self.xy = np.ascontiguousarray(xy, np.float64)
+        self.tri = np.ascontiguousarray(tri, np.uint32)
+        self.np = self.xy.size // 2
+        self.ntri = self.tri.size // 3
+        h = C.c_void_p()
+        N.call("dfm2g_trimesh2_create", C.byref(h), mat._h, self.xy.ctypes.data, self.np, self.tri.ctypes.data,
+               self.ntri)
+        self._h = h
+        self.mat = mat
+
+    def assemble_poisson(self, alpha: float, source: float, b, val=None):
+        """Scalar K += K_e, b += source area/3 - K_e val_e (1x1 blocks)."""
+        pb, mb, kb = _vec(b, np.float64, True)
+        pv, mv, kv = _vec(val, np.float64, False) if val is not None else (None, None, None)
+        N.call("dfm2g_trimesh2_assemble_poisson", self._h, self.mat._h, float(alpha), float(source), pv, pb,
+               _same_mem(mb, mv))
+
+    def assemble_solid_linear(self, myu: float, lam: float, rho: float, g, b, disp=None):
+        """K += K_e, b += area rho g/3 - K_e u_e (2x2 blocks; g = (gx, gy))."""
+        pb, mb, kb = _vec(b, np.float64, True)
+        pd, md, kd = _vec(disp, np.float64, False) if disp is not None else (None, None, None)
+        N.call("dfm2g_trimesh2_assemble_solid_linear", self._h, self.mat._h, float(myu), float(lam), float(rho),
+               float(g[0]), float(g[1]), pd, pb, _same_mem(mb, md))
+
+    def __del__(self):
+        try:
+            if self._h is not None:
+                N.load().dfm2g_trimesh2_destroy(self._h)
                 self._h = None
         except Exception:
             pass

@@ -84,7 +84,7 @@ def JArray_PSuP_MeshElem(elem, nnoel: int, np_: int):
 
 # ---------------------------------------------------------------------------
 class CMatrixSparse:
-    """Device-resident CMatrixSparse<double> with 3x3 blocks."""
+    """Device-resident CMatrixSparse<double> with ndim x ndim blocks (ndim 1, 2 or 3)."""
 
     def __init__(self):
         self._h = None
@@ -123,8 +123,9 @@ class CMatrixSparse:
         N.call("dfm2g_bsr_set_values", self._h, pc, pd, _same_mem(mc if pc else None, md if pd else None))
 
     def get_values(self):
-        vc = np.zeros(self.nnz * 9, np.float64)
-        vd = np.zeros(self.nrowblk * 9, np.float64)
+        bb = self.ndim * self.ndim
+        vc = np.zeros(self.nnz * bb, np.float64)
+        vd = np.zeros(self.nrowblk * bb, np.float64)
         N.call("dfm2g_bsr_get_values", self._h, vc.ctypes.data if vc.size else None, vd.ctypes.data, N.MEM_HOST)
         return vc, vd
 
@@ -167,14 +168,14 @@ class CMatrixSparse:
 
 
 def Merge(mat: CMatrixSparse, elem, emat):
-    """Merge<nno,nno,3,3,double> for a batch: elem (nelem, nno), emat (nelem, nno, nno, 3, 3).
+    """Merge<nno,nno,ndim,ndim,double> for a batch: elem (nelem, nno), emat (nelem, nno, nno, ndim, ndim).
 
     Raises Dfm2gError(ERR_MISSING_SLOT) where the reference returns false."""
     elem = np.ascontiguousarray(elem, np.uint32)
     if elem.ndim == 1:
         elem = elem.reshape(1, -1)
     nelem, nno = elem.shape
-    em = np.ascontiguousarray(emat, np.float64).reshape(nelem, nno, nno, 3, 3)
+    em = np.ascontiguousarray(emat, np.float64).reshape(nelem, nno, nno, mat.ndim, mat.ndim)
     N.call("dfm2g_bsr_merge", mat._h, nelem, nno, elem.ctypes.data, em.ctypes.data, N.MEM_HOST)
 
 
@@ -189,17 +190,19 @@ def setRHS_Zero(b, bc, iflag_nonzero: int = 0):
 
 # ---------------------------------------------------------------------------
 class CPreconditionerILU:
-    """Device-resident CPreconditionerILU<double> (ILU(0) or ILU(k), 3x3 blocks)."""
+    """Device-resident CPreconditionerILU<double> (ILU(0) or ILU(k); the matrix's block size)."""
 
     def __init__(self):
         h = C.c_void_p()
         N.call("dfm2g_ilu_create", C.byref(h))
         self._h = h
         self.nblk = 0
+        self.ndim = 0
 
     def SetPattern0(self, mat: CMatrixSparse):
         N.call("dfm2g_ilu_set_pattern0", self._h, mat._h)
         self.nblk = mat.nrowblk
+        self.ndim = mat.ndim
         self._nnz = mat.nnz
 
     def Initialize_ILUk(self, mat: CMatrixSparse, fill_level: int):
@@ -207,6 +210,7 @@ class CPreconditionerILU:
         SetPattern0, -1 keeps every fill."""
         N.call("dfm2g_ilu_set_pattern_k", self._h, mat._h, int(fill_level))
         self.nblk = mat.nrowblk
+        self.ndim = mat.ndim
         nnz = C.c_size_t(0)
         N.call("dfm2g_ilu_info", self._h, None, C.byref(nnz))
         self._nnz = nnz.value
@@ -256,10 +260,11 @@ class CPreconditionerILU:
         return col[: self._nnz], dia[: self.nblk]
 
     def values(self):
-        vc = np.zeros(max(self._nnz * 9, 1), np.float64)
-        vd = np.zeros(max(self.nblk * 9, 1), np.float64)
+        bb = self.ndim * self.ndim
+        vc = np.zeros(max(self._nnz * bb, 1), np.float64)
+        vd = np.zeros(max(self.nblk * bb, 1), np.float64)
         N.call("dfm2g_ilu_get_values", self._h, vc.ctypes.data, vd.ctypes.data, N.MEM_HOST)
-        return vc[: self._nnz * 9], vd[: self.nblk * 9]
+        return vc[: self._nnz * bb], vd[: self.nblk * bb]
 
     def levels(self, backward: bool = False):
         n = self.nblk

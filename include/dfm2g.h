@@ -1,7 +1,8 @@
 /*
  * dfm2g.h — C ABI of the GB300-native (sm_103a, one GPU) drop-in for DelFEM2's
- * implicit-FEM linear-solve path: 3x3 block-CSR assembly (CMatrixSparse /
- * Merge), ILU(0) (CPreconditionerILU) and preconditioned CG (Solve_PCG).
+ * implicit-FEM linear-solve path: block-CSR assembly (CMatrixSparse /
+ * Merge), ILU(k) (CPreconditionerILU) and preconditioned Krylov solvers
+ * (Solve_PCG, Solve_PBiCGStab).
  *
  * Conventions
  *  - Every entry point returns an int status (DFM2G_OK == 0). A failing call
@@ -10,14 +11,18 @@
  *    CMatrixSparse, `row_start` is what the reference calls col_ind_ (row
  *    offsets, nblk+1 entries) and `col` is its row_ptr_ (column id of each
  *    off-diagonal block). Diagonal blocks are stored separately. Blocks are
- *    row-major 3x3.
+ *    row-major ndim x ndim, vectors ndim entries per block row.
  *  - Vector arguments live in host or device memory as the per-call `mem`
  *    flag says (DFM2G_MEM_HOST / DFM2G_MEM_DEVICE). Device pointers must be on
  *    the library's current device; host pointers are copied in/out.
  *  - All work is queued on the library stream (dfm2g_set_stream); calls that
  *    return host data synchronise it.
- *  - Only 3x3 blocks (ndim == 3) are supported; other block sizes return
- *    DFM2G_ERR_UNSUPPORTED.
+ *  - Block sizes 1x1, 2x2 and 3x3 (ndim 1, 2, 3). The 3x3 path is the tuned
+ *    one (TMA-staged SpMV, every sweep schedule); 1x1 and 2x2 matrices run
+ *    warp-per-row kernels with the sync-free and level sweep schedules.
+ *    Entry points written for one block size (the linear-tet elasticity and
+ *    cloth assemblers: 3x3; Poisson: 1x1; the 2-D solid: 2x2) return
+ *    DFM2G_ERR_UNSUPPORTED for another.
  */
 #ifndef DFM2G_H
 #define DFM2G_H
@@ -66,9 +71,10 @@ enum dfm2g_sweep {
                                in shared memory)                            */
 };
 
-typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>, 3x3  */
+typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>       */
 typedef struct dfm2g_ilu_s *dfm2g_ilu;       /* CPreconditionerILU<double>  */
 typedef struct dfm2g_tetmesh_s *dfm2g_tetmesh; /* linear-tet assembler      */
+typedef struct dfm2g_trimesh2_s *dfm2g_trimesh2; /* 2-D linear-triangle assembler */
 
 /* Per-solve record filled by the solvers (any pointer may be NULL). */
 typedef struct dfm2g_solve_stats {
@@ -103,8 +109,9 @@ DFM2G_API int dfm2g_psup_fill(const unsigned *elem, size_t nelem, unsigned nnoel
                               const unsigned *psup_ind, unsigned *psup);
 
 /* ---- CMatrixSparse (include/delfem2/ls_block_sparse.h:24-204) ------------- */
-/* Initialize(nblk, ndim, is_dia=true), ls_block_sparse.h:45-55. */
+/* Initialize(nblk, ndim, is_dia=true), ls_block_sparse.h:45-55; ndim 1, 2 or 3. */
 DFM2G_API int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim);
+DFM2G_API int dfm2g_bsr_ndim(dfm2g_bsr m, unsigned *ndim);
 DFM2G_API int dfm2g_bsr_destroy(dfm2g_bsr m);
 /* SetPattern(colind, ncolind, rowptr, nrowptr), ls_block_sparse.h:72-85.
  * Host arrays. Values become zero. */
@@ -113,26 +120,30 @@ DFM2G_API int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size
 DFM2G_API int dfm2g_bsr_info(dfm2g_bsr m, unsigned *nblk, size_t *nnz);
 /* setZero, ls_block_sparse.h:92-105. */
 DFM2G_API int dfm2g_bsr_set_zero(dfm2g_bsr m);
-/* Direct access to val_crs_ (9*nnz) and val_dia_ (9*nblk); either may be NULL. */
+/* Direct access to val_crs_ (ndim^2*nnz) and val_dia_ (ndim^2*nblk); either may be NULL. */
 DFM2G_API int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, int mem);
 DFM2G_API int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem);
 /* SetFixedBC = SetFixedBC_Dia(1)+Row+Col, ls_block_sparse.h:147-151,
- * ls_block_sparse.cpp:397-472. bc: 3*nblk ints, nonzero = fixed. */
+ * ls_block_sparse.cpp:397-472. bc: ndim*nblk ints, nonzero = fixed. */
 DFM2G_API int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem);
 /* AddDia(eps), ls_block_sparse.h:153-164. */
 DFM2G_API int dfm2g_bsr_add_dia(dfm2g_bsr m, double eps);
-/* MatVec: y = alpha*K*x + beta*y, ls_block_sparse.cpp:215-273 (y is scaled by
- * beta first, so a NaN in y survives beta == 0). prec DFM2G_F32 uses the FP32
+/* MatVec: y = alpha*K*x + beta*y, ls_block_sparse.cpp:213-273 (y is scaled by
+ * beta first, so a NaN in y survives beta == 0; the 1x1 / 2x2 / 3x3 loops of
+ * 59-133). prec DFM2G_F32 uses the FP32
  * mirror of the values (refreshed by dfm2g_bsr_update_f32) and float vectors. */
 DFM2G_API int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x,
                                double beta, int mem);
 /* Refresh the FP32 mirror of the values from the FP64 values. */
 DFM2G_API int dfm2g_bsr_update_f32(dfm2g_bsr m);
-/* Merge<nno,nno,3,3,double> for a batch of elements, ls_block_sparse.h:260-310:
- * elem: nelem*nnoel node ids; emat: nelem*(nnoel*nnoel*9) row-major
- * [irow][jcol][3][3]. The batch is colour-scheduled (no two elements of one
- * colour share a node), so the scatter is atomic-free and deterministic.
- * Returns DFM2G_ERR_MISSING_SLOT (and adds nothing) if a block is absent. */
+/* Merge / Mearge for a batch of elements, ls_block_sparse.h:209-358:
+ * elem: nelem*nnoel node ids; emat: nelem*(nnoel*nnoel*ndim*ndim) row-major
+ * [irow][jcol][ndim][ndim]. As in the reference, a pair (irow, jcol) whose
+ * nodes are the same block adds the [irow][irow] block to the diagonal (this
+ * differs from [irow][jcol] only for an element that repeats a node). The
+ * batch is colour-scheduled (no two elements of one colour share a node), so
+ * the scatter is atomic-free and deterministic. Returns
+ * DFM2G_ERR_MISSING_SLOT (and adds nothing) if a block is absent. */
 DFM2G_API int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned *elem,
                               const double *emat, int mem);
 
@@ -153,13 +164,15 @@ DFM2G_API int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m);
 DFM2G_API int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level);
 /* CopyValue, ls_ilu_block_sparse.cpp:1009-1047. */
 DFM2G_API int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m);
-/* Decompose (3x3 branch), ls_ilu_block_sparse.cpp:152-160,286-356, level-
- * scheduled on the device in FP64; also refreshes the FP32 copy of the factors.
+/* Decompose, ls_ilu_block_sparse.cpp:152-356 (1x1, 2x2 and 3x3 branches),
+ * level-scheduled on the device in FP64 (1x1 and 2x2 in the reference's own
+ * rounding, so the factors equal the reference's); the FP32 copy of the factors
+ * is refreshed when an FP32 solve first needs it.
  * More than 10 pivots with |det| <= 1e-30 -> DFM2G_ERR_SINGULAR_PIVOT.
  * *n_singular (may be NULL) receives the count of such pivots. */
 DFM2G_API int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular);
 /* ForwardSubstitution / BackwardSubstitution / SolvePrecond (in place),
- * ls_ilu_block_sparse.cpp:544-573, 721-749, ls_ilu_block_sparse.h:38-41. */
+ * ls_ilu_block_sparse.cpp:500-573, 678-749, ls_ilu_block_sparse.h:38-41. */
 DFM2G_API int dfm2g_ilu_forward(dfm2g_ilu p, int prec, void *vec, int mem);
 DFM2G_API int dfm2g_ilu_backward(dfm2g_ilu p, int prec, void *vec, int mem);
 DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem);
@@ -170,11 +183,12 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * `vec` must be in device memory (in/out). The intermediate vector between
  * the two sweeps lives in one fixed array inside the library (8 MiB), which
  * every GPU that loads the library keeps until the process exits; so
- * 3*nblk may not exceed 1,048,576 (DFM2G_ERR_ARG otherwise). The first call on
+ * ndim*nblk may not exceed 1,048,576 (DFM2G_ERR_ARG otherwise). The first call on
  * a device looks up that array's device address. All calls share the array:
  * calls that overlap on the GPU (other streams, other threads) race. FP32 needs
  * FP32 factors made earlier by a DFM2G_F32 dfm2g_ilu_solve_precond call. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
+/* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE and DFM2G_SWEEP_LEVELS only. */
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
 /* Current schedule (set_pattern0 picks DFM2G_SWEEP_GROUPS when it fits). */
 DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
@@ -253,6 +267,31 @@ DFM2G_API int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const 
  * counterpart; K_e is linear in E). young is unused except for shape checks. */
 DFM2G_API int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu,
                                  const double *u, const double *lam, double *dLdE, int mem);
+/* Scalar Poisson (adds; the matrix has 1x1 blocks): the loop of
+ * MergeLinSys_Poission_MeshTet3D, include/delfem2/fem_poisson.h:128-162, with
+ * EMat_Poisson_Tet3D (fem_poisson.cpp:163-194): K_e[a][b] = alpha vol
+ * (dN_a . dN_b), b += source vol/4 - K_e val_e per node. val: np nodal values
+ * (the fixed values lifted into b), or NULL for zero. */
+DFM2G_API int dfm2g_tetmesh_assemble_poisson(dfm2g_tetmesh t, dfm2g_bsr m, double alpha, double source,
+                                             const double *val, double *b, int mem);
+
+/* ---- 2-D linear triangles ---------------------------------------------------- */
+/* Builds, for mesh (xy: 2*np, tri: 3*ntri, host arrays) against the pattern of
+ * a 1x1- or 2x2-block matrix: the element->slot map and a greedy colouring. */
+DFM2G_API int dfm2g_trimesh2_create(dfm2g_trimesh2 *out, dfm2g_bsr m, const double *xy, size_t np,
+                                    const unsigned *tri, size_t ntri);
+DFM2G_API int dfm2g_trimesh2_destroy(dfm2g_trimesh2 t);
+/* Scalar Poisson (adds; 1x1 blocks): MergeLinSys_Poission_MeshTri2D,
+ * include/delfem2/fem_poisson.h:92-127, with EMat_Poisson_Tri2D
+ * (fem_poisson.cpp:15-46). val: np values or NULL. */
+DFM2G_API int dfm2g_trimesh2_assemble_poisson(dfm2g_trimesh2 t, dfm2g_bsr m, double alpha, double source,
+                                              const double *val, double *b, int mem);
+/* Static linear solid (adds; 2x2 blocks): MergeLinSys_SolidLinear_Static_MeshTri2D,
+ * include/delfem2/fem_solidlinear.h:155-187, with EMat_SolidStaticLinear_Tri2D
+ * (fem_solidlinear.cpp:89-124). disp: 2*np or NULL; b: 2*np. */
+DFM2G_API int dfm2g_trimesh2_assemble_solid_linear(dfm2g_trimesh2 t, dfm2g_bsr m, double myu, double lambda,
+                                                   double rho, double gx, double gy, const double *disp,
+                                                   double *b, int mem);
 
 /* ---- implicit cloth (include/delfem2/femcloth.h, cloth_internal.h) --------- */
 /* Triangle sheet with StVK CST membrane + quadratic bending over the quads of

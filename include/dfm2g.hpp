@@ -64,7 +64,7 @@ class CMatrixSparse<double> {
   }
   void SetFixedBC(const int *bc_flag) { check(dfm2g_bsr_set_fixed_bc(h_, bc_flag, DFM2G_MEM_HOST), "SetFixedBC"); }
   void AddDia(double eps) { check(dfm2g_bsr_add_dia(h_, eps), "AddDia"); }
-  // Batched Merge: nelem elements of nno nodes, emat row-major [e][irow][jcol][3][3].
+  // Batched Merge: nelem elements of nno nodes, emat row-major [e][irow][jcol][ndim][ndim].
   void MergeBatch(unsigned nelem, unsigned nno, const unsigned *elem, const double *emat) {
     check(dfm2g_bsr_merge(h_, nelem, nno, elem, emat, DFM2G_MEM_HOST), "Merge");
   }
@@ -76,17 +76,33 @@ class CMatrixSparse<double> {
   dfm2g_bsr h_ = nullptr;
 };
 
-// Merge<nrow,ncol,3,3,double> for one element (aIpRow == aIpCol, as every
-// FEM caller passes). One call is one device launch: callers merging many
-// elements should collect them and use CMatrixSparse::MergeBatch.
+// Merge<nrow,ncol,ndim,ndim,double> (ls_block_sparse.h:260-310) and the
+// scalar Merge<nrow,ncol,double> (313-358) for one element (aIpRow == aIpCol,
+// as every FEM caller passes). One call is one device launch: callers merging
+// many elements should collect them and use CMatrixSparse::MergeBatch.
 template <int nrow, int ncol, int ndimrow, int ndimcol, typename T>
 bool Merge(CMatrixSparse<T> &A, const unsigned int aIpRow[nrow], const unsigned int aIpCol[ncol],
            const T emat[nrow][ncol][ndimrow][ndimcol], std::vector<unsigned int> &merge_buffer) {
-  static_assert(nrow == ncol && ndimrow == 3 && ndimcol == 3, "3x3 blocks, square element matrices");
+  static_assert(nrow == ncol && ndimrow == ndimcol, "square element matrices of square blocks");
   (void)merge_buffer;
+  if (A.nrowdim_ != (unsigned)ndimrow) throw Error(DFM2G_ERR_ARG, "Merge: block size differs from the matrix's");
   for (int i = 0; i < nrow; ++i)
     if (aIpRow[i] != aIpCol[i]) throw Error(DFM2G_ERR_UNSUPPORTED, "Merge: aIpRow must equal aIpCol");
   const int s = dfm2g_bsr_merge(A.handle(), 1, nrow, aIpRow, &emat[0][0][0][0], DFM2G_MEM_HOST);
+  if (s == DFM2G_ERR_MISSING_SLOT) return false;
+  check(s, "Merge");
+  return true;
+}
+
+template <int nrow, int ncol, typename T>
+bool Merge(CMatrixSparse<T> &A, const unsigned int *aIpRow, const unsigned int *aIpCol, const T emat[nrow][ncol],
+           std::vector<unsigned int> &merge_buffer) {
+  static_assert(nrow == ncol, "square element matrices");
+  (void)merge_buffer;
+  if (A.nrowdim_ != 1) throw Error(DFM2G_ERR_ARG, "Merge: scalar element matrix on a block matrix");
+  for (int i = 0; i < nrow; ++i)
+    if (aIpRow[i] != aIpCol[i]) throw Error(DFM2G_ERR_UNSUPPORTED, "Merge: aIpRow must equal aIpCol");
+  const int s = dfm2g_bsr_merge(A.handle(), 1, nrow, aIpRow, &emat[0][0], DFM2G_MEM_HOST);
   if (s == DFM2G_ERR_MISSING_SLOT) return false;
   check(s, "Merge");
   return true;
