@@ -108,6 +108,11 @@ SIGNATURES = {
     "dfm2g_tetmesh_assemble_linear": [_vp, _vp, _vp, _d, _d, _vp, _vp, _vp, _i],
     "dfm2g_tetmesh_dLdE": [_vp, _vp, _d, _vp, _vp, _vp, _i],
     "dfm2g_tetmesh_assemble_poisson": [_vp, _vp, _d, _d, _vp, _vp, _i],
+    "dfm2g_tetmesh_assemble_beuler": [_vp, _vp, _d, _d, _d, _vp, _d, _vp, _vp, _vp, _vp, _i],
+    "dfm2g_tetmesh_assemble_newmark": [_vp, _vp, _d, _d, _d, _vp, _d, _d, _d, _vp, _vp, _vp, _vp, _i],
+    "dfm2g_hexmesh_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz],
+    "dfm2g_hexmesh_destroy": [_vp],
+    "dfm2g_hexmesh_assemble_linear": [_vp, _vp, _d, _d, _d, _vp, _vp, _vp, _i],
     "dfm2g_trimesh2_create": [C.POINTER(_vp), _vp, _vp, _sz, _vp, _sz],
     "dfm2g_trimesh2_destroy": [_vp],
     "dfm2g_trimesh2_assemble_poisson": [_vp, _vp, _d, _d, _vp, _vp, _i],

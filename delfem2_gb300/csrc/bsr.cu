@@ -21,17 +21,16 @@ int require_3x3(const dfm2g_bsr_s *m, const char *what) {
   return DFM2G_OK;
 }
 
-// y = alpha*K*x + beta*y for 1x1 and 2x2 blocks, one warp per block row.
+// y = alpha*K*x + beta*y for 1x1 and 2x2 blocks, eight lanes per block row.
 template <typename T, int B>
 __global__ void __launch_bounds__(256) k_nd_spmv(unsigned nblk, const unsigned *__restrict__ row_start,
                                                  const unsigned *__restrict__ col, const T *__restrict__ vcrs,
                                                  const T *__restrict__ vdia, T *__restrict__ y, T alpha,
                                                  const T *__restrict__ x, T beta) {
-  const unsigned lane = threadIdx.x & 31;
-  nd_spmv_rows<T, B>(nblk, row_start, col, vcrs, vdia, x, [&](unsigned row, const T s[B]) {
-    if (lane < (unsigned)B) {
-      T *py = y + (size_t)row * B + lane;
-      *py = beta * *py + alpha * nd_pick<T, B>(s, lane);
+  nd_spmv_rows<T, B>(nblk, row_start, col, vcrs, vdia, x, [&](unsigned row, const T s[B], unsigned sub) {
+    if (sub < (unsigned)B) {
+      T *py = y + (size_t)row * B + sub;
+      *py = beta * *py + alpha * nd_pick<T, B>(s, sub);
     }
   });
 }

@@ -642,6 +642,83 @@ __global__ void __launch_bounds__(256) k_sweep_level_nd(const uint4 *__restrict_
   if (lane < (unsigned)B) out[(size_t)m.x * B + lane] = nd_sweep_value<T, FWD, B>(m, lane, t, vdia);
 }
 
+// One row of the pipelined sync-free sweep, held in registers: lane l keeps
+// block s0 + l of the row's triangle (column and values), lanes < B the row's
+// right-hand side entry and, forward, row `lane` of D_i^-1. Blocks past the
+// first 32 of a long row are read when the row finishes.
+template <typename T, int B>
+struct NdSweepRow {
+  unsigned i, s0, s1, j;  // j = ~0u: no block for this lane
+  T a[B * B];
+  T in;
+  T d[B];
+};
+
+template <typename T, bool FWD, int B>
+__device__ __forceinline__ void nd_sweep_load(NdSweepRow<T, B> &R, unsigned lane, uint4 m,
+                                              const unsigned *__restrict__ col, const T *__restrict__ vcrs,
+                                              const T *__restrict__ vdia, const T *in) {
+  R.i = m.x;
+  R.s0 = m.y;
+  R.s1 = m.z;
+  const unsigned s = m.y + lane;
+  R.j = ~0u;
+  if (s < m.z) {
+    R.j = col[s];
+#pragma unroll
+    for (int q = 0; q < B * B; ++q) R.a[q] = vcrs[(size_t)s * (B * B) + q];
+  }
+  if (lane < (unsigned)B) {
+    R.in = in[(size_t)m.x * B + lane];
+    if constexpr (FWD) {
+#pragma unroll
+      for (int c = 0; c < B; ++c) R.d[c] = vdia[(size_t)m.x * (B * B) + lane * B + c];
+    }
+  }
+}
+
+template <typename T, bool FWD, int B>
+__device__ __forceinline__ void nd_sweep_finish(const NdSweepRow<T, B> &R, unsigned lane,
+                                                const unsigned *__restrict__ col, const T *__restrict__ vcrs, T *out,
+                                                int *err, unsigned long long timeout_ns) {
+  T acc[B];
+#pragma unroll
+  for (int r = 0; r < B; ++r) acc[r] = T(0);
+  if (R.j != ~0u) {
+    T xj[B];
+#pragma unroll
+    for (int c = 0; c < B; ++c) xj[c] = wait_value(out + (size_t)R.j * B + c, err, timeout_ns);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      T t = R.a[r * B] * xj[0];
+#pragma unroll
+      for (int c = 1; c < B; ++c) t += R.a[r * B + c] * xj[c];
+      acc[r] += t;
+    }
+  }
+  if (R.s1 > R.s0 + 32) nd_row_partial<T, B, true>(lane, R.s0 + 32, R.s1, col, vcrs, out, acc, err, timeout_ns);
+#pragma unroll
+  for (int r = 0; r < B; ++r) acc[r] = warp_sum(acc[r]);
+  if (lane < (unsigned)B) {
+    const T t = R.in - nd_pick<T, B>(acc, lane);  // this lane's entry of in_i - sum
+    T z;
+    if constexpr (FWD) {
+      // z = row `lane` of D_i^-1 times (in_i - sum): gather the other entries from lanes 0..B-1
+      z = T(0);
+#pragma unroll
+      for (int c = 0; c < B; ++c) z += R.d[c] * __shfl_sync((1u << B) - 1u, t, c);
+    } else {
+      z = t;
+    }
+    st_relaxed(out + (size_t)R.i * B + lane, z);
+  }
+}
+
+// Sync-free sweep for 1x1 and 2x2 blocks: the co-resident grid of
+// k_sweep_syncfree, warp w taking positions w, w + W, ... of the level order.
+// Pipelined: the next position's row is loaded before the current row waits
+// for its dependencies, and the metadata of the one after that before the
+// current row is finished.
 template <typename T, bool FWD, int B>
 __global__ void __launch_bounds__(256) k_sweep_syncfree_nd(unsigned n, const uint4 *__restrict__ meta,
                                                            const unsigned *__restrict__ col,
@@ -651,16 +728,21 @@ __global__ void __launch_bounds__(256) k_sweep_syncfree_nd(unsigned n, const uin
   if (skip && *skip) return;
   const unsigned lane = threadIdx.x & 31;
   const unsigned nwarp = (gridDim.x * blockDim.x) >> 5;
-  for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n; q += nwarp) {
-    const uint4 m = meta[q];
-    T acc[B];
-    nd_row_sum<T, B, true>(lane, m.y, m.z, col, vcrs, out, acc, err, timeout_ns);
-    if (lane < (unsigned)B) {
-      T t[B];
-#pragma unroll
-      for (int r = 0; r < B; ++r) t[r] = in[(size_t)m.x * B + r] - acc[r];
-      st_relaxed(out + (size_t)m.x * B + lane, nd_sweep_value<T, FWD, B>(m, lane, t, vdia));
-    }
+  unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= n) return;
+  NdSweepRow<T, B> cur, nxt;
+  nd_sweep_load<T, FWD, B>(cur, lane, meta[q], col, vcrs, vdia, in);
+  uint4 m1 = (q + nwarp < n) ? meta[q + nwarp] : make_uint4(0u, 0u, 0u, 0u);
+  for (;;) {
+    const unsigned q1 = q + nwarp;
+    if (q1 < n) nd_sweep_load<T, FWD, B>(nxt, lane, m1, col, vcrs, vdia, in);
+    const unsigned q2 = q1 + nwarp;
+    const uint4 m2 = (q2 < n) ? meta[q2] : make_uint4(0u, 0u, 0u, 0u);
+    nd_sweep_finish<T, FWD, B>(cur, lane, col, vcrs, out, err, timeout_ns);
+    if (q1 >= n) break;
+    q = q1;
+    cur = nxt;
+    m1 = m2;
   }
 }
 

@@ -113,13 +113,12 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pAp_nd(IterState *st, unsigne
                                                           T *__restrict__ Ap, double *partials) {
   __shared__ double sh[32];
   if (st->done) return;
-  const unsigned lane = threadIdx.x & 31;
   double dot = 0.0;
-  nd_spmv_rows<T, B>(nblk, row_start, col, vcrs, vdia, p, [&](unsigned row, const T s[B]) {
-    if (lane < (unsigned)B) {
-      const T v = nd_pick<T, B>(s, lane);
-      Ap[(size_t)row * B + lane] = v;
-      dot += (double)(v * p[(size_t)row * B + lane]);
+  nd_spmv_rows<T, B>(nblk, row_start, col, vcrs, vdia, p, [&](unsigned row, const T s[B], unsigned sub) {
+    if (sub < (unsigned)B) {
+      const T v = nd_pick<T, B>(s, sub);
+      Ap[(size_t)row * B + sub] = v;
+      dot += (double)(v * p[(size_t)row * B + sub]);
     }
   });
   double total;
@@ -183,10 +182,11 @@ __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsig
   const unsigned lane = threadIdx.x & 31;
   const double sc = st->scale_next, inv_old = 1.0 / st->scale;
   double rr = 0.0, dd = 0.0;
-  auto row_done = [&](unsigned row, const double s[B]) {
-    if (lane < (unsigned)B) {
-      const size_t k = (size_t)row * B + lane;
-      const double r = b[k] - (B == 3 ? pick3(s, lane) : nd_pick<double, B>(s, lane));
+  // sub: the lane's index in the row's lanes (the warp lane for 3x3 rows)
+  auto row_done = [&](unsigned row, const double s[B], unsigned sub) {
+    if (sub < (unsigned)B) {
+      const size_t k = (size_t)row * B + sub;
+      const double r = b[k] - (B == 3 ? pick3(s, sub) : nd_pick<double, B>(s, sub));
       const double gap = r - (double)r32[k] * inv_old;  // true minus recursive residual
       r32[k] = (float)(r * sc);
       rr += r * r;
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsig
     }
   };
   if constexpr (B == 3)
-    spmv_rows(nblk, row_start, col, vcrs, vdia, x64, row_done);
+    spmv_rows(nblk, row_start, col, vcrs, vdia, x64, [&](unsigned row, const double s[3]) { row_done(row, s, lane); });
   else
     nd_spmv_rows<double, B>(nblk, row_start, col, vcrs, vdia, x64, row_done);
   // |true - recursive|^2: block sums go to partials[gridDim.x + block] (written

@@ -75,6 +75,7 @@ typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>       */
 typedef struct dfm2g_ilu_s *dfm2g_ilu;       /* CPreconditionerILU<double>  */
 typedef struct dfm2g_tetmesh_s *dfm2g_tetmesh; /* linear-tet assembler      */
 typedef struct dfm2g_trimesh2_s *dfm2g_trimesh2; /* 2-D linear-triangle assembler */
+typedef struct dfm2g_hexmesh_s *dfm2g_hexmesh; /* trilinear-hex (Q1) assembler */
 
 /* Per-solve record filled by the solvers (any pointer may be NULL). */
 typedef struct dfm2g_solve_stats {
@@ -267,6 +268,22 @@ DFM2G_API int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const 
  * counterpart; K_e is linear in E). young is unused except for shape checks. */
 DFM2G_API int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu,
                                  const double *u, const double *lam, double *dLdE, int mem);
+/* Backward-Euler linear solid (adds; 3x3 blocks): MergeLinSys_SolidLinear_BEuler_MeshTet3D,
+ * include/delfem2/fem_solidlinear.h:381-443, or, with rot (9*np row-major
+ * rotations, else NULL), MergeLinSys_SolidStiffwarp_BEuler_MeshTet3D (445-530).
+ * K += K_e + rho vol/(4 dt^2) I on the diagonal blocks, b += r_e/dt. disp,
+ * velo: 3*np; g: 3 host doubles. */
+DFM2G_API int dfm2g_tetmesh_assemble_beuler(dfm2g_tetmesh t, dfm2g_bsr m, double myu, double lambda, double rho,
+                                            const double *g, double dt, const double *disp, const double *velo,
+                                            const double *rot, double *b, int mem);
+/* Newmark-beta linear solid (adds; 3x3 blocks): MergeLinSys_SolidLinear_NewmarkBeta_MeshTet3D,
+ * fem_solidlinear.h:331-379, with the first-iteration element matrix of
+ * EMat_SolidLinear_NewmarkBeta_MeshTet3D (fem_solidlinear.cpp:437-488):
+ * K += M_e + beta dt^2 K_e (consistent mass), b += r_e. gamma is unused there. */
+DFM2G_API int dfm2g_tetmesh_assemble_newmark(dfm2g_tetmesh t, dfm2g_bsr m, double myu, double lambda, double rho,
+                                             const double *g, double dt, double gamma, double beta,
+                                             const double *disp, const double *velo, const double *acc, double *b,
+                                             int mem);
 /* Scalar Poisson (adds; the matrix has 1x1 blocks): the loop of
  * MergeLinSys_Poission_MeshTet3D, include/delfem2/fem_poisson.h:128-162, with
  * EMat_Poisson_Tet3D (fem_poisson.cpp:163-194): K_e[a][b] = alpha vol
@@ -274,6 +291,21 @@ DFM2G_API int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu
  * (the fixed values lifted into b), or NULL for zero. */
 DFM2G_API int dfm2g_tetmesh_assemble_poisson(dfm2g_tetmesh t, dfm2g_bsr m, double alpha, double source,
                                              const double *val, double *b, int mem);
+
+/* ---- trilinear hexahedra (Q1) ------------------------------------------------- */
+/* Builds, for mesh (xyz: 3*np, hex: 8*nhex in ShapeFunc_Hex8's corner order,
+ * host arrays) against the pattern of a 3x3-block matrix: the element->slot map
+ * and a greedy colouring. A hex that repeats a node is refused (DFM2G_ERR_ARG). */
+DFM2G_API int dfm2g_hexmesh_create(dfm2g_hexmesh *out, dfm2g_bsr m, const double *xyz, size_t np,
+                                   const unsigned *hex, size_t nhex);
+DFM2G_API int dfm2g_hexmesh_destroy(dfm2g_hexmesh t);
+/* Static linear solid (adds): the element loop of MergeLinSys_LinearSolid3D_Static_Q1,
+ * include/delfem2/fem_solidlinear.h:239-276, with
+ * elemMatRes_LinearSolidGravity3_Static_Q1 (fem_solidlinear.cpp:238-281, the
+ * reference's three-point Gauss rule per direction): K += K_e,
+ * b += int(rho g N) - K_e u_e. g: 3 host doubles; disp: 3*np or NULL. */
+DFM2G_API int dfm2g_hexmesh_assemble_linear(dfm2g_hexmesh t, dfm2g_bsr m, double myu, double lambda, double rho,
+                                            const double *g, const double *disp, double *b, int mem);
 
 /* ---- 2-D linear triangles ---------------------------------------------------- */
 /* Builds, for mesh (xy: 2*np, tri: 3*ntri, host arrays) against the pattern of

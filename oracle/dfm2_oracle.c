@@ -1817,3 +1817,243 @@ int orc_assemble_tri2(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, c
   free(buf);
   return status;
 }
+
+/* ---- dynamic linear tets (3x3 blocks) ----------------------------------- */
+
+/* MergeLinSys_SolidLinear_BEuler_MeshTet3D, include/delfem2/fem_solidlinear.h: */
+/* 381-443, and, with rot (np 3x3 row-major rotations) not NULL,              */
+/* MergeLinSys_SolidStiffwarp_BEuler_MeshTet3D (445-530). Per tet: K_e of     */
+/* SetEmat_LinearSolid3<4>; stiffness warping makes K_ij <- R_i K_ij R_i^T;   */
+/* r_i = vol rho g / 4 - sum_j K_ij w_j with w_j = u_j + dt v_j (warped:      */
+/* w_j = P_j + u_j + dt v_j - R_i P_j); then K_ii += rho vol / (4 dt^2) I,    */
+/* b_i += r_i / dt and Merge<4,4,3,3>. Returns 0, or 1 on a missing slot.      */
+int orc_assemble_tet_beuler(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                            double *vdia, double *b, double myu, double lambda, double rho, const double g[3],
+                            double dt, const double *xyz, const uint32_t *tet, size_t ntet, const double *disp,
+                            const double *velo, const double *rot) {
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  int status = 0;
+  for (size_t e = 0; e < ntet && status == 0; ++e) {
+    const uint32_t *n = tet + e * 4;
+    double P[4][3], u[4][3], v[4][3], emat[4][4][3][3], vol;
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) {
+        P[k][d] = xyz[(size_t)n[k] * 3 + d];
+        u[k][d] = disp[(size_t)n[k] * 3 + d];
+        v[k][d] = velo[(size_t)n[k] * 3 + d];
+      }
+    orc_emat_tet_linear(P, myu, lambda, emat, &vol);
+    if (rot) { /* MatMatTrans3 then MatMat3 (femutil.cpp:96-116): R_i K_ij R_i^T */
+      for (int i = 0; i < 4; ++i) {
+        const double *R = rot + (size_t)n[i] * 9;
+        for (int j = 0; j < 4; ++j) {
+          double t[3][3];
+          for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+              t[r][c] = emat[i][j][r][0] * R[c * 3 + 0] + emat[i][j][r][1] * R[c * 3 + 1] +
+                        emat[i][j][r][2] * R[c * 3 + 2];
+          for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c)
+              emat[i][j][r][c] = R[r * 3 + 0] * t[0][c] + R[r * 3 + 1] * t[1][c] + R[r * 3 + 2] * t[2][c];
+        }
+      }
+    }
+    double res[4][3];
+    for (int i = 0; i < 4; ++i) {
+      const double *R = rot ? rot + (size_t)n[i] * 9 : NULL;
+      for (int a = 0; a < 3; ++a) res[i][a] = vol * rho * g[a] * 0.25;
+      for (int j = 0; j < 4; ++j) {
+        double w[3];
+        if (R) {
+          for (int d = 0; d < 3; ++d) {
+            const double pj1 = R[d * 3 + 0] * P[j][0] + R[d * 3 + 1] * P[j][1] + R[d * 3 + 2] * P[j][2];
+            w[d] = P[j][d] + u[j][d] + dt * v[j][d] - pj1;
+          }
+        } else {
+          for (int d = 0; d < 3; ++d) w[d] = u[j][d] + dt * v[j][d];
+        }
+        for (int a = 0; a < 3; ++a) {
+          res[i][a] -= emat[i][j][a][0] * w[0];
+          res[i][a] -= emat[i][j][a][1] * w[1];
+          res[i][a] -= emat[i][j][a][2] * w[2];
+        }
+      }
+    }
+    const double m = rho * vol * 0.25 / (dt * dt);
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) emat[i][i][a][a] += m;
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) b[(size_t)n[i] * 3 + a] += res[i][a] / dt;
+    status = orc_merge(nblk, row_start, col, vcrs, vdia, 4, n, &emat[0][0][0][0], buf);
+  }
+  free(buf);
+  return status;
+}
+
+/* MergeLinSys_SolidLinear_NewmarkBeta_MeshTet3D, include/delfem2/           */
+/* fem_solidlinear.h:331-379, with EMat_SolidLinear_NewmarkBeta_MeshTet3D     */
+/* (fem_solidlinear.cpp:437-488, is_initial_iter true): K_e of                */
+/* SetEmat_LinearSolid3<4>, consistent mass M_ij = rho vol / 20 (1 + d_ij) I  */
+/* (femutil.cpp:260-280); E_e = M + beta dt^2 K; r = vol rho g / 4 - K u -    */
+/* M a - dt K v - dt^2/2 K a (AddEmatEvecScale3, femutil.h:252-268, in that  */
+/* order); b += r and Merge<4,4,3,3> of E_e. gamma is unused, as in the       */
+/* reference. Returns 0, or 1 on a missing slot.                              */
+int orc_assemble_tet_newmark(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                             double *vdia, double *b, double myu, double lambda, double rho, const double g[3],
+                             double dt, double gamma, double beta, const double *xyz, const uint32_t *tet,
+                             size_t ntet, const double *disp, const double *velo, const double *acc) {
+  (void)gamma;
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  int status = 0;
+  for (size_t e = 0; e < ntet && status == 0; ++e) {
+    const uint32_t *n = tet + e * 4;
+    double P[4][3], U[3][4][3], eK[4][4][3][3], eM[4][4][3][3], emat[4][4][3][3], vol;
+    const double *src[3] = {disp, velo, acc};
+    for (int k = 0; k < 4; ++k)
+      for (int d = 0; d < 3; ++d) {
+        P[k][d] = xyz[(size_t)n[k] * 3 + d];
+        for (int q = 0; q < 3; ++q) U[q][k][d] = src[q][(size_t)n[k] * 3 + d];
+      }
+    orc_emat_tet_linear(P, myu, lambda, eK, &vol);
+    const double mw = rho * vol * 0.05;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j)
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) eM[i][j][r][c] = (r == c) ? mw + (i == j ? mw : 0.0) : 0.0;
+    const double bdt2 = beta * dt * dt;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j)
+        for (int r = 0; r < 3; ++r)
+          for (int c = 0; c < 3; ++c) emat[i][j][r][c] = eM[i][j][r][c] + bdt2 * eK[i][j][r][c];
+    double res[4][3];
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) res[i][a] = vol * rho * g[a] * 0.25;
+    /* (matrix, vector, scale) in the reference's order */
+    const double (*mats[4])[4][3][3] = {eK, eM, eK, eK};
+    const int vecs[4] = {0, 2, 1, 2};
+    const double scales[4] = {-1.0, -1.0, -dt, -0.5 * dt * dt};
+    for (int t = 0; t < 4; ++t)
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+          for (int a = 0; a < 3; ++a) {
+            const double(*Mt)[3] = mats[t][i][j];
+            const double *x = U[vecs[t]][j];
+            res[i][a] += scales[t] * (Mt[a][0] * x[0] + Mt[a][1] * x[1] + Mt[a][2] * x[2]);
+          }
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) b[(size_t)n[i] * 3 + a] += res[i][a];
+    status = orc_merge(nblk, row_start, col, vcrs, vdia, 4, n, &emat[0][0][0][0], buf);
+  }
+  free(buf);
+  return status;
+}
+
+/* ---- trilinear hexahedra (Q1, 3x3 blocks) ----------------------------- */
+
+/* Three-point Gauss-Legendre rule as the reference tabulates it (include/  */
+/* delfem2/quadrature.h:28-31, in that order, to 15 digits): the Q1 element */
+/* asks for table block iGauss = 2, which is the three-point rule.           */
+static const double kOrcGauss3[3][2] = {
+    {+0.000000000000000, 0.888888888888889}, {-0.774596669241483, 0.555555555555556},
+    {+0.774596669241483, 0.555555555555556}};
+
+/* ShapeFunc_Hex8 + HexVox, include/delfem2/femutil.cpp:118-170, 372-421:   */
+/* shape values an[8], physical gradients dndx[8][3] and det(dx/dr) at the  */
+/* reference point (r0, r1, r2); node k sits at the corner                  */
+/* ((k+1)&2 ? + : -, k&2 ? + : -, k&4 ? + : -).                               */
+static void orc_hex8_shape(double r0, double r1, double r2, const double P[8][3], double *detjac,
+                           double dndx[8][3], double an[8]) {
+  static const double sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+                      sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+  double dndr[8][3];
+  for (int k = 0; k < 8; ++k) {
+    const double a = 1.0 + sx[k] * r0, b = 1.0 + sy[k] * r1, c = 1.0 + sz[k] * r2;
+    an[k] = 0.125 * a * b * c;
+    dndr[k][0] = sx[k] * 0.125 * b * c;
+    dndr[k][1] = sy[k] * 0.125 * a * c;
+    dndr[k][2] = sz[k] * 0.125 * a * b;
+  }
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int k = 0; k < 8; ++k)
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) J[r][c] += P[k][r] * dndr[k][c];
+  const double det = J[0][0] * J[1][1] * J[2][2] + J[1][0] * J[2][1] * J[0][2] + J[2][0] * J[0][1] * J[1][2] -
+                     J[0][0] * J[2][1] * J[1][2] - J[1][0] * J[0][1] * J[2][2] - J[2][0] * J[1][1] * J[0][2];
+  const double s = 1.0 / det;
+  double Ji[3][3];
+  Ji[0][0] = s * (J[1][1] * J[2][2] - J[1][2] * J[2][1]);
+  Ji[0][1] = s * (J[0][2] * J[2][1] - J[0][1] * J[2][2]);
+  Ji[0][2] = s * (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
+  Ji[1][0] = s * (J[1][2] * J[2][0] - J[1][0] * J[2][2]);
+  Ji[1][1] = s * (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
+  Ji[1][2] = s * (J[0][2] * J[1][0] - J[0][0] * J[1][2]);
+  Ji[2][0] = s * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  Ji[2][1] = s * (J[0][1] * J[2][0] - J[0][0] * J[2][1]);
+  Ji[2][2] = s * (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 3; ++c)
+      dndx[k][c] = dndr[k][0] * Ji[0][c] + dndr[k][1] * Ji[1][c] + dndr[k][2] * Ji[2][c];
+  *detjac = det;
+}
+
+/* elemMatRes_LinearSolidGravity3_Static_Q1, include/delfem2/               */
+/* fem_solidlinear.cpp:238-281: 3x3x3 Gauss points (r0 outer, r2 inner);    */
+/* at each, w = det J w0 w1 w2; K += AddEmat_LinearSolid3<8>(w) (55-79) and */
+/* r_i += w rho g N_i; then r -= K u.                                        */
+void orc_emat_hex_q1(const double P[8][3], double myu, double lambda, double rho, const double g[3],
+                     const double disp[8][3], double emat[8][8][3][3], double eres[8][3]) {
+  memset(emat, 0, sizeof(double) * 8 * 8 * 9);
+  memset(eres, 0, sizeof(double) * 8 * 3);
+  for (int i0 = 0; i0 < 3; ++i0)
+    for (int i1 = 0; i1 < 3; ++i1)
+      for (int i2 = 0; i2 < 3; ++i2) {
+        double det, dn[8][3], an[8];
+        orc_hex8_shape(kOrcGauss3[i0][0], kOrcGauss3[i1][0], kOrcGauss3[i2][0], P, &det, dn, an);
+        const double w = det * kOrcGauss3[i0][1] * kOrcGauss3[i1][1] * kOrcGauss3[i2][1];
+        for (int i = 0; i < 8; ++i)
+          for (int j = 0; j < 8; ++j) {
+            for (int r = 0; r < 3; ++r)
+              for (int c = 0; c < 3; ++c)
+                emat[i][j][r][c] += w * (lambda * dn[i][r] * dn[j][c] + myu * dn[j][r] * dn[i][c]);
+            const double dd = dn[i][0] * dn[j][0] + dn[i][1] * dn[j][1] + dn[i][2] * dn[j][2];
+            for (int r = 0; r < 3; ++r) emat[i][j][r][r] += w * myu * dd;
+          }
+        for (int i = 0; i < 8; ++i)
+          for (int r = 0; r < 3; ++r) eres[i][r] += w * rho * g[r] * an[i];
+      }
+  for (int i = 0; i < 8; ++i)
+    for (int j = 0; j < 8; ++j)
+      for (int r = 0; r < 3; ++r)
+        eres[i][r] += -1.0 * (emat[i][j][r][0] * disp[j][0] + emat[i][j][r][1] * disp[j][1] +
+                              emat[i][j][r][2] * disp[j][2]);
+}
+
+/* The element loop of MergeLinSys_LinearSolid3D_Static_Q1                   */
+/* (include/delfem2/fem_solidlinear.h:239-276) without its own zeroing of K */
+/* and b: per hex b += r_e and Merge<8,8,3,3> of K_e. disp may be NULL.       */
+/* Returns 0, or 1 on a missing slot.                                        */
+int orc_assemble_hex_q1(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs, double *vdia,
+                        double *b, double myu, double lambda, double rho, const double g[3], const double *xyz,
+                        const uint32_t *hex, size_t nhex, const double *disp) {
+  uint32_t *buf = (uint32_t *)malloc((size_t)nblk * sizeof(uint32_t) + 1);
+  for (uint32_t i = 0; i < nblk; ++i) buf[i] = ORC_UNSET;
+  int status = 0;
+  static double emat[8][8][3][3];
+  for (size_t e = 0; e < nhex && status == 0; ++e) {
+    const uint32_t *n = hex + e * 8;
+    double P[8][3], U[8][3], eres[8][3];
+    for (int k = 0; k < 8; ++k)
+      for (int d = 0; d < 3; ++d) {
+        P[k][d] = xyz[(size_t)n[k] * 3 + d];
+        U[k][d] = disp ? disp[(size_t)n[k] * 3 + d] : 0.0;
+      }
+    orc_emat_hex_q1(P, myu, lambda, rho, g, U, emat, eres);
+    for (int k = 0; k < 8; ++k)
+      for (int d = 0; d < 3; ++d) b[(size_t)n[k] * 3 + d] += eres[k][d];
+    status = orc_merge(nblk, row_start, col, vcrs, vdia, 8, n, &emat[0][0][0][0], buf);
+  }
+  free(buf);
+  return status;
+}

@@ -164,6 +164,23 @@ int orc_assemble_tri2(uint32_t nblk, uint32_t ndim, const uint32_t *row_start, c
                       double *vdia, double *b, const double *param, const double *xy, const uint32_t *tri,
                       size_t ntri, const double *val);
 
+/* --- dynamic linear tets ------------------------------------------------ */
+int orc_assemble_tet_beuler(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                            double *vdia, double *b, double myu, double lambda, double rho, const double g[3],
+                            double dt, const double *xyz, const uint32_t *tet, size_t ntet, const double *disp,
+                            const double *velo, const double *rot);
+int orc_assemble_tet_newmark(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                             double *vdia, double *b, double myu, double lambda, double rho, const double g[3],
+                             double dt, double gamma, double beta, const double *xyz, const uint32_t *tet,
+                             size_t ntet, const double *disp, const double *velo, const double *acc);
+
+/* --- trilinear hexahedra (Q1) ------------------------------------------- */
+void orc_emat_hex_q1(const double P[8][3], double myu, double lambda, double rho, const double g[3],
+                     const double disp[8][3], double emat[8][8][3][3], double eres[8][3]);
+int orc_assemble_hex_q1(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs, double *vdia,
+                        double *b, double myu, double lambda, double rho, const double g[3], const double *xyz,
+                        const uint32_t *hex, size_t nhex, const double *disp);
+
 #ifdef __cplusplus
 }
 #endif

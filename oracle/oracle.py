@@ -401,6 +401,91 @@ class Oracle:
         return vc[: col.size * bb], vd, b
 
 
+    # ---- dynamic linear tets (3x3 blocks) -----------------------------------------
+    def assemble_tet_beuler(self, row_start, col, xyz, tet, myu, lam, rho, g, dt, disp, velo, rot=None):
+        """BEuler (rot None) or stiffness-warped BEuler tet assembly into a zeroed matrix: (vcrs, vdia, b)."""
+        nblk = row_start.size - 1
+        f = self._f("assemble_tet_beuler")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_double, _f64p,
+                      C.c_double, _f64p, _u32p, C.c_size_t, _f64p, _f64p, C.c_void_p]
+        f.restype = C.c_int
+        vc = np.zeros(max(col.size * 9, 1), np.float64)
+        vd = np.zeros(nblk * 9, np.float64)
+        b = np.zeros(nblk * 3, np.float64)
+        tet = np.ascontiguousarray(tet, np.uint32)
+        r = None if rot is None else np.ascontiguousarray(rot, np.float64)
+        st = f(nblk, row_start, _nz(col), vc, vd, b, myu, lam, rho, np.ascontiguousarray(g, np.float64), dt,
+               np.ascontiguousarray(xyz, np.float64), tet, tet.size // 4, np.ascontiguousarray(disp, np.float64),
+               np.ascontiguousarray(velo, np.float64), _optr(r))
+        assert st == 0
+        return vc[: col.size * 9], vd, b
+
+    def assemble_tet_newmark(self, row_start, col, xyz, tet, myu, lam, rho, g, dt, gamma, beta, disp, velo, acc):
+        """Newmark-beta tet assembly (initial iteration) into a zeroed matrix: (vcrs, vdia, b)."""
+        nblk = row_start.size - 1
+        f = self._f("assemble_tet_newmark")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_double, _f64p,
+                      C.c_double, C.c_double, C.c_double, _f64p, _u32p, C.c_size_t, _f64p, _f64p, _f64p]
+        f.restype = C.c_int
+        vc = np.zeros(max(col.size * 9, 1), np.float64)
+        vd = np.zeros(nblk * 9, np.float64)
+        b = np.zeros(nblk * 3, np.float64)
+        tet = np.ascontiguousarray(tet, np.uint32)
+        st = f(nblk, row_start, _nz(col), vc, vd, b, myu, lam, rho, np.ascontiguousarray(g, np.float64), dt, gamma,
+               beta, np.ascontiguousarray(xyz, np.float64), tet, tet.size // 4,
+               *[np.ascontiguousarray(v, np.float64) for v in (disp, velo, acc)])
+        assert st == 0
+        return vc[: col.size * 9], vd, b
+
+
+    # ---- trilinear hexahedra (Q1) ------------------------------------------------
+    def emat_hex_q1(self, P, myu, lam, rho, g, disp):
+        f = self._f("emat_hex_q1")
+        f.argtypes = [_f64p, C.c_double, C.c_double, C.c_double, _f64p, _f64p, _f64p, _f64p]
+        emat = np.zeros(8 * 8 * 9, np.float64)
+        eres = np.zeros(24, np.float64)
+        f(np.ascontiguousarray(P, np.float64).ravel(), myu, lam, rho, np.ascontiguousarray(g, np.float64),
+          np.ascontiguousarray(disp, np.float64).ravel(), emat, eres)
+        return emat.reshape(8, 8, 3, 3), eres.reshape(8, 3)
+
+    def assemble_hex_q1(self, row_start, col, xyz, hexa, myu, lam, rho, g, disp=None):
+        """Q1 hex assembly into a zeroed matrix: (vcrs, vdia, b)."""
+        nblk = row_start.size - 1
+        f = self._f("assemble_hex_q1")
+        f.argtypes = [C.c_uint32, _u32p, _u32p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_double, _f64p,
+                      _f64p, _u32p, C.c_size_t, C.c_void_p]
+        f.restype = C.c_int
+        vc = np.zeros(max(col.size * 9, 1), np.float64)
+        vd = np.zeros(nblk * 9, np.float64)
+        b = np.zeros(nblk * 3, np.float64)
+        hexa = np.ascontiguousarray(hexa, np.uint32)
+        d = None if disp is None else np.ascontiguousarray(disp, np.float64)
+        st = f(nblk, row_start, _nz(col), vc, vd, b, myu, lam, rho, np.ascontiguousarray(g, np.float64),
+               np.ascontiguousarray(xyz, np.float64), hexa, hexa.size // 8, _optr(d))
+        assert st == 0
+        return vc[: col.size * 9], vd, b
+
+
+def hex_grid(nx: int, ny: int, nz: int, h: float, seed: int | None = None, jitter: float = 0.0):
+    """A structured nx x ny x nz hex mesh of spacing h (node (ix,iy,iz) = ix*(ny+1)*(nz+1) + iy*(nz+1) + iz), each
+    hex's nodes in ShapeFunc_Hex8's corner order; interior nodes moved by up to jitter*h when seeded."""
+    ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    xyz = np.stack([ii, jj, kk], -1).reshape(-1, 3).astype(np.float64) * h
+    if seed is not None and jitter > 0:
+        rng = np.random.default_rng(seed)
+        inner = ((ii > 0) & (ii < nx) & (jj > 0) & (jj < ny) & (kk > 0) & (kk < nz)).ravel()
+        xyz[inner] += rng.uniform(-jitter * h, jitter * h, (int(inner.sum()), 3))
+
+    def nid(i, j, k):
+        return (i * (ny + 1) + j) * (nz + 1) + k
+
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    hexa = np.stack([nid(i, j, k), nid(i + 1, j, k), nid(i + 1, j + 1, k), nid(i, j + 1, k),
+                     nid(i, j, k + 1), nid(i + 1, j, k + 1), nid(i + 1, j + 1, k + 1), nid(i, j + 1, k + 1)], -1)
+    return xyz.ravel(), hexa.astype(np.uint32).ravel()
+
+
 def _nz(a):
     """Never hand a zero-length array to C (its data pointer may be NULL)."""
     if a.size == 0:

@@ -324,6 +324,74 @@ uint32_t ref_solve_cg(uint32_t nblk, const uint32_t *row_start, const uint32_t *
   return static_cast<uint32_t>(h.size());
 }
 
+// MergeLinSys_SolidLinear_BEuler_MeshTet3D (fem_solidlinear.h:381-443) or,
+// with rot, MergeLinSys_SolidStiffwarp_BEuler_MeshTet3D (445-530), into the
+// given 3x3 matrix; the contract of orc_assemble_tet_beuler.
+int ref_assemble_tet_beuler(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                            double *vdia, double *b, double myu, double lambda, double rho, const double g[3],
+                            double dt, const double *xyz, const uint32_t *tet, size_t ntet, const double *disp,
+                            const double *velo, const double *rot) {
+  auto m = make_matrix(nblk, row_start, col, vcrs, vdia);
+  if (rot) {
+    std::vector<double> aR(rot, rot + (size_t)nblk * 9);
+    dfm2::MergeLinSys_SolidStiffwarp_BEuler_MeshTet3D(m, b, myu, lambda, rho, g, dt, xyz, nblk, tet,
+                                                      (unsigned)ntet, disp, velo, aR);
+  } else {
+    dfm2::MergeLinSys_SolidLinear_BEuler_MeshTet3D(m, b, myu, lambda, rho, g, dt, xyz, nblk, tet, (unsigned)ntet,
+                                                   disp, velo);
+  }
+  std::memcpy(vcrs, m.val_crs_.data(), sizeof(double) * 9 * row_start[nblk]);
+  std::memcpy(vdia, m.val_dia_.data(), sizeof(double) * 9 * nblk);
+  return 0;
+}
+
+// MergeLinSys_SolidLinear_NewmarkBeta_MeshTet3D (fem_solidlinear.h:331-379).
+int ref_assemble_tet_newmark(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs,
+                             double *vdia, double *b, double myu, double lambda, double rho, const double g[3],
+                             double dt, double gamma, double beta, const double *xyz, const uint32_t *tet,
+                             size_t ntet, const double *disp, const double *velo, const double *acc) {
+  auto m = make_matrix(nblk, row_start, col, vcrs, vdia);
+  dfm2::MergeLinSys_SolidLinear_NewmarkBeta_MeshTet3D(m, b, myu, lambda, rho, g, dt, gamma, beta, xyz, nblk, tet,
+                                                      ntet, disp, velo, acc);
+  std::memcpy(vcrs, m.val_crs_.data(), sizeof(double) * 9 * row_start[nblk]);
+  std::memcpy(vdia, m.val_dia_.data(), sizeof(double) * 9 * nblk);
+  return 0;
+}
+
+// elemMatRes_LinearSolidGravity3_Static_Q1 (fem_solidlinear.cpp:238-281).
+void ref_emat_hex_q1(const double P[8][3], double myu, double lambda, double rho, const double g[3],
+                     const double disp[8][3], double emat[8][8][3][3], double eres[8][3]) {
+  dfm2::elemMatRes_LinearSolidGravity3_Static_Q1(myu, lambda, rho, g, P, disp, emat, eres);
+}
+
+// The element loop of MergeLinSys_LinearSolid3D_Static_Q1 (fem_solidlinear.h:
+// 239-276: elemMatRes_LinearSolidGravity3_Static_Q1, b += r_e, Merge<8,8,3,3>)
+// run here on a CMatrixSparse, without the function's own zeroing, whose
+// `mat_A.SetZero()` names a member CMatrixSparse does not have (`setZero`).
+int ref_assemble_hex_q1(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs, double *vdia,
+                        double *b, double myu, double lambda, double rho, const double g[3], const double *xyz,
+                        const uint32_t *hex, size_t nhex, const double *disp) {
+  auto m = make_matrix(nblk, row_start, col, vcrs, vdia);
+  std::vector<unsigned int> buf(nblk, UINT_MAX);
+  std::vector<double> zero((size_t)nblk * 3, 0.0);
+  const double *u = disp ? disp : zero.data();
+  bool ok = true;
+  static double emat[8][8][3][3];
+  for (size_t e = 0; e < nhex && ok; ++e) {
+    const unsigned int *aIP = hex + e * 8;
+    double coords[8][3], disps[8][3], eres[8][3];
+    dfm2::FetchData<8, 3>(coords, aIP, xyz);
+    dfm2::FetchData<8, 3>(disps, aIP, u);
+    dfm2::elemMatRes_LinearSolidGravity3_Static_Q1(myu, lambda, rho, g, coords, disps, emat, eres);
+    for (int k = 0; k < 8; ++k)
+      for (int d = 0; d < 3; ++d) b[aIP[k] * 3 + d] += eres[k][d];
+    ok = dfm2::Merge<8, 8, 3, 3, double>(m, aIP, aIP, emat, buf);
+  }
+  std::memcpy(vcrs, m.val_crs_.data(), sizeof(double) * 9 * row_start[nblk]);
+  std::memcpy(vdia, m.val_dia_.data(), sizeof(double) * 9 * nblk);
+  return ok ? 0 : 1;
+}
+
 int ref_poisson_tri2(uint32_t nblk, const uint32_t *row_start, const uint32_t *col, double *vcrs, double *vdia,
                      double *b, double alpha, double source, const double *xy, const uint32_t *tri, size_t ntri,
                      const double *val);  // ref_driver_nd.cpp

@@ -5,7 +5,7 @@ oracle/Makefile), so it only works where the reference source tree exists.
 The outputs are small .npz files committed next to this script; the tests
 read them on machines without the reference.
 
-  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab nd]
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab nd dynamic]
 """
 from __future__ import annotations
 
@@ -251,6 +251,23 @@ def make_nd(R):
     np.savez_compressed(os.path.join(HERE, "nd.npz"), **out)
 
 
+def make_dynamic(R):
+    """The reference's MergeLinSys_SolidLinear_BEuler_MeshTet3D,
+    MergeLinSys_SolidStiffwarp_BEuler_MeshTet3D and
+    MergeLinSys_SolidLinear_NewmarkBeta_MeshTet3D, and the Q1 hex element loop,
+    on the inputs of tests/dyn_systems.py (K values and b)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import dyn_systems as DS
+    s = DS.inputs(R)
+    out = {}
+    for kind in DS.KINDS:
+        vc, vd, b = DS.assemble(R, s, kind)
+        out.update({f"{kind}_vc": vc, f"{kind}_vd": vd, f"{kind}_b": b})
+    vc, vd, b = DS.assemble_hex(R, DS.hex_inputs(R))  # the element loop of MergeLinSys_LinearSolid3D_Static_Q1
+    out.update({"hexq1_vc": vc, "hexq1_vd": vd, "hexq1_b": b})
+    np.savez_compressed(os.path.join(HERE, "dynamic.npz"), **out)
+
+
 def main(which):
     build(quiet=True)
     R = reference()
@@ -275,6 +292,8 @@ def main(which):
         make_bicgstab(R)
     if "nd" in which:
         make_nd(R)
+    if "dynamic" in which:
+        make_dynamic(R)
 
 
 if __name__ == "__main__":
