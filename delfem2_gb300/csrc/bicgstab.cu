@@ -142,6 +142,12 @@ int dfm2g_solve_pbicgstab(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_pbicgstab: null vector");
   DFM2G_TRY(ensure_context());
   const size_t n = (size_t)m->nblk * m->ndim;
+  if (n == 0) {  // an empty system: history [|r0|] = [0], as the |r0|^2 < 1e-60 early return
+    if (hist && hist_cap) hist[0] = 0.0;
+    if (n_hist) *n_hist = 1;
+    if (stats) *stats = dfm2g_solve_stats{0u, 0u, 0.0, 0.0};
+    return DFM2G_OK;
+  }
   auto &W = g_bi;
   const unsigned grid = (unsigned)ctx().num_sms * 4;
   DFM2G_TRY(W.st.ensure(1));

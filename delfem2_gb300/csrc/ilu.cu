@@ -239,7 +239,7 @@ static int compute_levels(dfm2g_ilu_s *p, bool backward) {
   DFM2G_TRY(order.resize(n));
   DevBuf<unsigned> counters;  // [0] assigned, [1] max level
   DFM2G_TRY(counters.resize(2));
-  DFM2G_CUDA(cudaMemsetAsync(level.p, 0xFF, sizeof(unsigned) * n, stream()));
+  if (n) DFM2G_CUDA(cudaMemsetAsync(level.p, 0xFF, sizeof(unsigned) * n, stream()));
   DFM2G_CUDA(cudaMemsetAsync(counters.p, 0, sizeof(unsigned) * 2, stream()));
   unsigned h[2] = {0, 0};
   unsigned sweeps = 0;

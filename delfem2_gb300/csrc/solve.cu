@@ -607,6 +607,15 @@ static int true_residual(dfm2g_bsr_s *m, const double *b, const double *x, doubl
   return DFM2G_OK;
 }
 
+// An empty system (no block rows): nothing to queue on the device. The
+// history is [|r0|] = [0] (the |r0|^2 < 1e-30 early return of Solve_PCG).
+static int empty_solve(double *hist, unsigned hist_cap, unsigned *n_hist, dfm2g_solve_stats *stats) {
+  if (hist && hist_cap) hist[0] = 0.0;
+  if (n_hist) *n_hist = 1;
+  if (stats) *stats = dfm2g_solve_stats{0u, 0u, 0.0, 0.0};
+  return DFM2G_OK;
+}
+
 }  // namespace dfm2g
 
 using namespace dfm2g;
@@ -619,6 +628,7 @@ int dfm2g_solve_pcg(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol, 
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg: null preconditioner");
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_pcg: null vector");
   const size_t n = (size_t)m->nblk * m->ndim;
+  if (n == 0) return empty_solve(hist, hist_cap, n_hist, stats);
   DFM2G_TRY(ws_prepare(n, max_iter + 2, false));
   VecArg<double> ar, ax;
   DFM2G_TRY(ar.in(r, n, mem, true));
@@ -656,6 +666,11 @@ int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_i
   DFM2G_TRY(check_pair(m, nullptr));
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_cg: null vector");
   const size_t n = (size_t)m->nblk * m->ndim;
+  if (n == 0) {  // Solve_CG's history has no initial entry: empty for |r0|^2 < 1e-30
+    if (n_hist) *n_hist = 0;
+    if (stats) *stats = dfm2g_solve_stats{0u, 0u, 0.0, 0.0};
+    return DFM2G_OK;
+  }
   DFM2G_TRY(ws_prepare(n, max_iter + 2, false));
   VecArg<double> ar, ax;
   DFM2G_TRY(ar.in(r, n, mem, true));
@@ -695,6 +710,7 @@ int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const double *b, do
   if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null vector");
   if (!(delta > 0 && delta < 1)) return fail(DFM2G_ERR_ARG, "delta must be in (0,1)");
   const size_t n = (size_t)m->nblk * m->ndim;
+  if (n == 0) return empty_solve(nullptr, 0, nullptr, stats);
   DFM2G_TRY(ws_prepare(n, max_iter + 4, true));
   DFM2G_TRY(bsr_ensure_f32(m));
   DFM2G_TRY(ilu_ensure_f32(p));
@@ -747,6 +763,7 @@ int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, 
   if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null vector");
   if (!(inner_tol > 0 && inner_tol < 1)) return fail(DFM2G_ERR_ARG, "inner_tol must be in (0,1)");
   const size_t n = (size_t)m->nblk * m->ndim;
+  if (n == 0) return empty_solve(nullptr, 0, nullptr, stats);
   DFM2G_TRY(ws_prepare(n, 4, true));
   DFM2G_TRY(bsr_ensure_f32(m));
   DFM2G_TRY(ilu_ensure_f32(p));

@@ -1,11 +1,14 @@
 """One static-elasticity solve on a voxel block, for profiler captures.
 
   python -m delfem2_gb300.profile_case [--nx 64 --ny 64 --nz 64] [--fp64] [--solves 1] [--method reliable]
+                                       [--poisson]
 
 Sets the problem up (mesh, pattern, level sets, assembly, ILU(0)) and runs
 `--solves` solves of K u = b to 1e-10 (FP32-inner/FP64-refinement by default,
 with reliable updates or restarted refinement; plain FP64 Solve_PCG with
---fp64), printing the device time of each.
+--fp64), printing the device time of each. --poisson solves the scalar
+Poisson problem (1x1 blocks) on the same mesh instead: alpha = 1, source = 1,
+the z = 0 face at 0 and the top face at 1.
 """
 from __future__ import annotations
 
@@ -22,6 +25,7 @@ def main():
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--levels", action="store_true", help="level-by-level sweep schedule")
     ap.add_argument("--method", choices=["reliable", "restart"], default="reliable")
+    ap.add_argument("--poisson", action="store_true", help="scalar Poisson (1x1 blocks) on the same mesh")
     args = ap.parse_args()
 
     import torch
@@ -29,22 +33,41 @@ def main():
     from delfem2_gb300 import _native as N
 
     a = D.voxel_problem_arrays(args.nx, args.ny, args.nz, 1.0 / args.nx, seed=3)
-    P = D.StaticElasticProblem(a)
+    if args.poisson:
+        import numpy as np
+        K = D.CMatrixSparse()
+        K.Initialize(a["np"], 1, True)
+        K.SetPattern(a["psup_ind"], a["psup"])
+        ilu = D.CPreconditionerILU()
+        ilu.SetPattern0(K)
+        z = a["xyz"].reshape(-1, 3)[:, 2]
+        top = z > z.max() - 1e-12
+        bc = torch.tensor(((z < 1e-12) | top).astype(np.int32), device="cuda")
+        b = torch.zeros(a["np"], dtype=torch.float64, device="cuda")
+        D.TetMesh(K, a["xyz"], a["tet"]).assemble_poisson(1.0, 1.0, b, torch.tensor(np.where(top, 1.0, 0.0),
+                                                                                     device="cuda"))
+        K.SetFixedBC(bc)
+        D.setRHS_Zero(b, bc)
+        ilu.CopyValue(K)
+        assert ilu.Decompose()
+    else:
+        P = D.StaticElasticProblem(a)
+        K, ilu = P.K, P.ilu
+        b = P.assemble(b=torch.zeros(a["np"] * 3, dtype=torch.float64, device="cuda"))
+        assert P.factor()
     if args.levels:
-        P.ilu.set_sweep_mode(N.SWEEP_LEVELS)
-    b = P.assemble(b=torch.zeros(a["np"] * 3, dtype=torch.float64, device="cuda"))
-    assert P.factor()
+        ilu.set_sweep_mode(N.SWEEP_LEVELS)
     torch.cuda.synchronize()
     for k in range(args.solves):
         t = time.perf_counter()
         if args.fp64:
             r, x = b.clone(), torch.zeros_like(b)
-            hist = D.Solve_PCG(r, x, 1e-10, 20000, P.K, P.ilu)
+            hist = D.Solve_PCG(r, x, 1e-10, 20000, K, ilu)
             torch.cuda.synchronize()
             print(f"solve {k}: fp64 {len(hist) - 1} iterations, {1e3 * (time.perf_counter() - t):.1f} ms")
         else:
             x = torch.zeros_like(b)
-            st = D.Solve_PCG_Mixed(b, x, 1e-10, P.K, P.ilu, method=args.method)
+            st = D.Solve_PCG_Mixed(b, x, 1e-10, K, ilu, method=args.method)
             torch.cuda.synchronize()
             print(f"solve {k}: mixed {st.iterations} inner / {st.outer} outer, rel {st.rel_residual:.2e}, "
                   f"{1e3 * (time.perf_counter() - t):.1f} ms")
