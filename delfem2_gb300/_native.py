@@ -33,6 +33,7 @@ SWEEP_LEVELS = 1
 SWEEP_GROUPS = 2
 SWEEP_BLOCK = 3
 SWEEP_PARTS = 4
+SWEEP_CHAINS = 5
 
 
 class SolveStats(C.Structure):

@@ -269,6 +269,20 @@ struct StreamSched {
   dfm2g::DevBuf<size_t> vdst;     // its first value in the stream
 };
 
+// Chains of one sweep direction (chain.cu): descriptors, the record of each
+// row, and the row records per value type (rewritten after each decomposition).
+struct ChainSched {
+  bool built = false, ok = false;
+  unsigned nchain = 0, m = 0;       // chains; longest cross list (blocks)
+  unsigned ver32 = ~0u, ver64 = ~0u; // factor_version the records were written from
+  int coop[2] = {0, 0};             // resident CTAs of the sweep kernel [f64]
+  dfm2g::DevBuf<uint4> chains;      // {first row, rows, record of the first row, 0}
+  dfm2g::DevBuf<unsigned> rec_of;   // record index of each row
+  dfm2g::DevBuf<unsigned char> linked;  // 1 when the row continues its predecessor's chain
+  dfm2g::DevBuf<unsigned char> bytes32, bytes64;
+  dfm2g::DevBuf<unsigned> ctr;      // chain counter and done-ticket of the launch
+};
+
 struct dfm2g_ilu_s {
   unsigned nblk = 0;
   unsigned ndim = 3;  // block size of the matrix the pattern was taken from
@@ -285,6 +299,7 @@ struct dfm2g_ilu_s {
   GroupSched gs_f, gs_b;                // FP32 blob schedules (forward, backward)
   PartSched parts_f, parts_b;           // row-range partitions (forward, backward)
   StreamSched ss32_f, ss32_b, ss64_f, ss64_b;  // level streams of the single-CTA sweep
+  ChainSched cs_f, cs_b;                // chain schedules (forward, backward)
   dfm2g::DevBuf<double> in_lv64;        // right-hand side gathered in level order
   dfm2g::DevBuf<float> in_lv32;
   unsigned factor_version = 0;          // incremented by each decomposition
@@ -330,6 +345,10 @@ template <typename T>
 int stream_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                  unsigned long long timeout, bool *usable);
 void stream_schedules_reset(dfm2g_ilu_s *p);
+template <typename T>
+int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
+                unsigned long long timeout, bool may_alloc, bool *usable);
+void chain_schedules_reset(dfm2g_ilu_s *p);
 template <typename T>
 int part_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout);

@@ -818,7 +818,7 @@ static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, cons
 
 template <typename T>
 static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia,
-                      const int *skip, bool prefilled) {
+                      const int *skip, bool prefilled, bool may_alloc = true) {
   const unsigned n = p->nblk;
   if (n == 0) return DFM2G_OK;
   if (p->ndim == 1) return nd_sweep_impl<T, 1>(p, forward, in, out, vcrs, vdia, skip, prefilled);
@@ -856,8 +856,15 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     return part_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev);
   }
-  // sync-free and blob schedules: `out` is filled with the pending marker
+  // sync-free, chain and blob schedules: `out` is filled with the pending marker
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
+  if (p->sweep_mode == DFM2G_SWEEP_CHAINS) {
+    const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+    bool usable = false;
+    DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
+                             &usable));
+    if (usable) return DFM2G_OK;  // else (records too long for the ring): the sync-free schedule below
+  }
   if constexpr (sizeof(T) == 4) {
     const GroupSched &gs = forward ? p->gs_f : p->gs_b;
     if (p->sweep_mode == DFM2G_SWEEP_GROUPS && gs.ok && gs.values_ok)
@@ -887,6 +894,16 @@ int ilu_sweep(dfm2g_ilu_s *p, int prec, bool forward, const void *in, void *out)
     return sweep_impl<double>(p, forward, (const double *)in, (double *)out, p->vcrs.p, p->vdia.p, nullptr, false);
   DFM2G_TRY(ilu_ensure_f32(p));
   return sweep_impl<float>(p, forward, (const float *)in, (float *)out, p->vcrs32.p, p->vdia32.p, nullptr, false);
+}
+
+// A sweep that allocates nothing: the chain schedule is used only when its
+// records already exist, otherwise the sync-free one. The FP32 factors must exist.
+static int ilu_sweep_noalloc(dfm2g_ilu_s *p, int prec, bool forward, const void *in, void *out) {
+  if (prec == DFM2G_F64)
+    return sweep_impl<double>(p, forward, (const double *)in, (double *)out, p->vcrs.p, p->vdia.p, nullptr, false,
+                              false);
+  return sweep_impl<float>(p, forward, (const float *)in, (float *)out, p->vcrs32.p, p->vdia32.p, nullptr, false,
+                           false);
 }
 
 // Variant for the solver loops: the sweep is skipped once *skip != 0, and in
@@ -1014,6 +1031,7 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, unsigned ndim, size_t nn
   DFM2G_TRY(compute_levels(p, false));
   DFM2G_TRY(compute_levels(p, true));
   stream_schedules_reset(p);
+  chain_schedules_reset(p);
   if (ndim == 3) {  // the blob and row-range schedules are written for 3x3 blocks
     DFM2G_TRY(group_schedules_build(p));
     DFM2G_TRY(part_schedules_build(p));
@@ -1021,10 +1039,10 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, unsigned ndim, size_t nn
     p->gs_f.ok = p->gs_b.ok = false;
     p->parts_ok = false;
   }
-  // The blob schedule is correct but, with one CTA barrier per unit, a single
-  // row waiting on another blob stalls its whole CTA; measured 4.1 ms vs
-  // 0.9 ms per FP32 sweep at 3.24M DOF, so the sync-free schedule is the default.
-  p->sweep_mode = DFM2G_SWEEP_SYNCFREE;
+  // 3x3 blocks default to the chain schedule (FP32 / FP64 forward sweep at
+  // 3.24M DOF on GB300: 0.62 / 1.45 ms, against 0.91 / 2.19 ms sync-free);
+  // 1x1 and 2x2 blocks have the sync-free and level schedules only.
+  p->sweep_mode = ndim == 3 ? DFM2G_SWEEP_CHAINS : DFM2G_SWEEP_SYNCFREE;
   const size_t nvec = (size_t)n * ndim + 1;
   DFM2G_TRY(p->tmp64a.resize(nvec));
   DFM2G_TRY(p->tmp64b.resize(nvec));
@@ -1217,8 +1235,8 @@ int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec) {
   // its own output (the pending marker in the sync-free schedule, a copy of
   // its input in the level schedule), so no scratch content carries over
   // from an earlier call.
-  DFM2G_TRY(ilu_sweep(p, prec, true, vec, scratch));
-  DFM2G_TRY(ilu_sweep(p, prec, false, scratch, vec));
+  DFM2G_TRY(ilu_sweep_noalloc(p, prec, true, vec, scratch));
+  DFM2G_TRY(ilu_sweep_noalloc(p, prec, false, scratch, vec));
   return read_err(p);
 }
 
@@ -1229,7 +1247,7 @@ int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) { return 
 int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
-      mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS)
+      mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
   if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS)
     return fail(DFM2G_ERR_UNSUPPORTED, "sweep mode %d needs 3x3 blocks (the pattern has ndim %u)", mode, p->ndim);

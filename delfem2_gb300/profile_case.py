@@ -1,14 +1,16 @@
 """One static-elasticity solve on a voxel block, for profiler captures.
 
   python -m delfem2_gb300.profile_case [--nx 64 --ny 64 --nz 64] [--fp64] [--solves 1] [--method reliable]
-                                       [--poisson]
+                                       [--poisson] [--sweep-mode M] [--precond K]
 
 Sets the problem up (mesh, pattern, level sets, assembly, ILU(0)) and runs
 `--solves` solves of K u = b to 1e-10 (FP32-inner/FP64-refinement by default,
 with reliable updates or restarted refinement; plain FP64 Solve_PCG with
 --fp64), printing the device time of each. --poisson solves the scalar
 Poisson problem (1x1 blocks) on the same mesh instead: alpha = 1, source = 1,
-the z = 0 face at 0 and the top face at 1.
+the z = 0 face at 0 and the top face at 1. --sweep-mode selects the triangular-sweep
+schedule (a dfm2g_sweep value); --precond K replaces the solves by K FP32
+SolvePrecond calls (forward + backward sweep) on a seeded vector.
 """
 from __future__ import annotations
 
@@ -26,6 +28,8 @@ def main():
     ap.add_argument("--levels", action="store_true", help="level-by-level sweep schedule")
     ap.add_argument("--method", choices=["reliable", "restart"], default="reliable")
     ap.add_argument("--poisson", action="store_true", help="scalar Poisson (1x1 blocks) on the same mesh")
+    ap.add_argument("--sweep-mode", type=int, default=None, help="triangular-sweep schedule (dfm2g_sweep value)")
+    ap.add_argument("--precond", type=int, default=0, help="K FP32 SolvePrecond calls instead of solves")
     args = ap.parse_args()
 
     import torch
@@ -57,7 +61,19 @@ def main():
         assert P.factor()
     if args.levels:
         ilu.set_sweep_mode(N.SWEEP_LEVELS)
+    if args.sweep_mode is not None:
+        ilu.set_sweep_mode(args.sweep_mode)
     torch.cuda.synchronize()
+    if args.precond:
+        gen = torch.Generator(device="cuda").manual_seed(0)
+        v = torch.randn(b.numel(), dtype=torch.float32, device="cuda", generator=gen)
+        for k in range(args.precond):
+            u = v.clone()
+            t = time.perf_counter()
+            ilu.SolvePrecond(u)
+            torch.cuda.synchronize()
+            print(f"precond {k}: {1e3 * (time.perf_counter() - t):.3f} ms, |z| = {float(u.norm()):.6e}")
+        return
     for k in range(args.solves):
         t = time.perf_counter()
         if args.fp64:

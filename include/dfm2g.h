@@ -64,11 +64,17 @@ enum dfm2g_sweep {
                                level-ordered copy of the factors, one barrier
                                per level, recent results in a shared-memory
                                ring (for patterns with few rows per level)   */
-  DFM2G_SWEEP_PARTS = 4     /* sync-free over contiguous row ranges, one CTA
+  DFM2G_SWEEP_PARTS = 4,    /* sync-free over contiguous row ranges, one CTA
                                per range: dependencies inside a range are
                                polled in shared memory, only cross-range ones
                                in global memory (when a range's results fit
                                in shared memory)                            */
+  DFM2G_SWEEP_CHAINS = 5    /* sync-free over chains of consecutive rows in
+                               which each row depends on the one before: one
+                               warp per chain hands that dependency over in
+                               registers and polls only the others; the
+                               chain's factor blocks are TMA-streamed into
+                               shared memory ahead of the warp               */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>       */
@@ -187,11 +193,14 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * ndim*nblk may not exceed 1,048,576 (DFM2G_ERR_ARG otherwise). The first call on
  * a device looks up that array's device address. All calls share the array:
  * calls that overlap on the GPU (other streams, other threads) race. FP32 needs
- * FP32 factors made earlier by a DFM2G_F32 dfm2g_ilu_solve_precond call. */
+ * FP32 factors made earlier by a DFM2G_F32 dfm2g_ilu_solve_precond call.
+ * Under DFM2G_SWEEP_CHAINS the chain records are made by the first ordinary
+ * sweep in each precision; until then this entry point sweeps sync-free. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
 /* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE and DFM2G_SWEEP_LEVELS only. */
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
-/* Current schedule (set_pattern0 picks DFM2G_SWEEP_GROUPS when it fits). */
+/* Current schedule (a new pattern starts with DFM2G_SWEEP_CHAINS for 3x3
+ * blocks, DFM2G_SWEEP_SYNCFREE for 1x1 and 2x2). */
 DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with

@@ -4,7 +4,10 @@ The arrow pattern (row 0 coupled to every row) has two levels per direction:
 the forward sweep's second level reads row 0 from more than a shared-memory
 ring's length back (the single-CTA schedule's global-memory path), and the
 backward sweep's row 0 has n-1 blocks (the long-row paths). The chain pattern
-(tridiagonal blocks) has one row per level (n levels). Tolerance 1e-12
+(tridiagonal blocks) has one row per level (n levels) and is one chain of the
+chain schedule. The random pattern (runs of (i-1, i) couplings plus random
+long-range ones) makes the chain schedule cut chains where a row's other
+dependencies lie in later chains. Tolerance 1e-12
 relative (FP64), 1e-5 (FP32).
 """
 import numpy as np
@@ -19,8 +22,22 @@ def _system(kind, n, seed):
     rng = np.random.default_rng(seed)
     if kind == "arrow":
         nbr = [list(range(1, n))] + [[0] for _ in range(1, n)]
-    else:
+    elif kind == "chain":
         nbr = [[j for j in (i - 1, i + 1) if 0 <= j < n] for i in range(n)]
+    else:  # runs of i-1 couplings cut at random, plus two random couplings per row
+        links = set()
+        for i in range(1, n):
+            if rng.random() < 0.8:
+                links.add((i - 1, i))
+        for i in range(n):
+            for j in rng.integers(0, n, 2):
+                if int(j) != i:
+                    links.add((min(i, int(j)), max(i, int(j))))
+        nbr = [[] for _ in range(n)]
+        for i, j in sorted(links):
+            nbr[i].append(j)
+            nbr[j].append(i)
+        nbr = [sorted(a) for a in nbr]
     ind = np.zeros(n + 1, np.uint32)
     ind[1:] = np.cumsum([len(a) for a in nbr])
     psup = np.array([j for a in nbr for j in a], np.uint32)
@@ -29,8 +46,8 @@ def _system(kind, n, seed):
     return ind, psup, vc, vd
 
 
-@pytest.mark.parametrize("kind,n", [("arrow", 20000), ("chain", 3000)])
-@pytest.mark.parametrize("mode", [0, 1, 3, 4])
+@pytest.mark.parametrize("kind,n", [("arrow", 20000), ("chain", 3000), ("random", 6000)])
+@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5])
 def test_sweep_modes_on_edge_patterns(gpu, port, kind, n, mode):
     import delfem2_gb300 as D
     ind, psup, vc, vd = _system(kind, n, 3)
