@@ -75,6 +75,23 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_bsr_spmv_tma(const unsigned 
                    });
 }
 
+// FP32 product in the component layout (spmv_tma_rows_c).
+__global__ void __launch_bounds__(kTmaThreads, 1) k_bsr_spmv_tma_c(const unsigned *__restrict__ tiles, unsigned ntiles,
+                                                                   const unsigned *__restrict__ row_start,
+                                                                   const unsigned *__restrict__ col,
+                                                                   const float *__restrict__ vcrs,
+                                                                   const float *__restrict__ vdia,
+                                                                   float *__restrict__ y, float alpha,
+                                                                   const float *__restrict__ x, float beta, int *err,
+                                                                   unsigned long long timeout_ns) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  spmv_tma_rows_c(tiles, ntiles, row_start, col, vcrs, vdia, x, err, timeout_ns, tma_smem,
+                  [&](unsigned row, unsigned a, float v) {
+                    float *py = y + (size_t)row * 3 + a;
+                    *py = beta * *py + alpha * v;
+                  });
+}
+
 // Tiles of consecutive rows with at most `maxb` off-diagonal blocks and `maxr`
 // rows each; false when one row alone has more than `maxb` blocks.
 static bool make_tiles(const std::vector<unsigned> &rs, unsigned nblk, unsigned maxb, unsigned maxr,
@@ -95,7 +112,7 @@ static bool make_tiles(const std::vector<unsigned> &rs, unsigned nblk, unsigned 
 int bsr_tiles_build(dfm2g_bsr_s *m) {
   m->tiles_ok = false;
   std::vector<unsigned> t32, t64;
-  if (m->nblk == 0 || !make_tiles(m->h_row_start, m->nblk, TileCfg<float>::kBlocks, TileCfg<float>::kRows, t32) ||
+  if (m->nblk == 0 || !make_tiles(m->h_row_start, m->nblk, TileCfgC::kBlocks, TileCfgC::kRows, t32) ||
       !make_tiles(m->h_row_start, m->nblk, TileCfg<double>::kBlocks, TileCfg<double>::kRows, t64))
     return DFM2G_OK;
   DFM2G_TRY(m->tiles32.resize(t32.size()));
@@ -108,8 +125,8 @@ int bsr_tiles_build(dfm2g_bsr_s *m) {
   DFM2G_CUDA(cudaMemsetAsync(m->err.p, 0, sizeof(int), stream()));
   static int attr_device = -1;  // opt the kernels in to their shared memory once per device
   if (attr_device != ctx().device) {
-    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)TileCfg<float>::kSmem));
+    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma_c, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)TileCfgC::kSmem));
     DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)TileCfg<double>::kSmem));
     attr_device = ctx().device;
@@ -165,8 +182,8 @@ int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, dou
           (const double *)x, beta, m->err.p, timeout);
     } else {
       DFM2G_TRY(bsr_ensure_f32(m));
-      const unsigned grid = std::min(m->ntiles32, (unsigned)ctx().num_sms * 2);
-      k_bsr_spmv_tma<float><<<grid, kTmaThreads, TileCfg<float>::kSmem, stream()>>>(
+      const unsigned grid = std::min(m->ntiles32, (unsigned)ctx().num_sms);
+      k_bsr_spmv_tma_c<<<grid, kTmaThreads, TileCfgC::kSmem, stream()>>>(
           m->tiles32.p, m->ntiles32, m->row_start.p, m->col.p, m->vcrs32.p, m->vdia32.p, (float *)y, (float)alpha,
           (const float *)x, (float)beta, m->err.p, timeout);
     }

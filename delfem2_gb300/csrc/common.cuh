@@ -226,7 +226,7 @@ struct dfm2g_bsr_s {
   dfm2g::DevBuf<float> vcrs32, vdia32;
   bool f32_valid = false;
   unsigned pattern_version = 0;
-  // row tiles of the TMA-staged SpMV (FP32 and FP64 tile sizes); tiles_ok is
+  // row tiles of the TMA-staged SpMV (FP32: component layout, TileCfgC; FP64: TileCfg<double>); tiles_ok is
   // false when a row alone exceeds a tile
   dfm2g::DevBuf<unsigned> tiles32, tiles64;
   unsigned ntiles32 = 0, ntiles64 = 0;

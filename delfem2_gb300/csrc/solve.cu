@@ -104,6 +104,31 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_spmv_pAp_tma(IterState *st, 
   }
 }
 
+// FP32: the same in the component layout of spmv_tma_rows_c.
+__global__ void __launch_bounds__(kTmaThreads, 1) k_spmv_pAp_tma_c(IterState *st, const unsigned *__restrict__ tiles,
+                                                                   unsigned ntiles,
+                                                                   const unsigned *__restrict__ row_start,
+                                                                   const unsigned *__restrict__ col,
+                                                                   const float *__restrict__ vcrs,
+                                                                   const float *__restrict__ vdia,
+                                                                   const float *__restrict__ p,
+                                                                   float *__restrict__ Ap, double *partials,
+                                                                   int *err, unsigned long long timeout_ns) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  __shared__ double sh[32];
+  if (st->done) return;
+  double dot = 0.0;
+  spmv_tma_rows_c(tiles, ntiles, row_start, col, vcrs, vdia, p, err, timeout_ns, tma_smem,
+                  [&](unsigned row, unsigned a, float v) {
+                    Ap[(size_t)row * 3 + a] = v;
+                    dot += (double)(v * p[(size_t)row * 3 + a]);
+                  });
+  double total;
+  if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
+    st->alpha = st->rPr / total;
+  }
+}
+
 // The same for 1x1 and 2x2 blocks (nd.cuh).
 template <typename T, int B>
 __global__ void __launch_bounds__(kThreads) k_spmv_pAp_nd(IterState *st, unsigned nblk,
@@ -136,6 +161,17 @@ static int launch_spmv_pAp(dfm2g_bsr_s *m, IterState *st, const T *vcrs, const T
   } else if (m->ndim == 2) {
     k_spmv_pAp_nd<T, 2><<<spmv_blocks, kThreads, 0, stream()>>>(st, m->nblk, m->row_start.p, m->col.p, vcrs, vdia, pv,
                                                                Ap, partials);
+  } else if (m->tiles_ok && sizeof(T) == 4) {
+    static int attr_device_c = -1;  // once per device
+    if (attr_device_c != ctx().device) {
+      DFM2G_CUDA(cudaFuncSetAttribute(k_spmv_pAp_tma_c, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)TileCfgC::kSmem));
+      attr_device_c = ctx().device;
+    }
+    const unsigned grid = std::min(m->ntiles32, (unsigned)ctx().num_sms);
+    k_spmv_pAp_tma_c<<<grid, kTmaThreads, TileCfgC::kSmem, stream()>>>(
+        st, m->tiles32.p, m->ntiles32, m->row_start.p, m->col.p, (const float *)vcrs, (const float *)vdia,
+        (const float *)pv, (float *)Ap, partials, m->err.p, kWaitTimeoutNs);
   } else if (m->tiles_ok) {
     static int attr_device = -1;  // per instantiation, once per device
     if (attr_device != ctx().device) {
