@@ -55,41 +55,19 @@ __global__ void __launch_bounds__(256) k_bsr_spmv(unsigned nblk, const unsigned 
   });
 }
 
-// Same product through the TMA-staged pipeline of spmv_tma.cuh.
+// Same product in the component layout (spmv_tma_rows_c).
 template <typename T>
-__global__ void __launch_bounds__(kTmaThreads, 2) k_bsr_spmv_tma(const unsigned *__restrict__ tiles, unsigned ntiles,
-                                                                 const unsigned *__restrict__ row_start,
-                                                                 const unsigned *__restrict__ col,
-                                                                 const T *__restrict__ vcrs,
-                                                                 const T *__restrict__ vdia, T *__restrict__ y,
-                                                                 T alpha, const T *__restrict__ x, T beta, int *err,
-                                                                 unsigned long long timeout_ns) {
+__global__ void __launch_bounds__(TileCfgC<T>::kThreads, 1)
+    k_bsr_spmv_tma_c(const unsigned *__restrict__ tiles, unsigned ntiles, const unsigned *__restrict__ row_start,
+                     const unsigned *__restrict__ col, const T *__restrict__ vcrs, const T *__restrict__ vdia,
+                     T *__restrict__ y, T alpha, const T *__restrict__ x, T beta, int *err,
+                     unsigned long long timeout_ns) {
   extern __shared__ __align__(128) unsigned char tma_smem[];
-  const unsigned lane = threadIdx.x & 31;
-  spmv_tma_rows<T>(tiles, ntiles, row_start, col, vcrs, vdia, x, err, timeout_ns, tma_smem,
-                   [&](unsigned row, const T s[3]) {
-                     if (lane < 3) {
-                       T *py = y + (size_t)row * 3 + lane;
-                       *py = beta * *py + alpha * pick3(s, lane);
-                     }
-                   });
-}
-
-// FP32 product in the component layout (spmv_tma_rows_c).
-__global__ void __launch_bounds__(kTmaThreads, 1) k_bsr_spmv_tma_c(const unsigned *__restrict__ tiles, unsigned ntiles,
-                                                                   const unsigned *__restrict__ row_start,
-                                                                   const unsigned *__restrict__ col,
-                                                                   const float *__restrict__ vcrs,
-                                                                   const float *__restrict__ vdia,
-                                                                   float *__restrict__ y, float alpha,
-                                                                   const float *__restrict__ x, float beta, int *err,
-                                                                   unsigned long long timeout_ns) {
-  extern __shared__ __align__(128) unsigned char tma_smem[];
-  spmv_tma_rows_c(tiles, ntiles, row_start, col, vcrs, vdia, x, err, timeout_ns, tma_smem,
-                  [&](unsigned row, unsigned a, float v) {
-                    float *py = y + (size_t)row * 3 + a;
-                    *py = beta * *py + alpha * v;
-                  });
+  spmv_tma_rows_c<T>(tiles, ntiles, row_start, col, vcrs, vdia, x, err, timeout_ns, tma_smem,
+                     [&](unsigned row, unsigned a, T v) {
+                       T *py = y + (size_t)row * 3 + a;
+                       *py = beta * *py + alpha * v;
+                     });
 }
 
 // Tiles of consecutive rows with at most `maxb` off-diagonal blocks and `maxr`
@@ -112,8 +90,9 @@ static bool make_tiles(const std::vector<unsigned> &rs, unsigned nblk, unsigned 
 int bsr_tiles_build(dfm2g_bsr_s *m) {
   m->tiles_ok = false;
   std::vector<unsigned> t32, t64;
-  if (m->nblk == 0 || !make_tiles(m->h_row_start, m->nblk, TileCfgC::kBlocks, TileCfgC::kRows, t32) ||
-      !make_tiles(m->h_row_start, m->nblk, TileCfg<double>::kBlocks, TileCfg<double>::kRows, t64))
+  if (m->nblk == 0 ||
+      !make_tiles(m->h_row_start, m->nblk, TileCfgC<float>::kBlocks, TileCfgC<float>::kRows, t32) ||
+      !make_tiles(m->h_row_start, m->nblk, TileCfgC<double>::kBlocks, TileCfgC<double>::kRows, t64))
     return DFM2G_OK;
   DFM2G_TRY(m->tiles32.resize(t32.size()));
   DFM2G_TRY(m->tiles64.resize(t64.size()));
@@ -125,10 +104,10 @@ int bsr_tiles_build(dfm2g_bsr_s *m) {
   DFM2G_CUDA(cudaMemsetAsync(m->err.p, 0, sizeof(int), stream()));
   static int attr_device = -1;  // opt the kernels in to their shared memory once per device
   if (attr_device != ctx().device) {
-    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma_c, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)TileCfgC::kSmem));
-    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)TileCfg<double>::kSmem));
+    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma_c<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)TileCfgC<float>::kSmem));
+    DFM2G_CUDA(cudaFuncSetAttribute(k_bsr_spmv_tma_c<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)TileCfgC<double>::kSmem));
     attr_device = ctx().device;
   }
   m->ntiles32 = (unsigned)t32.size() - 1;
@@ -176,14 +155,14 @@ int bsr_spmv(dfm2g_bsr_s *m, int prec, void *y, double alpha, const void *x, dou
   if (m->tiles_ok && (prec == DFM2G_F64 || prec == DFM2G_F32)) {
     const unsigned long long timeout = kWaitTimeoutNs;
     if (prec == DFM2G_F64) {
-      const unsigned grid = std::min(m->ntiles64, (unsigned)ctx().num_sms * 2);
-      k_bsr_spmv_tma<double><<<grid, kTmaThreads, TileCfg<double>::kSmem, stream()>>>(
+      const unsigned grid = std::min(m->ntiles64, (unsigned)ctx().num_sms);
+      k_bsr_spmv_tma_c<double><<<grid, TileCfgC<double>::kThreads, TileCfgC<double>::kSmem, stream()>>>(
           m->tiles64.p, m->ntiles64, m->row_start.p, m->col.p, m->vcrs.p, m->vdia.p, (double *)y, alpha,
           (const double *)x, beta, m->err.p, timeout);
     } else {
       DFM2G_TRY(bsr_ensure_f32(m));
       const unsigned grid = std::min(m->ntiles32, (unsigned)ctx().num_sms);
-      k_bsr_spmv_tma_c<<<grid, kTmaThreads, TileCfgC::kSmem, stream()>>>(
+      k_bsr_spmv_tma_c<float><<<grid, TileCfgC<float>::kThreads, TileCfgC<float>::kSmem, stream()>>>(
           m->tiles32.p, m->ntiles32, m->row_start.p, m->col.p, m->vcrs32.p, m->vdia32.p, (float *)y, (float)alpha,
           (const float *)x, (float)beta, m->err.p, timeout);
     }

@@ -74,55 +74,23 @@ __global__ void __launch_bounds__(kThreads) k_spmv_pAp(IterState *st, unsigned n
   }
 }
 
-// Ap = K p and alpha = rPr / (p, Ap) through the TMA-staged pipeline of
-// spmv_tma.cuh (the producer warp contributes 0 to the dot product).
+// The same in the component layout of spmv_tma_rows_c (the default when the
+// pattern has tiles).
 template <typename T>
-__global__ void __launch_bounds__(kTmaThreads, 2) k_spmv_pAp_tma(IterState *st, const unsigned *__restrict__ tiles,
-                                                                 unsigned ntiles,
-                                                                 const unsigned *__restrict__ row_start,
-                                                                 const unsigned *__restrict__ col,
-                                                                 const T *__restrict__ vcrs,
-                                                                 const T *__restrict__ vdia, const T *__restrict__ p,
-                                                                 T *__restrict__ Ap, double *partials, int *err,
-                                                                 unsigned long long timeout_ns) {
-  extern __shared__ __align__(128) unsigned char tma_smem[];
-  __shared__ double sh[32];
-  if (st->done) return;
-  const unsigned lane = threadIdx.x & 31;
-  double dot = 0.0;
-  spmv_tma_rows<T>(tiles, ntiles, row_start, col, vcrs, vdia, p, err, timeout_ns, tma_smem,
-                   [&](unsigned row, const T s[3]) {
-                     if (lane < 3) {
-                       const T v = pick3(s, lane);
-                       Ap[(size_t)row * 3 + lane] = v;
-                       dot += (double)(v * p[(size_t)row * 3 + lane]);
-                     }
-                   });
-  double total;
-  if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
-    st->alpha = st->rPr / total;
-  }
-}
-
-// FP32: the same in the component layout of spmv_tma_rows_c.
-__global__ void __launch_bounds__(kTmaThreads, 1) k_spmv_pAp_tma_c(IterState *st, const unsigned *__restrict__ tiles,
-                                                                   unsigned ntiles,
-                                                                   const unsigned *__restrict__ row_start,
-                                                                   const unsigned *__restrict__ col,
-                                                                   const float *__restrict__ vcrs,
-                                                                   const float *__restrict__ vdia,
-                                                                   const float *__restrict__ p,
-                                                                   float *__restrict__ Ap, double *partials,
-                                                                   int *err, unsigned long long timeout_ns) {
+__global__ void __launch_bounds__(TileCfgC<T>::kThreads, 1)
+    k_spmv_pAp_tma_c(IterState *st, const unsigned *__restrict__ tiles, unsigned ntiles,
+                     const unsigned *__restrict__ row_start, const unsigned *__restrict__ col,
+                     const T *__restrict__ vcrs, const T *__restrict__ vdia, const T *__restrict__ p,
+                     T *__restrict__ Ap, double *partials, int *err, unsigned long long timeout_ns) {
   extern __shared__ __align__(128) unsigned char tma_smem[];
   __shared__ double sh[32];
   if (st->done) return;
   double dot = 0.0;
-  spmv_tma_rows_c(tiles, ntiles, row_start, col, vcrs, vdia, p, err, timeout_ns, tma_smem,
-                  [&](unsigned row, unsigned a, float v) {
-                    Ap[(size_t)row * 3 + a] = v;
-                    dot += (double)(v * p[(size_t)row * 3 + a]);
-                  });
+  spmv_tma_rows_c<T>(tiles, ntiles, row_start, col, vcrs, vdia, p, err, timeout_ns, tma_smem,
+                     [&](unsigned row, unsigned a, T v) {
+                       Ap[(size_t)row * 3 + a] = v;
+                       dot += (double)(v * p[(size_t)row * 3 + a]);
+                     });
   double total;
   if (grid_sum_last(dot, partials, &st->ticket[0], sh, &total)) {
     st->alpha = st->rPr / total;
@@ -161,29 +129,20 @@ static int launch_spmv_pAp(dfm2g_bsr_s *m, IterState *st, const T *vcrs, const T
   } else if (m->ndim == 2) {
     k_spmv_pAp_nd<T, 2><<<spmv_blocks, kThreads, 0, stream()>>>(st, m->nblk, m->row_start.p, m->col.p, vcrs, vdia, pv,
                                                                Ap, partials);
-  } else if (m->tiles_ok && sizeof(T) == 4) {
-    static int attr_device_c = -1;  // once per device
-    if (attr_device_c != ctx().device) {
-      DFM2G_CUDA(cudaFuncSetAttribute(k_spmv_pAp_tma_c, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)TileCfgC::kSmem));
-      attr_device_c = ctx().device;
-    }
-    const unsigned grid = std::min(m->ntiles32, (unsigned)ctx().num_sms);
-    k_spmv_pAp_tma_c<<<grid, kTmaThreads, TileCfgC::kSmem, stream()>>>(
-        st, m->tiles32.p, m->ntiles32, m->row_start.p, m->col.p, (const float *)vcrs, (const float *)vdia,
-        (const float *)pv, (float *)Ap, partials, m->err.p, kWaitTimeoutNs);
   } else if (m->tiles_ok) {
+    using C = TileCfgC<T>;
     static int attr_device = -1;  // per instantiation, once per device
     if (attr_device != ctx().device) {
-      DFM2G_CUDA(cudaFuncSetAttribute(k_spmv_pAp_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)TileCfg<T>::kSmem));
+      DFM2G_CUDA(cudaFuncSetAttribute(k_spmv_pAp_tma_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)C::kSmem));
       attr_device = ctx().device;
     }
     const unsigned nt = sizeof(T) == 8 ? m->ntiles64 : m->ntiles32;
     const unsigned *tiles = sizeof(T) == 8 ? m->tiles64.p : m->tiles32.p;
-    const unsigned grid = std::min(nt, (unsigned)ctx().num_sms * 2);
-    k_spmv_pAp_tma<T><<<grid, kTmaThreads, TileCfg<T>::kSmem, stream()>>>(
-        st, tiles, nt, m->row_start.p, m->col.p, vcrs, vdia, pv, Ap, partials, m->err.p, kWaitTimeoutNs);
+    const unsigned grid = std::min(nt, (unsigned)ctx().num_sms);
+    k_spmv_pAp_tma_c<T><<<grid, C::kThreads, C::kSmem, stream()>>>(st, tiles, nt, m->row_start.p, m->col.p, vcrs,
+                                                                     vdia, pv, Ap, partials, m->err.p,
+                                                                     kWaitTimeoutNs);
   } else {
     k_spmv_pAp<T><<<spmv_blocks, kThreads, 0, stream()>>>(st, m->nblk, m->row_start.p, m->col.p, vcrs, vdia, pv, Ap,
                                                          partials);
