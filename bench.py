@@ -112,8 +112,8 @@ def algorithmic_bytes(kind: str, nb: int, nz: int, s: int) -> float:
         return 9 * s * (nz / 2 + nb) + 4 * nz / 2 + 4 * (3 * nb + 1) + 2 * v3
     if kind == "bwd":       # U' blocks + col/row_start/dia_ind/order, in read, out written
         return 9 * s * (nz / 2) + 4 * nz / 2 + 4 * (3 * nb + 1) + 2 * v3
-    if kind == "update":    # r, x, p, Ap read; r, x written
-        return 6 * v3
+    if kind == "update":    # r, x, p, Ap read; r, x and the sweeps' two pending-marker outputs written
+        return 8 * v3
     if kind == "dot":       # r, z read
         return 2 * v3
     if kind == "pupdate":   # p, z read; p written

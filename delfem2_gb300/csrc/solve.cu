@@ -219,38 +219,77 @@ __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsig
   }
 }
 
-// r -= alpha Ap; x += alpha p; |r|^2 -> history and the stop test.
+// Pending marker of the sync-free sweeps, as a value of type T.
+template <typename T>
+__device__ __forceinline__ T pending_marker() {
+  if constexpr (sizeof(T) == 8)
+    return __longlong_as_double(-1ll);
+  else
+    return __uint_as_float(0xffffffffu);
+}
+
+// r -= alpha Ap; x += alpha p; |r|^2 -> history and the stop test. When fill_a
+// and fill_b are given, both are set to the sweeps' pending marker element by
+// element after Ap is read (Ap may alias fill_a). Four elements per thread and
+// pass, all loads issued before the arithmetic.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T *__restrict__ r, T *__restrict__ x,
-                                                     const T *__restrict__ p, const T *__restrict__ Ap,
-                                                     double *partials, double *hist) {
+                                                     const T *p, const T *Ap, double *partials, double *hist,
+                                                     T *fill_a, T *fill_b) {
   __shared__ double sh[32];
   if (st->done) return;
   const double alpha = st->alpha;
+  const size_t S = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   double rr = 0.0;
-  if (sizeof(T) == 8) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      const double ri = (double)r[i] + (-alpha) * (double)Ap[i];
-      r[i] = (T)ri;
-      x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-      rr += ri * ri;
+  const T pend = pending_marker<T>();
+  auto one = [&](T ri, T xi, T pi, T api, size_t k) -> double {
+    double rn;
+    if constexpr (sizeof(T) == 8) {
+      rn = ri + (-alpha) * api;
+      r[k] = rn;
+      x[k] = xi + alpha * pi;
+    } else {
+      const float a = (float)alpha;
+      const float rf = ri - a * api;
+      r[k] = rf;
+      x[k] = xi + a * pi;
+      rn = rf;
     }
-  } else {
-    const float a = (float)alpha;
-    float acc = 0.f;
-    unsigned k = 0;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      const float ri = (float)r[i] - a * (float)Ap[i];
-      r[i] = (T)ri;
-      x[i] = (T)((float)x[i] + a * (float)p[i]);
-      acc += ri * ri;
-      if (++k == 8) {  // short FP32 runs, accumulated in FP64
-        rr += (double)acc;
-        acc = 0.f;
-        k = 0;
+    if (fill_a) {
+      fill_a[k] = pend;
+      fill_b[k] = pend;
+    }
+    return rn;
+  };
+  for (; i + 3 * S < n; i += 4 * S) {
+    T rv[4], xv[4], pv[4], av[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      av[u] = Ap[i + u * S];
+      rv[u] = r[i + u * S];
+      xv[u] = x[i + u * S];
+      pv[u] = p[i + u * S];
+    }
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const double rn = one(rv[u], xv[u], pv[u], av[u], i + u * S);
+        rr += rn * rn;
       }
+    } else {  // a short FP32 run, accumulated in FP64
+      float acc = 0.f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float rn = (float)one(rv[u], xv[u], pv[u], av[u], i + u * S);
+        acc += rn * rn;
+      }
+      rr += (double)acc;
     }
-    rr += (double)acc;
+  }
+  for (; i < n; i += S) {
+    const double rn = one(r[i], x[i], p[i], Ap[i], i);
+    rr += rn * rn;
   }
   double total;
   if (grid_sum_last(rr, partials, &st->ticket[1], sh, &total)) {
@@ -291,28 +330,33 @@ __global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T 
   }
 }
 
-// rPr1 = (r, Pr); beta = rPr1/rPr.
+// rPr1 = (r, Pr); beta = rPr1/rPr. Four elements per thread and pass.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_dot_beta(IterState *st, size_t n, const T *__restrict__ r,
                                                        const T *__restrict__ z, double *partials) {
   __shared__ double sh[32];
   if (st->done) return;
+  const size_t S = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   double s = 0.0;
-  float acc = 0.f;
-  unsigned k = 0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    if (sizeof(T) == 8) {
-      s += (double)r[i] * (double)z[i];
-    } else {
-      acc += (float)r[i] * (float)z[i];
-      if (++k == 8) {
-        s += (double)acc;
-        acc = 0.f;
-        k = 0;
-      }
+  for (; i + 3 * S < n; i += 4 * S) {
+    T a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = r[i + u * S];
+      b[u] = z[i + u * S];
+    }
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s += a[u] * b[u];
+    } else {  // a short FP32 run, accumulated in FP64
+      float acc = 0.f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc += a[u] * b[u];
+      s += (double)acc;
     }
   }
-  s += (double)acc;
+  for (; i < n; i += S) s += (double)r[i] * (double)z[i];
   double total;
   if (grid_sum_last(s, partials, &st->ticket[2], sh, &total)) {
     // after a rescale of the FP32 vectors, the old p and (r,Pr) are in the old
@@ -324,28 +368,24 @@ __global__ void __launch_bounds__(kThreads) k_dot_beta(IterState *st, size_t n, 
   }
 }
 
-// p = z + beta p
+// p = z + beta p. Four elements per thread and pass.
 template <typename T>
 __global__ void k_p_update(const IterState *st, size_t n, T *__restrict__ p, const T *__restrict__ z) {
   if (st->done) return;
-  const double beta = st->beta;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    if (sizeof(T) == 8)
-      p[i] = (T)(beta * (double)p[i] + (double)z[i]);
-    else
-      p[i] = (T)((float)beta * (float)p[i] + (float)z[i]);
+  const T beta = (T)st->beta;
+  const size_t S = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * S < n; i += 4 * S) {
+    T a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = p[i + u * S];
+      b[u] = z[i + u * S];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[i + u * S] = beta * a[u] + b[u];
   }
-}
-
-template <typename T>
-__global__ void k_fill_pending(const IterState *st, size_t n, T *out) {
-  if (st && st->done) return;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    if (sizeof(T) == 8)
-      reinterpret_cast<unsigned long long *>(out)[i] = ~0ull;
-    else
-      reinterpret_cast<unsigned *>(out)[i] = ~0u;
-  }
+  for (; i < n; i += S) p[i] = beta * p[i] + z[i];
 }
 
 // generic deterministic dot into a device scalar
@@ -517,7 +557,10 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
       }
       {
         ProfScope ps(DFM2G_PROF_UPDATE, 1);
-        k_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, x, pv, Ap, g_ws.partials.p, g_ws.hist.p);
+        // the sweeps' outputs get their pending marker here (Ap is Pr: read first, element by element)
+        const bool fill = mode != 1 && p->sweep_mode != DFM2G_SWEEP_LEVELS;
+        k_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, x, pv, Ap, g_ws.partials.p, g_ws.hist.p,
+                                                           fill ? mid : nullptr, fill ? Pr : nullptr);
       }
       if constexpr (sizeof(T) == 4) {
         if (mode == 2) {
@@ -538,11 +581,6 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
         }
       }
       if (mode != 1) {
-        if (p->sweep_mode != DFM2G_SWEEP_LEVELS) {
-          ProfScope ps(DFM2G_PROF_FILL, 2);
-          k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, mid);
-          k_fill_pending<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, Pr);
-        }
         {
           ProfScope ps(DFM2G_PROF_FWD, 0);
           DFM2G_TRY(ilu_sweep_guarded(p, prec, true, r, mid, &st->done));
