@@ -1,4 +1,4 @@
-// Chain-scheduled sync-free triangular sweep (DFM2G_SWEEP_CHAINS), 3x3 blocks.
+// Chain-scheduled sync-free triangular sweep (DFM2G_SWEEP_CHAINS), 1x1, 2x2 and 3x3 blocks.
 //
 // A chain is a run of consecutive rows i, i+1, ..., i+k (descending in the
 // backward sweep) in which every row depends on the one before it: the last
@@ -67,25 +67,26 @@ struct ChainGeom {
   unsigned m, vo, rec;  // cross blocks per record, offset of the values, record bytes
 };
 
-inline ChainGeom chain_geom(unsigned m, unsigned vs, bool fwd) {
+inline ChainGeom chain_geom(unsigned m, unsigned vs, bool fwd, unsigned B) {
   ChainGeom g;
   g.m = m;
   g.vo = 16u + pad16u(4u * m);
-  g.rec = pad16u(g.vo + (m + (fwd ? 2u : 1u)) * 9u * vs);
+  g.rec = pad16u(g.vo + (m + (fwd ? 2u : 1u)) * B * B * vs);
   return g;
 }
 
 inline size_t chain_smem(unsigned rec) { return (size_t)kChWarps * (kChHead + (size_t)kChSlots * rec); }
 
-template <typename T, unsigned R>
+template <typename T, unsigned NV>
 struct ChainStage {
-  T xv[R];  // the lane's cross values (lane layout of rowkern.cuh)
-  T in[3];  // the row's right-hand side, on every lane
+  T xv[NV];  // the lane's cross values: 3x3, one per round (lane layout of
+             // rowkern.cuh); 1x1 and 2x2, the components of the lane's block
+  T in[3];   // the row's right-hand side (B values), on every lane
 };
 
 // Records of the rows: header, cross columns and values (rec_of[i] = record
 // index of row i, linked[i] = 1 when row i continues its predecessor's chain).
-template <typename T, bool FWD>
+template <typename T, bool FWD, int B>
 __global__ void k_chain_fill(unsigned n, const unsigned *__restrict__ rs, const unsigned *__restrict__ col,
                              const unsigned *__restrict__ dia, const T *__restrict__ vcrs,
                              const T *__restrict__ vdia, const unsigned *__restrict__ rec_of,
@@ -103,11 +104,12 @@ __global__ void k_chain_fill(unsigned n, const unsigned *__restrict__ rs, const 
     unsigned *cols = reinterpret_cast<unsigned *>(rp + 16);
     for (unsigned t = lane; t < nc; t += 32) cols[t] = col[c0 + t];
     T *vals = reinterpret_cast<T *>(rp + vo);
-    for (unsigned e = lane; e < nc * 9u; e += 32) vals[e] = vcrs[(size_t)c0 * 9 + e];
+    constexpr unsigned BB = B * B;
+    for (unsigned e = lane; e < nc * BB; e += 32) vals[e] = vcrs[(size_t)c0 * BB + e];
     const unsigned lb = FWD ? s1 - 1u : s0;  // the block on the chain predecessor
-    if (lane < 9) {
-      vals[(size_t)m * 9 + lane] = lk ? vcrs[(size_t)lb * 9 + lane] : T(0);
-      if (FWD) vals[(size_t)(m + 1) * 9 + lane] = vdia[(size_t)i * 9 + lane];
+    if (lane < BB) {
+      vals[(size_t)m * BB + lane] = lk ? vcrs[(size_t)lb * BB + lane] : T(0);
+      if (FWD) vals[(size_t)(m + 1) * BB + lane] = vdia[(size_t)i * BB + lane];
     }
   }
 }
@@ -115,7 +117,9 @@ __global__ void k_chain_fill(unsigned n, const unsigned *__restrict__ rs, const 
 // chains[c] = {first row, rows, record index of the first row, 0};
 // ctr[0] hands out chain numbers beyond the grid's warps, ctr[1] counts the
 // warps that are done (the last one resets both for the next launch).
-template <typename T, bool FWD, unsigned R>
+// B = 3 uses the lane layout of rowkern.cuh (R rounds of three blocks);
+// B = 1, 2 give each lane one cross block (32 per pass; R unused).
+template <typename T, bool FWD, int B, unsigned R>
 __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, const uint4 *__restrict__ chains,
                                                             const unsigned char *__restrict__ bytes, unsigned rec,
                                                             unsigned m, unsigned vo, const T *in, T *out,
@@ -176,7 +180,8 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
     };
 
     // ---- issue the loads of row u (its record must have landed)
-    auto poll = [&](unsigned u, ChainStage<T, R> &S) {
+    constexpr unsigned NV = B == 3 ? R : (unsigned)B;
+    auto poll = [&](unsigned u, ChainStage<T, NV> &S) {
       const unsigned s = u % kChSlots;
       if (!mbar_wait_bounded(&bar[s], (u / kChSlots) & 1u, timeout_ns)) {
         atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
@@ -186,38 +191,96 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
       const unsigned ncr = *reinterpret_cast<const unsigned *>(rp);
       const unsigned *cols = reinterpret_cast<const unsigned *>(rp + 16);
       const unsigned row = smeta[s].x;
+      if constexpr (B == 3) {
 #pragma unroll
-      for (unsigned k = 0; k < R; ++k) {
-        const unsigned blk = 3u * k + L.g;
-        S.xv[k] = T(0);
-        if (L.active && blk < ncr) S.xv[k] = ld_relaxed(out + (size_t)cols[blk] * 3 + L.c);
+        for (unsigned k = 0; k < R; ++k) {
+          const unsigned blk = 3u * k + L.g;
+          S.xv[k] = T(0);
+          if (L.active && blk < ncr) S.xv[k] = ld_relaxed(out + (size_t)cols[blk] * 3 + L.c);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+          S.xv[c] = T(0);
+          if (lane < ncr) S.xv[c] = ld_relaxed(out + (size_t)cols[lane] * B + c);
+        }
       }
 #pragma unroll
-      for (unsigned c = 0; c < 3; ++c) S.in[c] = in[(size_t)row * 3 + c];
+      for (int c = 0; c < B; ++c) S.in[c] = in[(size_t)row * B + c];
     };
 
     // ---- finish row t: wait for its cross values, reduce, chain step, store
     T zp0 = T(0), zp1 = T(0), zp2 = T(0);
-    auto finish = [&](unsigned t, ChainStage<T, R> &S) {
+    // 1x1 and 2x2 blocks: each lane's block row sums, the warp sum, then the
+    // chain step on every lane (zp0, zp1 hold the predecessor's values)
+    auto finish_nd = [&](unsigned ncr, const unsigned *cols, const T *vals, uint2 sm, ChainStage<T, NV> &S) {
+      constexpr unsigned BB = (unsigned)(B * B);
+      T acc[2] = {T(0), T(0)};
+      if (lane < ncr) {
+        const T *a = vals + (size_t)lane * BB;
+#pragma unroll
+        for (int r = 0; r < B; ++r)
+#pragma unroll
+          for (int c = 0; c < B; ++c) acc[r] += a[r * B + c] * S.xv[c];
+      }
+      for (unsigned blk = 32u + lane; blk < ncr; blk += 32u) {  // more than 32 cross blocks: read inline
+        const T *a = vals + (size_t)blk * BB;
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+          const T x = abort ? T(0) : wait_value(out + (size_t)cols[blk] * B + c, err, timeout_ns);
+#pragma unroll
+          for (int r = 0; r < B; ++r) acc[r] += a[r * B + c] * x;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < B; ++r) acc[r] = warp_sum(acc[r]);
+      if (sm.y) zp0 = zp1 = T(0);
+      const T *lc = vals + (size_t)m * BB;
+      T u[2];
+      if constexpr (B == 1) {
+        u[0] = S.in[0] - acc[0] - lc[0] * zp0;
+        zp0 = FWD ? vals[(size_t)(m + 1)] * u[0] : u[0];
+      } else {
+        u[0] = S.in[0] - acc[0] - (lc[0] * zp0 + lc[1] * zp1);
+        u[1] = S.in[1] - acc[1] - (lc[2] * zp0 + lc[3] * zp1);
+        if (FWD) {
+          const T *d = vals + (size_t)(m + 1) * BB;
+          zp0 = d[0] * u[0] + d[1] * u[1];
+          zp1 = d[2] * u[0] + d[3] * u[1];
+        } else {
+          zp0 = u[0];
+          zp1 = u[1];
+        }
+      }
+      if (lane < (unsigned)B) st_relaxed(out + (size_t)sm.x * B + lane, lane == 0 ? zp0 : zp1);
+    };
+    auto finish = [&](unsigned t, ChainStage<T, NV> &S) {
       const unsigned s = t % kChSlots;
       const unsigned char *rp = slots + (size_t)s * rec;
       const unsigned ncr = *reinterpret_cast<const unsigned *>(rp);
       const unsigned *cols = reinterpret_cast<const unsigned *>(rp + 16);
       const T *vals = reinterpret_cast<const T *>(rp + vo);
       const uint2 sm = smeta[s];
+      // address of the lane's cross value k (pending ones are re-read)
+      auto xaddr = [&](unsigned k) -> const T * {
+        if constexpr (B == 3)
+          return out + (size_t)cols[3u * k + L.g] * 3 + L.c;
+        else
+          return out + (size_t)cols[lane] * B + k;
+      };
       bool pend = false;
 #pragma unroll
-      for (unsigned k = 0; k < R; ++k) pend |= is_pending(S.xv[k]);
+      for (unsigned k = 0; k < NV; ++k) pend |= is_pending(S.xv[k]);
       if (pend && !abort) {
         const unsigned long long t0 = globaltimer_ns();
         unsigned spins = 0;
         for (;;) {
 #pragma unroll
-          for (unsigned k = 0; k < R; ++k)
-            if (is_pending(S.xv[k])) S.xv[k] = ld_relaxed(out + (size_t)cols[3u * k + L.g] * 3 + L.c);
+          for (unsigned k = 0; k < NV; ++k)
+            if (is_pending(S.xv[k])) S.xv[k] = ld_relaxed(xaddr(k));
           pend = false;
 #pragma unroll
-          for (unsigned k = 0; k < R; ++k) pend |= is_pending(S.xv[k]);
+          for (unsigned k = 0; k < NV; ++k) pend |= is_pending(S.xv[k]);
           if (!pend) break;
           if ((++spins & 15u) == 0 && (ld_relaxed(err) != 0 || globaltimer_ns() - t0 > timeout_ns)) {
             atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
@@ -228,8 +291,12 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
       }
       if (abort) {
 #pragma unroll
-        for (unsigned k = 0; k < R; ++k)
+        for (unsigned k = 0; k < NV; ++k)
           if (is_pending(S.xv[k])) S.xv[k] = T(0);
+      }
+      if constexpr (B < 3) {
+        finish_nd(ncr, cols, vals, sm, S);
+        return;
       }
       T acc = T(0);
 #pragma unroll
@@ -291,11 +358,11 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
     // load is still in flight waits for the load, which would put a round
     // trip to L2 back on every row.)
     constexpr unsigned NST = kChLook + 1;
-    ChainStage<T, R> st[NST];
+    ChainStage<T, NV> st[NST];
 #pragma unroll
     for (unsigned k = 0; k < NST; ++k) {
 #pragma unroll
-      for (unsigned q = 0; q < R; ++q) st[k].xv[q] = T(0);
+      for (unsigned q = 0; q < NV; ++q) st[k].xv[q] = T(0);
       st[k].in[0] = st[k].in[1] = st[k].in[2] = T(0);
       if (k < kChLook && k < issued) poll(k, st[k]);
     }
@@ -395,10 +462,27 @@ int chain_build(dfm2g_ilu_s *p, bool fwd, ChainSched &cs) {
 }
 
 template <typename T, bool FWD>
-void *chain_kernel(unsigned m) {
-  if (m <= 6) return (void *)k_sweep_chain<T, FWD, 2>;
-  if (m <= 12) return (void *)k_sweep_chain<T, FWD, 4>;
-  return (void *)k_sweep_chain<T, FWD, 8>;
+void *chain_kernel(unsigned m, unsigned B) {
+  if (B == 1) return (void *)k_sweep_chain<T, FWD, 1, 1>;
+  if (B == 2) return (void *)k_sweep_chain<T, FWD, 2, 1>;
+  if (m <= 6) return (void *)k_sweep_chain<T, FWD, 3, 2>;
+  if (m <= 12) return (void *)k_sweep_chain<T, FWD, 3, 4>;
+  return (void *)k_sweep_chain<T, FWD, 3, 8>;
+}
+
+template <typename T, bool FWD>
+void chain_fill_launch(unsigned B, unsigned blocks, dfm2g_ilu_s *p, const T *vcrs, const T *vdia,
+                       const ChainSched &cs, unsigned char *bytes, const ChainGeom &g) {
+  const unsigned n = p->nblk;
+  if (B == 1)
+    k_chain_fill<T, FWD, 1><<<blocks, 256, 0, stream()>>>(n, p->row_start.p, p->col.p, p->dia_ind.p, vcrs, vdia,
+                                                          cs.rec_of.p, cs.linked.p, bytes, g.rec, g.m, g.vo);
+  else if (B == 2)
+    k_chain_fill<T, FWD, 2><<<blocks, 256, 0, stream()>>>(n, p->row_start.p, p->col.p, p->dia_ind.p, vcrs, vdia,
+                                                          cs.rec_of.p, cs.linked.p, bytes, g.rec, g.m, g.vo);
+  else
+    k_chain_fill<T, FWD, 3><<<blocks, 256, 0, stream()>>>(n, p->row_start.p, p->col.p, p->dia_ind.p, vcrs, vdia,
+                                                          cs.rec_of.p, cs.linked.p, bytes, g.rec, g.m, g.vo);
 }
 
 DevBuf<unsigned char> &chain_bytes(ChainSched &cs, double) { return cs.bytes64; }
@@ -422,7 +506,8 @@ int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs
   }
   if (!cs.ok) return DFM2G_OK;
   const bool f64 = sizeof(T) == 8;
-  const ChainGeom g = chain_geom(cs.m, (unsigned)sizeof(T), forward);
+  const unsigned B = p->ndim;
+  const ChainGeom g = chain_geom(cs.m, (unsigned)sizeof(T), forward, B);
   if (g.rec > kChMaxRecord) return DFM2G_OK;
   const unsigned n = p->nblk;
   DevBuf<unsigned char> &bytes = chain_bytes(cs, T(0));
@@ -434,16 +519,14 @@ int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs
   if (ver != p->factor_version) {
     const unsigned blocks = blocks_for((size_t)n * 32, 256, ctx().num_sms * 16);
     if (forward)
-      k_chain_fill<T, true><<<blocks, 256, 0, stream()>>>(n, p->row_start.p, p->col.p, p->dia_ind.p, vcrs, vdia,
-                                                          cs.rec_of.p, cs.linked.p, bytes.p, g.rec, g.m, g.vo);
+      chain_fill_launch<T, true>(B, blocks, p, vcrs, vdia, cs, bytes.p, g);
     else
-      k_chain_fill<T, false><<<blocks, 256, 0, stream()>>>(n, p->row_start.p, p->col.p, p->dia_ind.p, vcrs, vdia,
-                                                           cs.rec_of.p, cs.linked.p, bytes.p, g.rec, g.m, g.vo);
+      chain_fill_launch<T, false>(B, blocks, p, vcrs, vdia, cs, bytes.p, g);
     DFM2G_LAUNCH_CHECK();
     note_launches(1);
     ver = p->factor_version;
   }
-  void *kernel = forward ? chain_kernel<T, true>(cs.m) : chain_kernel<T, false>(cs.m);
+  void *kernel = forward ? chain_kernel<T, true>(cs.m, B) : chain_kernel<T, false>(cs.m, B);
   const size_t smem = chain_smem(g.rec);
   int &cap = cs.coop[f64 ? 1 : 0];
   if (cap <= 0) {

@@ -774,7 +774,7 @@ static int coop_blocks(const void *kernel, int *cache) {
 
 template <typename T, int B>
 static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia,
-                         const int *skip, bool prefilled) {
+                         const int *skip, bool prefilled, bool may_alloc) {
   const unsigned n = p->nblk;
   const uint4 *meta = forward ? p->meta_f.p : p->meta_b.p;
   if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
@@ -800,6 +800,13 @@ static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, cons
   }
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * B, stream()));
+  if (p->sweep_mode == DFM2G_SWEEP_CHAINS) {
+    const unsigned nlev_c = forward ? p->nlev_f : p->nlev_b;
+    bool usable = false;
+    DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev_c, may_alloc,
+                             &usable));
+    if (usable) return DFM2G_OK;  // else (records too long for the ring): the sync-free schedule below
+  }
   void *kernel = forward ? (void *)k_sweep_syncfree_nd<T, true, B> : (void *)k_sweep_syncfree_nd<T, false, B>;
   int *cache = &p->coop_cache[sizeof(T) == 8 ? 1 : 0][forward ? 1 : 0][0];
   DFM2G_TRY(coop_blocks<T>(kernel, cache));
@@ -821,8 +828,8 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
                       const int *skip, bool prefilled, bool may_alloc = true) {
   const unsigned n = p->nblk;
   if (n == 0) return DFM2G_OK;
-  if (p->ndim == 1) return nd_sweep_impl<T, 1>(p, forward, in, out, vcrs, vdia, skip, prefilled);
-  if (p->ndim == 2) return nd_sweep_impl<T, 2>(p, forward, in, out, vcrs, vdia, skip, prefilled);
+  if (p->ndim == 1) return nd_sweep_impl<T, 1>(p, forward, in, out, vcrs, vdia, skip, prefilled, may_alloc);
+  if (p->ndim == 2) return nd_sweep_impl<T, 2>(p, forward, in, out, vcrs, vdia, skip, prefilled, may_alloc);
   if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
     // levels in order; rows of one level are independent (in == out allowed)
     if (in != out) {
@@ -1039,10 +1046,10 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, unsigned ndim, size_t nn
     p->gs_f.ok = p->gs_b.ok = false;
     p->parts_ok = false;
   }
-  // 3x3 blocks default to the chain schedule (FP32 / FP64 forward sweep at
-  // 3.24M DOF on GB300: 0.62 / 1.45 ms, against 0.91 / 2.19 ms sync-free);
-  // 1x1 and 2x2 blocks have the sync-free and level schedules only.
-  p->sweep_mode = ndim == 3 ? DFM2G_SWEEP_CHAINS : DFM2G_SWEEP_SYNCFREE;
+  // The chain schedule is the default (3x3, 3.24M DOF on GB300, FP32 / FP64
+  // forward sweep: 0.62 / 1.45 ms against 0.91 / 2.19 ms sync-free; scalar
+  // Poisson on the same mesh: mixed solve 165 ms against 225 ms).
+  p->sweep_mode = DFM2G_SWEEP_CHAINS;
   const size_t nvec = (size_t)n * ndim + 1;
   DFM2G_TRY(p->tmp64a.resize(nvec));
   DFM2G_TRY(p->tmp64b.resize(nvec));
@@ -1249,7 +1256,7 @@ int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
       mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
-  if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS)
+  if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_CHAINS)
     return fail(DFM2G_ERR_UNSUPPORTED, "sweep mode %d needs 3x3 blocks (the pattern has ndim %u)", mode, p->ndim);
   if (mode == DFM2G_SWEEP_PARTS && !p->parts_ok)
     return fail(DFM2G_ERR_UNSUPPORTED, "row-range partition unavailable for this pattern");

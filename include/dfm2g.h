@@ -197,10 +197,9 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * Under DFM2G_SWEEP_CHAINS the chain records are made by the first ordinary
  * sweep in each precision; until then this entry point sweeps sync-free. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
-/* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE and DFM2G_SWEEP_LEVELS only. */
+/* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE, DFM2G_SWEEP_LEVELS and DFM2G_SWEEP_CHAINS. */
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
-/* Current schedule (a new pattern starts with DFM2G_SWEEP_CHAINS for 3x3
- * blocks, DFM2G_SWEEP_SYNCFREE for 1x1 and 2x2). */
+/* Current schedule (a new pattern starts with DFM2G_SWEEP_CHAINS). */
 DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
