@@ -159,6 +159,37 @@ __global__ void k_flush_x(const IterState *st, size_t n, double *__restrict__ x6
   }
 }
 
+// End of a refresh: |b - K x64|^2 (rr) and |true - recursive residual|^2 (dd)
+// summed over the grid; the last block updates the iteration state. The
+// block sums of dd go to partials[gridDim.x + block] (written before
+// grid_sum_last's fence); the last block adds them in block order.
+__device__ __forceinline__ void refresh_tail(IterState *st, double rr, double dd, double *partials, double *sh,
+                                             double *sh2) {
+  dd = block_sum(dd, sh2);
+  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = dd;
+  double total;
+  if (grid_sum_last(rr, partials, &st->ticket[3], sh, &total)) {
+    const double rt = sqrt(total);
+    double gap2 = 0.0;
+    for (unsigned b2 = 0; b2 < gridDim.x; ++b2) gap2 += ld_relaxed(partials + gridDim.x + b2);
+    st->restart_p = sqrt(gap2) > 0.5 * rt ? 1 : 0;
+    st->rtrue = rt;
+    st->update = 0;
+    st->n_updates++;
+    if (!isfinite(rt)) {
+      st->done = 4;
+    } else if (rt < st->tol * st->bnorm) {
+      st->done = 1;
+    } else if (st->it >= st->max_iter) {
+      st->done = 2;
+    } else {
+      st->rmax = rt;
+    }
+    st->ratio = st->scale_next / st->scale;
+    st->scale = st->scale_next;
+  }
+}
+
 // Reliable update, part 2: r64 = b - K64 x64 in FP64, r32 = (float) r64, and
 // |r64| decides convergence (|r64| < tol |b|) or the next refresh threshold.
 // B = 3 runs the 3x3 row product of rowkern.cuh, B = 1, 2 that of nd.cuh.
@@ -192,31 +223,33 @@ __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsig
     spmv_rows(nblk, row_start, col, vcrs, vdia, x64, [&](unsigned row, const double s[3]) { row_done(row, s, lane); });
   else
     nd_spmv_rows<double, B>(nblk, row_start, col, vcrs, vdia, x64, row_done);
-  // |true - recursive|^2: block sums go to partials[gridDim.x + block] (written
-  // before grid_sum_last's fence), the last block adds them in block order
-  dd = block_sum(dd, sh2);
-  if (threadIdx.x == 0) partials[gridDim.x + blockIdx.x] = dd;
-  double total;
-  if (grid_sum_last(rr, partials, &st->ticket[3], sh, &total)) {
-    const double rt = sqrt(total);
-    double gap2 = 0.0;
-    for (unsigned b2 = 0; b2 < gridDim.x; ++b2) gap2 += ld_relaxed(partials + gridDim.x + b2);
-    st->restart_p = sqrt(gap2) > 0.5 * rt ? 1 : 0;
-    st->rtrue = rt;
-    st->update = 0;
-    st->n_updates++;
-    if (!isfinite(rt)) {
-      st->done = 4;
-    } else if (rt < st->tol * st->bnorm) {
-      st->done = 1;
-    } else if (st->it >= st->max_iter) {
-      st->done = 2;
-    } else {
-      st->rmax = rt;
-    }
-    st->ratio = st->scale_next / st->scale;
-    st->scale = st->scale_next;
-  }
+  refresh_tail(st, rr, dd, partials, sh, sh2);
+}
+
+// The same product through the TMA-staged component-layout pipeline
+// (spmv_tma_rows_c<double>), for 3x3 patterns with tiles.
+__global__ void __launch_bounds__(TileCfgC<double>::kThreads, 1)
+    k_true_residual_tma(IterState *st, const unsigned *__restrict__ tiles, unsigned ntiles,
+                        const unsigned *__restrict__ row_start, const unsigned *__restrict__ col,
+                        const double *__restrict__ vcrs, const double *__restrict__ vdia,
+                        const double *__restrict__ x64, const double *__restrict__ b, float *__restrict__ r32,
+                        double *partials, int *err, unsigned long long timeout_ns) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  __shared__ double sh[32];
+  __shared__ double sh2[32];
+  if (st->done || !st->update) return;
+  const double sc = st->scale_next, inv_old = 1.0 / st->scale;
+  double rr = 0.0, dd = 0.0;
+  spmv_tma_rows_c<double>(tiles, ntiles, row_start, col, vcrs, vdia, x64, err, timeout_ns, tma_smem,
+                          [&](unsigned row, unsigned a, double v) {
+                            const size_t k = (size_t)row * 3 + a;
+                            const double r = b[k] - v;
+                            const double gap = r - (double)r32[k] * inv_old;  // true minus recursive residual
+                            r32[k] = (float)(r * sc);
+                            rr += r * r;
+                            dd += gap * gap;
+                          });
+  refresh_tail(st, rr, dd, partials, sh, sh2);
 }
 
 // Pending marker of the sync-free sweeps, as a value of type T.
@@ -566,7 +599,19 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
         if (mode == 2) {
           ProfScope ps(DFM2G_PROF_OUTER, 2);
           k_flush_x<<<vec_blocks, kThreads, 0, stream()>>>(st, n, rf.x64, (float *)x);
-          if (m->ndim == 3)
+          if (m->ndim == 3 && m->tiles_ok) {
+            using C = TileCfgC<double>;
+            static int attr_device = -1;  // once per device
+            if (attr_device != ctx().device) {
+              DFM2G_CUDA(cudaFuncSetAttribute(k_true_residual_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)C::kSmem));
+              attr_device = ctx().device;
+            }
+            k_true_residual_tma<<<std::min(m->ntiles64, (unsigned)ctx().num_sms), C::kThreads, C::kSmem,
+                                  stream()>>>(st, m->tiles64.p, m->ntiles64, m->row_start.p, m->col.p, m->vcrs.p,
+                                              m->vdia.p, rf.x64, rf.b64, (float *)r, g_ws.partials.p, m->err.p,
+                                              kWaitTimeoutNs);
+          } else if (m->ndim == 3)
             k_true_residual<3><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p,
                                                                        m->vcrs.p, m->vdia.p, rf.x64, rf.b64,
                                                                        (float *)r, g_ws.partials.p);
