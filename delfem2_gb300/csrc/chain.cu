@@ -107,8 +107,11 @@ __global__ void k_chain_fill(unsigned n, const unsigned *__restrict__ rs, const 
     constexpr unsigned BB = B * B;
     for (unsigned e = lane; e < nc * BB; e += 32) vals[e] = vcrs[(size_t)c0 * BB + e];
     const unsigned lb = FWD ? s1 - 1u : s0;  // the block on the chain predecessor
+    // FP64 3x3 records keep it right after the cross blocks (the sweep sums it
+    // with them); the others in slot m
+    const unsigned lslot = (sizeof(T) == 8 && B == 3) ? nc : m;
     if (lane < BB) {
-      vals[(size_t)m * BB + lane] = lk ? vcrs[(size_t)lb * BB + lane] : T(0);
+      vals[(size_t)lslot * BB + lane] = lk ? vcrs[(size_t)lb * BB + lane] : T(0);
       if (FWD) vals[(size_t)(m + 1) * BB + lane] = vdia[(size_t)i * BB + lane];
     }
   }
@@ -298,6 +301,44 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
         finish_nd(ncr, cols, vals, sm, S);
         return;
       }
+      if constexpr (sizeof(T) == 8) {
+        // FP64: the block on the chain predecessor (record slot ncr, x = zp)
+        // and -in join the row's reduction, and D^-1 is applied to the
+        // reduced sums on lanes 0..2: s = L x + Lc zp - in, z = -D^-1 s
+        // (forward) or -s (backward). Fewer FP64 instructions per row than
+        // a separate chain step (GB300's FP64 pipe is narrow).
+        if (sm.y) zp0 = zp1 = zp2 = T(0);
+        const T zpa[3] = {zp0, zp1, zp2};
+        T acc = (L.g == 0 && L.c == 0) ? -pick3(S.in, L.r) : T(0);
+#pragma unroll
+        for (unsigned k = 0; k < R; ++k) {
+          const unsigned blk = 3u * k + L.g;
+          if (L.active && blk <= ncr)
+            acc += vals[(size_t)blk * 9 + L.e] * (blk < ncr ? S.xv[k] : pick3(zpa, L.c));
+        }
+        if (ncr + 1u > 3u * R && L.active) {  // longer than the registers: read inline
+          for (unsigned blk = 3u * R + L.g; blk <= ncr; blk += 3u) {
+            const T x = blk == ncr ? pick3(zpa, L.c)
+                                   : (abort ? T(0) : wait_value(out + (size_t)cols[blk] * 3 + L.c, err, timeout_ns));
+            acc += vals[(size_t)blk * 9 + L.e] * x;
+          }
+        }
+        T s3[3];
+        row_reduce(acc, s3);
+        const unsigned a = lane < 3 ? lane : 2u;
+        T za;
+        if (FWD) {
+          const T *d = vals + (size_t)(m + 1) * 9 + a * 3;
+          za = -(d[0] * s3[0] + d[1] * s3[1] + d[2] * s3[2]);
+        } else {
+          za = -pick3(s3, a);
+        }
+        if (lane < 3) st_relaxed(out + (size_t)sm.x * 3 + lane, za);
+        zp0 = __shfl_sync(0xffffffffu, za, 0);
+        zp1 = __shfl_sync(0xffffffffu, za, 1);
+        zp2 = __shfl_sync(0xffffffffu, za, 2);
+        return;
+      }
       T acc = T(0);
 #pragma unroll
       for (unsigned k = 0; k < R; ++k) {
@@ -314,25 +355,7 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
       row_reduce(acc, s3);
       if (sm.y) zp0 = zp1 = zp2 = T(0);
       const T *lc = vals + (size_t)m * 9;
-      if constexpr (sizeof(T) == 8) {
-        // FP64: lane a < 3 computes component a (GB300's FP64 pipe is narrow,
-        // so the step is not repeated on every lane); the others compute a
-        // copy of component 2 and discard it.
-        const unsigned a = lane < 3 ? lane : 2u;
-        const T *la = lc + a * 3;
-        const T ua = pick3(S.in, a) - pick3(s3, a) - (la[0] * zp0 + la[1] * zp1 + la[2] * zp2);
-        T za = ua;
-        if (FWD) {
-          const T u0 = __shfl_sync(0xffffffffu, ua, 0), u1 = __shfl_sync(0xffffffffu, ua, 1),
-                  u2 = __shfl_sync(0xffffffffu, ua, 2);
-          const T *d = vals + (size_t)(m + 1) * 9 + a * 3;
-          za = d[0] * u0 + d[1] * u1 + d[2] * u2;
-        }
-        if (lane < 3) st_relaxed(out + (size_t)sm.x * 3 + lane, za);
-        zp0 = __shfl_sync(0xffffffffu, za, 0);
-        zp1 = __shfl_sync(0xffffffffu, za, 1);
-        zp2 = __shfl_sync(0xffffffffu, za, 2);
-      } else {
+      {
         // FP32: every lane computes all three components (no shuffle on the
         // row-to-row path)
         const T u0 = S.in[0] - s3[0] - (lc[0] * zp0 + lc[1] * zp1 + lc[2] * zp2);
@@ -465,8 +488,11 @@ template <typename T, bool FWD>
 void *chain_kernel(unsigned m, unsigned B) {
   if (B == 1) return (void *)k_sweep_chain<T, FWD, 1, 1>;
   if (B == 2) return (void *)k_sweep_chain<T, FWD, 2, 1>;
-  if (m <= 6) return (void *)k_sweep_chain<T, FWD, 3, 2>;
-  if (m <= 12) return (void *)k_sweep_chain<T, FWD, 3, 4>;
+  // FP64 sums the chain predecessor's block with the cross blocks
+  const unsigned need = sizeof(T) == 8 ? m + 1 : m;
+  if (need <= 6) return (void *)k_sweep_chain<T, FWD, 3, 2>;
+  if (need <= 9 && sizeof(T) == 8) return (void *)k_sweep_chain<T, FWD, 3, 3>;
+  if (need <= 12) return (void *)k_sweep_chain<T, FWD, 3, 4>;
   return (void *)k_sweep_chain<T, FWD, 3, 8>;
 }
 
