@@ -55,11 +55,14 @@ namespace {
 constexpr unsigned kChThreads = 128;
 constexpr unsigned kChWarps = kChThreads / 32;
 constexpr unsigned kChSlots = 12;     // records in flight per warp
+constexpr unsigned kChGroup = 4;      // records per copy group (one mbarrier each)
+constexpr unsigned kChGroups = kChSlots / kChGroup;
 constexpr unsigned kChLook = 3;       // rows whose polls are issued ahead
 constexpr unsigned kChHead = 256;     // per-warp barriers and slot rows
 constexpr unsigned kChGrabLead = 8;   // rows before a chain's end at which the next chain is taken
 constexpr unsigned kChMaxRecord = 4096;
 static_assert(kChSlots * (8 + 8) <= kChHead, "slot barriers and slot rows must fit the per-warp header");
+static_assert(kChSlots % kChGroup == 0, "whole copy groups");
 
 inline unsigned pad16u(unsigned x) { return (x + 15u) & ~15u; }
 
@@ -139,7 +142,7 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
   unsigned char *slots = wb + kChHead;
   if (w < nchain) {
     if (lane == 0) {
-      for (unsigned s = 0; s < kChSlots; ++s) mbar_init(&bar[s], 1);
+      for (unsigned g = 0; g < kChGroups; ++g) mbar_init(&bar[g], 1);
       mbar_fence_init();
     }
     __syncwarp();
@@ -147,22 +150,16 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
     bool abort = false;
 
     // ---- producer: lane 0 copies the records of this warp's rows, in order,
-    // into the slot ring (cp.async.bulk)
+    // into the slot ring (cp.async.bulk), kChGroup slots per copy group and
+    // mbarrier (a group's rows from one chain are one contiguous copy)
     // The next chain is taken from the counter only kChGrabLead rows before
     // the producer reaches the end of the current one (its number is read
     // kChGrabLead / 2 rows later), so chains go to warps in the order the
     // warps become free: a chain taken early could wait behind a long one.
     unsigned pc = w, pt = 0, issued = 0, grabbed = 0, nc = nchain, next_state = 0;  // 0 none, 1 taken, 2 read
     uint4 pd = chains[pc], nd = make_uint4(0u, 0u, 0u, 0u);
-    auto produce = [&]() {
-      if (pc >= nchain) return;
-      const unsigned s = issued % kChSlots;
-      if (lane == 0) {
-        smeta[s] = make_uint2(FWD ? pd.x + pt : pd.x - pt, pt == 0 ? 1u : 0u);
-        // relaxed: a release here would wait for this warp's polls in flight
-        mbar_arrive_expect_tx_relaxed(&bar[s], rec);
-        tma_load_1d(slots + (size_t)s * rec, bytes + (size_t)(pd.z + pt) * rec, rec, &bar[s]);
-      }
+    // advances the cursor by one row (taking the next chain when it ends)
+    auto advance = [&]() {
       ++issued;
       ++pt;
       if (next_state == 0 && pt + kChGrabLead >= pd.y) {
@@ -181,12 +178,47 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
         next_state = 0;
       }
     };
+    // fills the next copy group with up to kChGroup rows
+    auto produce = [&]() {
+      if (pc >= nchain) return;
+      const unsigned s0 = issued % kChSlots, g = s0 / kChGroup;
+      unsigned ri[kChGroup];  // record index of each row of the group (~0u: none)
+      unsigned total = 0;
+#pragma unroll
+      for (unsigned q = 0; q < kChGroup; ++q) {
+        ri[q] = ~0u;
+        if (pc < nchain) {
+          ri[q] = pd.z + pt;
+          if (lane == 0) smeta[s0 + q] = make_uint2(FWD ? pd.x + pt : pd.x - pt, pt == 0 ? 1u : 0u);
+          ++total;
+          advance();
+        }
+      }
+      if (lane == 0) {
+        // relaxed: a release here would wait for this warp's polls in flight
+        mbar_arrive_expect_tx_relaxed(&bar[g], total * rec);
+        // one copy per run of consecutive records (rows of one chain)
+#pragma unroll
+        for (unsigned q = 0; q < kChGroup; ++q) {
+          if (ri[q] != ~0u && (q == 0 || ri[q] != ri[q - 1] + 1)) {
+            unsigned len = 1;
+            bool run = true;
+#pragma unroll
+            for (unsigned q2 = q + 1; q2 < kChGroup; ++q2) {
+              run = run && ri[q2] != ~0u && ri[q2] == ri[q2 - 1] + 1;
+              if (run) ++len;
+            }
+            tma_load_1d(slots + (size_t)(s0 + q) * rec, bytes + (size_t)ri[q] * rec, len * rec, &bar[g]);
+          }
+        }
+      }
+    };
 
     // ---- issue the loads of row u (its record must have landed)
     constexpr unsigned NV = B == 3 ? R : (unsigned)B;
     auto poll = [&](unsigned u, ChainStage<T, NV> &S) {
       const unsigned s = u % kChSlots;
-      if (!mbar_wait_bounded(&bar[s], (u / kChSlots) & 1u, timeout_ns)) {
+      if (!mbar_wait_bounded(&bar[s / kChGroup], (u / kChSlots) & 1u, timeout_ns)) {
         atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
         abort = true;
       }
@@ -375,7 +407,7 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
       }
     };
 
-    for (unsigned j = 0; j < kChSlots; ++j) produce();
+    for (unsigned j = 0; j < kChGroups; ++j) produce();
     // kChLook + 1 stages used in rotation: the loop is unrolled by that count
     // so every stage is a fixed set of registers. (Copying a register whose
     // load is still in flight waits for the load, which would put a round
@@ -396,8 +428,10 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
         if (t < issued) {
           if (t + kChLook < issued) poll(t + kChLook, st[(u + kChLook) % NST]);
           finish(t, st[u]);
-          __syncwarp();  // every lane is done with slot t % kChSlots before the next copy overwrites it
-          produce();
+          if ((t + 1) % kChGroup == 0) {  // its copy group is consumed
+            __syncwarp();                  // every lane is done with the group before the next copy overwrites it
+            produce();
+          }
         }
       }
     }
