@@ -26,14 +26,16 @@
 // Each direction and value type is stored once as fixed-size row records in
 // chain order, rewritten from the factors after each decomposition:
 //   [16 B: number of cross blocks nc, 0, 0, 0][m u32 cross columns, to 16 B]
-//   [m x 9 cross values][9: block on the chain predecessor, zero on a chain's
-//   first row][9: D^-1, forward only], padded to 16 B,
-// m being the longest cross list of the pattern. Lane 0 of each warp streams
-// its chains' records into a ring of kChSlots shared-memory slots with
-// cp.async.bulk (one mbarrier per slot), kChSlots rows ahead of the row being
-// finished; the polls of a row's cross values and the loads of its right-hand
-// side are issued kChLook rows ahead. The step from one row of a chain to the
-// next is then the row's reduction and two 3x3 products in registers.
+//   [m x B*B cross values][B*B: block on the chain predecessor, zero on a
+//   chain's first row][B*B: D^-1, forward only], padded to 16 B,
+// m being the longest cross list of the pattern (FP64 3x3 records keep the
+// predecessor's block right after the nc cross blocks instead). Lane 0 of
+// each warp streams its chains' records into a ring of kChSlots shared-memory
+// slots with cp.async.bulk, kChGroup rows per copy and mbarrier, up to
+// kChSlots rows ahead of the row being finished; the polls of a row's cross
+// values and the loads of its right-hand side are issued kChLook rows ahead.
+// The step from one row of a chain to the next is then the row's reduction
+// and the chain step in registers.
 //
 // Measured on GB300 (128x128x64 voxels x 6 tets, 1,081,665 block rows, 321
 // levels per direction), forward / backward ms: FP32 0.62 / 0.59 and FP64
@@ -54,15 +56,26 @@ namespace {
 
 constexpr unsigned kChThreads = 128;
 constexpr unsigned kChWarps = kChThreads / 32;
-constexpr unsigned kChSlots = 12;     // records in flight per warp
-constexpr unsigned kChGroup = 4;      // records per copy group (one mbarrier each)
-constexpr unsigned kChGroups = kChSlots / kChGroup;
 constexpr unsigned kChLook = 3;       // rows whose polls are issued ahead
-constexpr unsigned kChHead = 256;     // per-warp barriers and slot rows
+constexpr unsigned kChBarBytes = 64;  // per-warp copy-group barriers (up to 8)
 constexpr unsigned kChGrabLead = 8;   // rows before a chain's end at which the next chain is taken
-constexpr unsigned kChMaxRecord = 4096;
-static_assert(kChSlots * (8 + 8) <= kChHead, "slot barriers and slot rows must fit the per-warp header");
-static_assert(kChSlots % kChGroup == 0, "whole copy groups");
+constexpr size_t kChSmemCap = 227u * 1024u;  // shared memory one CTA may opt in to
+
+// Record ring of one warp: 16 slots in copy groups of 4 rows, or, for the
+// kernels of long records (3x3 rows with more than 9 cross blocks), 12 slots
+// in groups of 2 so that those still fit two CTAs per SM and keep at least
+// 7 rows of records ahead. Per-warp header: the copy-group barriers, then one
+// {row, chain start} per slot, 128-byte aligned; then the slots.
+template <int B, unsigned R>
+struct ChainRing {
+  static constexpr bool kLong = B == 3 && R >= 4;
+  static constexpr unsigned kSlots = kLong ? 12u : 16u;
+  static constexpr unsigned kGroup = kLong ? 2u : 4u;
+  static constexpr unsigned kGroups = kSlots / kGroup;
+  static constexpr unsigned kHead = (kChBarBytes + 8 * kSlots + 127) / 128 * 128;
+  static_assert(kSlots % kGroup == 0, "whole copy groups");
+  static_assert(kGroups * 8 <= kChBarBytes, "copy-group barriers fit their header part");
+};
 
 inline unsigned pad16u(unsigned x) { return (x + 15u) & ~15u; }
 
@@ -78,7 +91,9 @@ inline ChainGeom chain_geom(unsigned m, unsigned vs, bool fwd, unsigned B) {
   return g;
 }
 
-inline size_t chain_smem(unsigned rec) { return (size_t)kChWarps * (kChHead + (size_t)kChSlots * rec); }
+inline size_t chain_smem(unsigned rec, unsigned slots, unsigned head) {
+  return (size_t)kChWarps * (head + (size_t)slots * rec);
+}
 
 template <typename T, unsigned NV>
 struct ChainStage {
@@ -136,9 +151,12 @@ __global__ void __launch_bounds__(kChThreads) k_sweep_chain(unsigned nchain, con
   const unsigned lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const unsigned nwarp = gridDim.x * kChWarps;
   const unsigned w = blockIdx.x * kChWarps + wib;
+  using Ring = ChainRing<B, R>;
+  constexpr unsigned kChSlots = Ring::kSlots, kChGroup = Ring::kGroup, kChGroups = Ring::kGroups,
+                     kChHead = Ring::kHead;
   unsigned char *wb = ch_smem + (size_t)wib * (kChHead + (size_t)kChSlots * rec);
   uint64_t *bar = reinterpret_cast<uint64_t *>(wb);
-  uint2 *smeta = reinterpret_cast<uint2 *>(wb + 8 * kChSlots);  // {row, 1 if first row of its chain}
+  uint2 *smeta = reinterpret_cast<uint2 *>(wb + kChBarBytes);  // {row, 1 if first row of its chain}
   unsigned char *slots = wb + kChHead;
   if (w < nchain) {
     if (lane == 0) {
@@ -518,15 +536,35 @@ int chain_build(dfm2g_ilu_s *p, bool fwd, ChainSched &cs) {
   return DFM2G_OK;
 }
 
+// Register rounds of the 3x3 kernel for cross lists of up to m blocks (FP64
+// also sums the chain predecessor's block with them); 1 for 1x1 and 2x2.
+inline unsigned chain_rounds(unsigned m, unsigned B, bool f64) {
+  if (B != 3) return 1;
+  const unsigned need = f64 ? m + 1 : m;
+  if (need <= 6) return 2;
+  if (need <= 9 && f64) return 3;
+  if (need <= 12) return 4;
+  return 8;
+}
+
+// Ring slots and per-warp header bytes of the kernel for (B, R).
+inline void chain_ring(unsigned B, unsigned R, unsigned &slots, unsigned &head) {
+  if (B == 3 && R >= 4) {
+    slots = ChainRing<3, 4>::kSlots;
+    head = ChainRing<3, 4>::kHead;
+  } else {
+    slots = ChainRing<3, 2>::kSlots;
+    head = ChainRing<3, 2>::kHead;
+  }
+}
+
 template <typename T, bool FWD>
-void *chain_kernel(unsigned m, unsigned B) {
+void *chain_kernel(unsigned R, unsigned B) {
   if (B == 1) return (void *)k_sweep_chain<T, FWD, 1, 1>;
   if (B == 2) return (void *)k_sweep_chain<T, FWD, 2, 1>;
-  // FP64 sums the chain predecessor's block with the cross blocks
-  const unsigned need = sizeof(T) == 8 ? m + 1 : m;
-  if (need <= 6) return (void *)k_sweep_chain<T, FWD, 3, 2>;
-  if (need <= 9 && sizeof(T) == 8) return (void *)k_sweep_chain<T, FWD, 3, 3>;
-  if (need <= 12) return (void *)k_sweep_chain<T, FWD, 3, 4>;
+  if (R == 2) return (void *)k_sweep_chain<T, FWD, 3, 2>;
+  if (R == 3) return (void *)k_sweep_chain<T, FWD, 3, 3>;
+  if (R == 4) return (void *)k_sweep_chain<T, FWD, 3, 4>;
   return (void *)k_sweep_chain<T, FWD, 3, 8>;
 }
 
@@ -568,7 +606,11 @@ int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs
   const bool f64 = sizeof(T) == 8;
   const unsigned B = p->ndim;
   const ChainGeom g = chain_geom(cs.m, (unsigned)sizeof(T), forward, B);
-  if (g.rec > kChMaxRecord) return DFM2G_OK;
+  const unsigned R = chain_rounds(cs.m, B, f64);
+  unsigned slots = 0, head = 0;
+  chain_ring(B, R, slots, head);
+  const size_t smem = chain_smem(g.rec, slots, head);
+  if (smem > kChSmemCap) return DFM2G_OK;  // records too long for the rings
   const unsigned n = p->nblk;
   DevBuf<unsigned char> &bytes = chain_bytes(cs, T(0));
   unsigned &ver = f64 ? cs.ver64 : cs.ver32;
@@ -586,8 +628,7 @@ int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs
     note_launches(1);
     ver = p->factor_version;
   }
-  void *kernel = forward ? chain_kernel<T, true>(cs.m, B) : chain_kernel<T, false>(cs.m, B);
-  const size_t smem = chain_smem(g.rec);
+  void *kernel = forward ? chain_kernel<T, true>(R, B) : chain_kernel<T, false>(R, B);
   int &cap = cs.coop[f64 ? 1 : 0];
   if (cap <= 0) {
     DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
