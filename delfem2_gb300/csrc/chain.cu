@@ -38,8 +38,8 @@
 // and the chain step in registers.
 //
 // Measured on GB300 (128x128x64 voxels x 6 tets, 1,081,665 block rows, 321
-// levels per direction), forward / backward ms: FP32 0.62 / 0.59 and FP64
-// 1.23 / 1.06, against 0.91 / 0.90 and 2.19 / 1.76 for the sync-free
+// levels per direction), forward / backward ms: FP32 0.58 / 0.56 and FP64
+// 1.23 / 1.04, against 0.91 / 0.90 and 2.19 / 1.76 for the sync-free
 // schedule. One chain alone (a block-tridiagonal matrix, one warp) advances
 // 0.61 us per row in FP32 and 0.93 us in FP64; the sync-free schedule takes
 // 1.21 / 2.93 us per row there (one row per level).
