@@ -472,18 +472,18 @@ int chain_to_host(std::vector<V> &h, const V *d, size_t n) {
 }
 
 // Chains of one direction (host, from the sorted pattern and the level order).
-int chain_build(dfm2g_ilu_s *p, bool fwd, ChainSched &cs) {
-  cs.ok = false;
-  const unsigned n = p->nblk;
-  std::vector<unsigned> rs, col, dia, order;
-  DFM2G_CUDA(cudaStreamSynchronize(stream()));
-  DFM2G_TRY(chain_to_host(rs, p->row_start.p, (size_t)n + 1));
-  DFM2G_TRY(chain_to_host(col, p->col.p, p->nnz));
-  DFM2G_TRY(chain_to_host(dia, p->dia_ind.p, n));
-  DFM2G_TRY(chain_to_host(order, fwd ? p->order_f.p : p->order_b.p, n));
-  std::vector<unsigned> chain_of(n), first, len;
-  std::vector<unsigned char> linked(n, 0);
-  unsigned m = 0;
+// The chain partition of one direction (host only). Rows are visited in the
+// sweep's (level, row) order; a row joins its predecessor's chain when its
+// triangle's block nearest the diagonal is on that predecessor and every other
+// block's row lies in a chain numbered no higher. m = the longest cross list.
+void chain_partition(unsigned n, const unsigned *rs, const unsigned *col, const unsigned *dia,
+                     const unsigned *order, bool fwd, std::vector<unsigned> &chain_of, std::vector<unsigned> &first,
+                     std::vector<unsigned> &len, std::vector<unsigned char> &linked, unsigned &m) {
+  chain_of.assign(n, 0u);
+  linked.assign(n, 0);
+  first.clear();
+  len.clear();
+  m = 0;
   for (unsigned q = 0; q < n; ++q) {
     const unsigned i = order[q];
     const unsigned s0 = fwd ? rs[i] : dia[i], s1 = fwd ? dia[i] : rs[i + 1];
@@ -510,6 +510,21 @@ int chain_build(dfm2g_ilu_s *p, bool fwd, ChainSched &cs) {
     }
     m = std::max(m, (s1 - s0) - (link ? 1u : 0u));
   }
+}
+
+int chain_build(dfm2g_ilu_s *p, bool fwd, ChainSched &cs) {
+  cs.ok = false;
+  const unsigned n = p->nblk;
+  std::vector<unsigned> rs, col, dia, order;
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  DFM2G_TRY(chain_to_host(rs, p->row_start.p, (size_t)n + 1));
+  DFM2G_TRY(chain_to_host(col, p->col.p, p->nnz));
+  DFM2G_TRY(chain_to_host(dia, p->dia_ind.p, n));
+  DFM2G_TRY(chain_to_host(order, fwd ? p->order_f.p : p->order_b.p, n));
+  std::vector<unsigned> chain_of, first, len;
+  std::vector<unsigned char> linked;
+  unsigned m = 0;
+  chain_partition(n, rs.data(), col.data(), dia.data(), order.data(), fwd, chain_of, first, len, linked, m);
   const unsigned nchain = (unsigned)first.size();
   std::vector<uint4> chains(nchain);
   std::vector<unsigned> rec_of(n);
@@ -673,3 +688,27 @@ void chain_schedules_reset(dfm2g_ilu_s *p) {
 }
 
 }  // namespace dfm2g
+
+using namespace dfm2g;
+
+extern "C" {
+
+// Host-only: the chain partition the chain schedule uses, from a sorted ILU
+// pattern (row offsets, columns, diagonal positions) and the sweep's level
+// order. No device work.
+int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const unsigned *col, const unsigned *dia_ind,
+                          const unsigned *order, int backward, unsigned *chain_of, unsigned *nchain,
+                          unsigned *max_cross) {
+  if (n && (!row_start || !col || !dia_ind || !order || !chain_of))
+    return fail(DFM2G_ERR_ARG, "chain_partition: null array");
+  std::vector<unsigned> co, first, len;
+  std::vector<unsigned char> linked;
+  unsigned m = 0;
+  chain_partition(n, row_start, col, dia_ind, order, backward == 0, co, first, len, linked, m);
+  if (n) std::copy(co.begin(), co.end(), chain_of);
+  if (nchain) *nchain = (unsigned)first.size();
+  if (max_cross) *max_cross = m;
+  return DFM2G_OK;
+}
+
+}  // extern "C"

@@ -212,6 +212,14 @@ DFM2G_API int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_in
 DFM2G_API int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem);
 DFM2G_API int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, unsigned *order,
                                    unsigned *level_start, unsigned *nlevels);
+/* Diagnostic, host only (no counterpart in the reference): the chain partition
+ * DFM2G_SWEEP_CHAINS uses, from a sorted ILU pattern (row offsets, columns,
+ * dia_ind) and the sweep's level order (dfm2g_ilu_get_levels). chain_of[i] is
+ * row i's chain (numbered in the level order of their first rows); *max_cross
+ * the longest list of a row's dependencies outside its chain. */
+DFM2G_API int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const unsigned *col,
+                                    const unsigned *dia_ind, const unsigned *order, int backward,
+                                    unsigned *chain_of, unsigned *nchain, unsigned *max_cross);
 
 /* ---- Krylov solvers -------------------------------------------------------- */
 /* Solve_PCG, include/delfem2/lsitrsol.h:80-148, in FP64: x starts at 0; r is
