@@ -44,6 +44,7 @@
 // 0.61 us per row in FP32 and 0.93 us in FP64; the sync-free schedule takes
 // 1.21 / 2.93 us per row there (one row per level).
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -598,6 +599,32 @@ void chain_fill_launch(unsigned B, unsigned blocks, dfm2g_ilu_s *p, const T *vcr
                                                           cs.rec_of.p, cs.linked.p, bytes, g.rec, g.m, g.vo);
 }
 
+// Lets `kernel` launch with `smem` bytes of dynamic shared memory. The
+// attribute belongs to the kernel, not to a pattern, so it only ever grows
+// (per kernel and device): a handle with shorter records must not lower the
+// limit another handle's launches rely on.
+int chain_allow_smem(void *kernel, size_t smem) {
+  struct Entry {
+    void *kernel;
+    int device;
+    size_t smem;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> done;
+  std::lock_guard<std::mutex> lock(mu);
+  const int dev = ctx().device;
+  for (auto &d : done) {
+    if (d.kernel != kernel || d.device != dev) continue;
+    if (d.smem >= smem) return DFM2G_OK;
+    DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    d.smem = smem;
+    return DFM2G_OK;
+  }
+  DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  done.push_back(Entry{kernel, dev, smem});
+  return DFM2G_OK;
+}
+
 DevBuf<unsigned char> &chain_bytes(ChainSched &cs, double) { return cs.bytes64; }
 DevBuf<unsigned char> &chain_bytes(ChainSched &cs, float) { return cs.bytes32; }
 
@@ -644,9 +671,9 @@ int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs
     ver = p->factor_version;
   }
   void *kernel = forward ? chain_kernel<T, true>(R, B) : chain_kernel<T, false>(R, B);
+  DFM2G_TRY(chain_allow_smem(kernel, smem));
   int &cap = cs.coop[f64 ? 1 : 0];
   if (cap <= 0) {
-    DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     DFM2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kChThreads, smem));
     if (per_sm <= 0) return DFM2G_OK;

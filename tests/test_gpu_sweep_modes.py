@@ -76,3 +76,41 @@ def test_sweep_modes_on_edge_patterns(gpu, port, kind, n, mode):
     z32 = v.astype(np.float32)
     ilu.SolvePrecond(z32)
     assert rel_err(z32, go) < 1e-5
+
+
+def test_chain_kernels_shared_by_patterns_with_different_records(gpu, port):
+    """Two preconditioners whose chain sweeps run the same kernel with different
+    record sizes (a voxel mesh: six cross blocks per row; a block-tridiagonal
+    matrix: none), swept in turn: the second must not break the first's
+    launches (the kernel's shared-memory limit is shared by both)."""
+    import delfem2_gb300 as D
+
+    def prepare(ind, psup, vc, vd, n):
+        K = D.CMatrixSparse()
+        K.Initialize(n, 3, True)
+        K.SetPattern(ind, psup)
+        K.set_values(vc, vd)
+        ilu = D.CPreconditionerILU()
+        ilu.SetPattern0(K)
+        ilu.CopyValue(K)
+        assert ilu.Decompose()
+        assert ilu.sweep_mode() == 5  # the default schedule
+        col, dia = port.ilu_pattern0(ind, psup)
+        ivc, ivd = port.ilu_copy_value(ind, col, psup, vc, vd)
+        assert port.ilu_decompose(ind, col, dia, ivc, ivd)[0] == 0
+        return ilu, (ind, col, dia, ivc, ivd)
+
+    a = D.voxel_problem_arrays(4, 4, 4, 0.25, young=1.0)
+    n1 = a["np"]
+    rng = np.random.default_rng(11)
+    vc1 = 0.05 * rng.standard_normal(a["psup"].size * 9)
+    vd1 = np.tile(np.eye(3).ravel(), n1) * 4.0 + 0.1 * rng.standard_normal(n1 * 9)
+    ilu1, o1 = prepare(a["psup_ind"], a["psup"], vc1, vd1, n1)
+    ind2, psup2, vc2, vd2 = _system("chain", 500, 4)
+    ilu2, o2 = prepare(ind2, psup2, vc2, vd2, 500)
+    for ilu, o, n in ((ilu1, o1, n1), (ilu2, o2, 500), (ilu1, o1, n1)):
+        v = np.random.default_rng(n).standard_normal(n * 3).astype(np.float32)
+        f = v.copy()
+        ilu.ForwardSubstitution(f)
+        fo = port.ilu_forward(o[0], o[1], o[2], o[3], o[4], v.astype(np.float64))
+        assert rel_err(f, fo) < 1e-5
