@@ -102,3 +102,21 @@ def test_empty_pattern(built_lib):
     assert built_lib.dfm2g_chain_partition(0, z.ctypes.data, z.ctypes.data, z.ctypes.data, z.ctypes.data, 0,
                                            z.ctypes.data, C.byref(nchain), C.byref(m)) == 0
     assert nchain.value == 0 and m.value == 0
+
+
+@pytest.mark.parametrize("k", [1, 2, -1])
+def test_fill_in_patterns(built_lib, port, k):
+    """ILU(k) patterns (Initialize_ILUk's fill, -1 = full) of a small voxel
+    mesh: longer rows, more dependencies outside a row's chain."""
+    import delfem2_gb300 as D
+    a = D.voxel_problem_arrays(5, 4, 3, 0.2, young=1.0)
+    rs, col, dia = port.ilu_pattern_k(a["psup_ind"], a["psup"], k)
+    m_prev = None
+    for backward in (False, True):
+        level, order, _ = port.ilu_levels(rs, col, dia, backward)
+        chain_of, nchain, m = _partition(built_lib, rs, col, dia, order, backward)
+        _check(rs, col, dia, level, chain_of, nchain, m, backward)
+        assert m > 6  # fill adds dependencies beyond the ILU(0) neighbours
+        if m_prev is not None:
+            assert m == m_prev  # the pattern is symmetric: both triangles alike
+        m_prev = m
