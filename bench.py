@@ -118,8 +118,6 @@ def algorithmic_bytes(kind: str, nb: int, nz: int, s: int) -> float:
         return 2 * v3
     if kind == "pupdate":   # p, z read; p written
         return 3 * v3
-    if kind == "fill":      # two output vectors written (two launches)
-        return v3
     return float("nan")
 
 
