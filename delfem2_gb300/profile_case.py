@@ -2,6 +2,7 @@
 
   python -m delfem2_gb300.profile_case [--nx 64 --ny 64 --nz 64] [--fp64] [--solves 1] [--method reliable]
                                        [--poisson] [--sweep-mode M] [--precond K]
+  python -m delfem2_gb300.profile_case --cloth NDIV [--solves K]
 
 Sets the problem up (mesh, pattern, level sets, assembly, ILU(0)) and runs
 `--solves` solves of K u = b to 1e-10 (FP32-inner/FP64-refinement by default,
@@ -11,6 +12,10 @@ Poisson problem (1x1 blocks) on the same mesh instead: alpha = 1, source = 1,
 the z = 0 face at 0 and the top face at 1. --sweep-mode selects the triangular-sweep
 schedule (a dfm2g_sweep value); --precond K replaces the solves by K FP32
 SolvePrecond calls (forward + backward sweep) on a seeded vector.
+--cloth NDIV runs `--solves` backward-Euler steps of the implicit cloth
+(StepTime_InternalDynamicsILU) on an NDIV x NDIV-cell sheet instead: E = 1e3,
+nu = 0.3, bending 1e-3, two corners pinned, dt = 0.01, FP64 ILU(0)-PCG to 1e-8
+capped at 100 iterations per step.
 """
 from __future__ import annotations
 
@@ -30,11 +35,16 @@ def main():
     ap.add_argument("--poisson", action="store_true", help="scalar Poisson (1x1 blocks) on the same mesh")
     ap.add_argument("--sweep-mode", type=int, default=None, help="triangular-sweep schedule (dfm2g_sweep value)")
     ap.add_argument("--precond", type=int, default=0, help="K FP32 SolvePrecond calls instead of solves")
+    ap.add_argument("--cloth", type=int, default=0, help="cloth sheet of NDIV x NDIV cells instead of the tets")
     args = ap.parse_args()
 
     import torch
     import delfem2_gb300 as D
     from delfem2_gb300 import _native as N
+
+    if args.cloth:
+        cloth_steps(args.cloth, args.solves)
+        return
 
     a = D.voxel_problem_arrays(args.nx, args.ny, args.nz, 1.0 / args.nx, seed=3)
     if args.poisson:
@@ -87,6 +97,23 @@ def main():
             torch.cuda.synchronize()
             print(f"solve {k}: mixed {st.iterations} inner / {st.outer} outer, rel {st.rel_residual:.2e}, "
                   f"{1e3 * (time.perf_counter() - t):.1f} ms")
+
+
+def cloth_steps(ndiv: int, nsteps: int):
+    import torch
+    from delfem2_gb300 import cloth as DC
+    xyz0, _, tri, quad = DC.SetClothShape_Square(ndiv, 1.0)
+    cl = DC.Cloth(xyz0, tri, quad)
+    bc = torch.tensor(DC.pin_two_corners(ndiv), device="cuda")
+    E = torch.full((cl.ntri,), 1e3, dtype=torch.float64, device="cuda")
+    x = torch.tensor(xyz0, device="cuda")
+    v = torch.zeros_like(x)
+    for k in range(nsteps):
+        t = time.perf_counter()
+        st = cl.StepTime_InternalDynamicsILU(x, v, bc, E, 0.3, 1e-3, (0.0, 0.0, -10.0), 1.0 / cl.np, 0.01, 1e-8, 100)
+        torch.cuda.synchronize()
+        print(f"cloth step {k}: {st.iterations} PCG iterations, rel {st.rel_residual:.2e}, "
+              f"{1e3 * (time.perf_counter() - t):.1f} ms")
 
 
 if __name__ == "__main__":
