@@ -139,6 +139,7 @@ SIGNATURES = {
     "dfm2g_profile_reset": [],
     "dfm2g_profile_read": [_i, _pu, C.POINTER(C.c_double)],
     "dfm2g_launch_count": [C.POINTER(C.c_ulonglong)],
+    "dfm2g_alloc_count": [C.POINTER(C.c_ulonglong)],
     "dfm2g_debug_wait_timeout": [_u],
 }
 

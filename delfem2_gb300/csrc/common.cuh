@@ -35,6 +35,7 @@ int fail(int status, const char *fmt, ...);
 
 // ---- instrumentation -----------------------------------------------------------
 void note_launches(unsigned n);
+void note_alloc();  // one device allocation (cudaMalloc) made by the library
 // Times the launches between construction and destruction as one `kind`
 // sample when profiling is on; counts them always.
 struct ProfScope {
@@ -75,6 +76,7 @@ struct DevBuf {
     if (count == n && p) return DFM2G_OK;
     release();
     if (count == 0) return DFM2G_OK;
+    note_alloc();
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
     if (e != cudaSuccess) {
       p = nullptr;
@@ -343,7 +345,7 @@ int group_sweep(dfm2g_ilu_s *p, bool forward, const float *in, float *out, const
 int part_schedules_build(dfm2g_ilu_s *p);
 template <typename T>
 int stream_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
-                 unsigned long long timeout, bool *usable);
+                 unsigned long long timeout, bool may_alloc, bool *usable);
 void stream_schedules_reset(dfm2g_ilu_s *p);
 template <typename T>
 int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,

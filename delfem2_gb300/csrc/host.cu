@@ -65,7 +65,10 @@ static std::vector<cudaEvent_t> g_event_pool;
 static unsigned g_prof_count[DFM2G_PROF_NKIND];
 static double g_prof_ms[DFM2G_PROF_NKIND];
 
+static std::atomic<unsigned long long> g_allocs{0};
+
 void note_launches(unsigned n) { g_launches += n; }
+void note_alloc() { g_allocs += 1; }
 
 static cudaEvent_t take_event() {
   if (!g_event_pool.empty()) {
@@ -145,6 +148,12 @@ int dfm2g_profile_read(int kind, unsigned *launches, double *total_ms) {
 int dfm2g_launch_count(unsigned long long *count) {
   if (!count) return fail(DFM2G_ERR_ARG, "null count");
   *count = g_launches.load();
+  return DFM2G_OK;
+}
+
+int dfm2g_alloc_count(unsigned long long *count) {
+  if (!count) return fail(DFM2G_ERR_ARG, "null count");
+  *count = g_allocs.load();
   return DFM2G_OK;
 }
 

@@ -855,8 +855,9 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
   if (p->sweep_mode == DFM2G_SWEEP_BLOCK) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
-    DFM2G_TRY(stream_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, &usable));
-    if (usable) return DFM2G_OK;  // else (a row too long for a unit): the sync-free schedule below
+    DFM2G_TRY(stream_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
+                              &usable));
+    if (usable) return DFM2G_OK;  // else (a row too long for a unit, or not built): the sync-free schedule below
   }
   if (p->sweep_mode == DFM2G_SWEEP_PARTS && p->parts_ok) {
     if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
@@ -1208,6 +1209,11 @@ static std::mutex g_noalloc_mutex;
 static int noalloc_scratch(void **out) {
   int dev = 0;
   DFM2G_CUDA(cudaGetDevice(&dev));
+  // The library's stream and handles live on ctx().device; a sweep launched
+  // there must get that device's copy of the array.
+  if (dev != ctx().device)
+    return fail(DFM2G_ERR_STATE, "solve_precond_noalloc: current device %d is not the library's device %d", dev,
+                ctx().device);
   if (dev < 0 || dev >= 64) return fail(DFM2G_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_addr[dev]) {

@@ -939,6 +939,7 @@ int dfm2g_dev_alloc(void **p, size_t bytes) {
   DFM2G_TRY(ensure_context());
   *p = nullptr;
   if (bytes == 0) return DFM2G_OK;
+  note_alloc();
   DFM2G_CUDA(cudaMalloc(p, bytes));
   return DFM2G_OK;
 }

@@ -316,12 +316,17 @@ DevBuf<float> &in_lv_of(dfm2g_ilu_s *p, float) { return p->in_lv32; }
 }  // namespace
 
 // Builds (first use) and refreshes (after each decomposition) the stream of
-// one direction and value type; false in *usable when the pattern does not fit.
+// one direction and value type; false in *usable when the pattern does not fit,
+// or when !may_alloc and the stream or its level-ordered input buffer does not
+// exist yet (building them allocates).
 template <typename T>
 int stream_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
-                 unsigned long long timeout, bool *usable) {
+                 unsigned long long timeout, bool may_alloc, bool *usable) {
   StreamSched &ss = sched_of(p, forward, T(0));
   *usable = false;
+  if (!may_alloc &&
+      (!ss.built || !ss.ok || !in_lv_of(p, T(0)).p || in_lv_of(p, T(0)).n < (size_t)p->nblk * 3 + 16))
+    return DFM2G_OK;
   if (!ss.built) {
     ss.built = true;
     DFM2G_TRY(build_stream(p, forward, sizeof(T), ss));
@@ -357,9 +362,9 @@ int stream_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcr
 }
 
 template int stream_sweep<float>(dfm2g_ilu_s *, bool, const float *, float *, const float *, const float *,
-                                 const int *, unsigned long long, bool *);
+                                 const int *, unsigned long long, bool, bool *);
 template int stream_sweep<double>(dfm2g_ilu_s *, bool, const double *, double *, const double *, const double *,
-                                  const int *, unsigned long long, bool *);
+                                  const int *, unsigned long long, bool, bool *);
 
 }  // namespace dfm2g
 

@@ -194,8 +194,12 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * a device looks up that array's device address. All calls share the array:
  * calls that overlap on the GPU (other streams, other threads) race. FP32 needs
  * FP32 factors made earlier by a DFM2G_F32 dfm2g_ilu_solve_precond call.
- * Under DFM2G_SWEEP_CHAINS the chain records are made by the first ordinary
- * sweep in each precision; until then this entry point sweeps sync-free. */
+ * The device current at the call must be the library's device
+ * (DFM2G_ERR_STATE otherwise). Schedules whose data is built on first use
+ * fall back to the sync-free schedule until an ordinary sweep of the same
+ * precision has built that data: DFM2G_SWEEP_CHAINS (chain records) and
+ * DFM2G_SWEEP_BLOCK (the level-ordered stream and its input buffer). The
+ * other schedules (sync-free, levels, groups, parts) need nothing built. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
 /* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE, DFM2G_SWEEP_LEVELS and DFM2G_SWEEP_CHAINS. */
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
@@ -431,6 +435,9 @@ DFM2G_API int dfm2g_profile_reset(void);
 DFM2G_API int dfm2g_profile_read(int kind, unsigned *launches, double *total_ms);
 /* Number of kernels this library has launched since load (all kinds). */
 DFM2G_API int dfm2g_launch_count(unsigned long long *count);
+/* Number of device allocations (cudaMalloc) this library has made since load
+ * (no counterpart in the reference; instrumentation). */
+DFM2G_API int dfm2g_alloc_count(unsigned long long *count);
 
 /* ---- test support ---------------------------------------------------------- */
 /* Launches one tiny kernel that waits on a value nothing ever writes, bounded
