@@ -43,14 +43,21 @@ static void emat_tet(const double P[4][3], double myu, double lam, double emat[4
   *vol_out = vol;
 }
 
-// A generic PCG written against the ADL primitives only (the call shapes of
-// the reference's Solve_PCG<MAT, VEC, PREC>): exercises the compatibility path
-// of dfm2g.hpp with device vectors. Returns the iteration count.
+// A generic PCG written against the ADL primitives only, step for step as the
+// reference's Solve_PCG<MAT, VEC, PREC> (lsitrsol.h:80-148): x = 0; history of
+// |r| starting with |r0|; early return when |r0|^2 < 1e-30; Ap shares Pr's
+// storage; stop when |r|/|r0| < tol; one more |r| entry when max_it runs out.
+// It exercises the compatibility path of dfm2g.hpp with device vectors (every
+// Dot is a device reduction read back to the host). Returns the history.
 template <class MAT, class VEC, class PREC>
-static unsigned generic_pcg(VEC &r, VEC &x, VEC &Pr, VEC &p, double tol, unsigned max_it, const MAT &K,
-                            const PREC &M) {
+static std::vector<double> generic_pcg(VEC &r, VEC &x, VEC &Pr, VEC &p, double tol, unsigned max_it, const MAT &K,
+                                       const PREC &M) {
+  std::vector<double> hist;
   x.setZero();
   const double rr0 = Dot(r, r);
+  hist.push_back(std::sqrt(rr0));
+  if (rr0 < 1.0e-30) return hist;
+  const double inv_rr0 = 1.0 / rr0;
   Pr = r;
   SolvePrecond(Pr, M);
   p = Pr;
@@ -61,14 +68,17 @@ static unsigned generic_pcg(VEC &r, VEC &x, VEC &Pr, VEC &p, double tol, unsigne
     const double alpha = rz / Dot(p, Ap);
     AddScaledVec(r, -alpha, Ap);
     AddScaledVec(x, alpha, p);
-    if (std::sqrt(Dot(r, r) / rr0) < tol) return it + 1;
+    const double rr = Dot(r, r);
+    hist.push_back(std::sqrt(rr));
+    if (std::sqrt(rr * inv_rr0) < tol) return hist;
     Pr = r;
     SolvePrecond(Pr, M);
     const double rz1 = Dot(r, Pr);
     ScaleAndAddVec(p, rz1 / rz, Pr);
     rz = rz1;
   }
-  return max_it;
+  hist.push_back(std::sqrt(Dot(r, r)));
+  return hist;
 }
 
 int main(int argc, char **argv) {
@@ -134,12 +144,22 @@ int main(int argc, char **argv) {
   g::DeviceVector dr(nd), dx(nd), dPr(nd), dp(nd);
   dr.upload(b.data());
   g::DeviceVectorView vr = dr.view(), vx = dx.view(), vPr = dPr.view(), vp = dp.view();
-  const unsigned its2 = generic_pcg(vr, vx, vPr, vp, 1e-10, 1000, K, ilu);
+  const std::vector<double> hist2 = generic_pcg(vr, vx, vPr, vp, 1e-10, 1000, K, ilu);
   std::vector<double> x2(nd);
   dx.download(x2.data());
   double xs2 = 0;
   for (size_t i = 0; i < nd; ++i) xs2 += x2[i];
-  std::printf("iterations %zu residual %.3e xsum %.17g compat_iterations %u compat_xsum %.17g\n", hist.size() - 1,
-              std::sqrt(rr / bb), xs, its2, xs2);
+  std::printf("iterations %zu residual %.3e xsum %.17g compat_iterations %zu compat_xsum %.17g\n", hist.size() - 1,
+              std::sqrt(rr / bb), xs, hist2.size() - 1, xs2);
+  // the compatibility path's solution and history, for the caller to compare with the oracle
+  if (argc > 2) {
+    FILE *f = std::fopen(argv[2], "wb");
+    if (!f) return 4;
+    const unsigned long long nh = hist2.size();
+    std::fwrite(&nh, sizeof nh, 1, f);
+    std::fwrite(hist2.data(), sizeof(double), hist2.size(), f);
+    std::fwrite(x2.data(), sizeof(double), x2.size(), f);
+    std::fclose(f);
+  }
   return 0;
 }

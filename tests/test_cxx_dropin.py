@@ -28,8 +28,9 @@ def test_dropin_header_compiles_and_links(exe):
 
 
 @pytest.mark.gpu
-def test_dropin_caller_matches_oracle(exe, gpu, port):
-    out = subprocess.run([exe, "8"], capture_output=True, text=True, timeout=120)
+def test_dropin_caller_matches_oracle(exe, gpu, port, tmp_path):
+    dump = str(tmp_path / "compat.bin")
+    out = subprocess.run([exe, "8", dump], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
     f = out.stdout.split()
     its, res, xsum = int(f[1]), float(f[3]), float(f[5])
@@ -53,16 +54,27 @@ def test_dropin_caller_matches_oracle(exe, gpu, port):
     port.ilu_decompose(ind, col, dia, ivc, ivd)
     x, _, h = port.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, 1e-10, 1000)
     assert abs(its - (len(h) - 1)) <= 1
+    # the compatibility path (a PCG written step for step as the reference's
+    # Solve_PCG over device vectors): its history and solution against the oracle's
+    raw = np.fromfile(dump, np.uint8)
+    nh = int(np.frombuffer(raw[:8], np.uint64)[0])
+    hist2 = np.frombuffer(raw[8:8 + 8 * nh], np.float64)
+    x2 = np.frombuffer(raw[8 + 8 * nh:], np.float64)
+    assert abs(len(hist2) - len(h)) <= 1
+    assert abs(hist2[0] - h[0]) <= 1e-12 * h[0]  # |r0|: the same right-hand side
+    assert np.abs(x2 - x).max() <= 1e-8 * np.abs(x).max()
     assert res < 1e-9
     assert abs(xsum - x.sum()) <= 1e-8 * np.abs(x).sum()
 
 
 COMPAT = os.path.join(ROOT, "tests", "cxx", "compat_reference_pcg.cpp")
-REF_INCLUDE = "/root/reference/include"
+# The DelFEM2 source tree, when the environment names it (no default).
+REF_ROOT = os.environ.get("DFM2_REFERENCE_ROOT", "")
+REF_INCLUDE = os.path.join(REF_ROOT, "include") if REF_ROOT else ""
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_INCLUDE, "delfem2")),
-                    reason="reference source tree not available")
+@pytest.mark.skipif(not (REF_INCLUDE and os.path.isdir(os.path.join(REF_INCLUDE, "delfem2"))),
+                    reason="DFM2_REFERENCE_ROOT does not name a DelFEM2 source tree")
 def test_reference_solve_pcg_template_accepts_device_views():
     """The reference's own generic Solve_PCG (lsitrsol.h:80-148) instantiates
     with delfem2::gb300::DeviceVectorView, CMatrixSparse<double> and
