@@ -34,6 +34,7 @@ SWEEP_GROUPS = 2
 SWEEP_BLOCK = 3
 SWEEP_PARTS = 4
 SWEEP_CHAINS = 5
+SWEEP_TILES = 6
 
 
 class SolveStats(C.Structure):
@@ -99,6 +100,7 @@ SIGNATURES = {
     "dfm2g_ilu_get_values": [_vp, _vp, _vp, _i],
     "dfm2g_ilu_get_levels": [_vp, _i, _vp, _vp, _vp, _pu],
     "dfm2g_chain_partition": [_u, _vp, _vp, _vp, _vp, _i, _vp, _pu, _pu],
+    "dfm2g_tile_partition": [_u, _vp, _vp, _vp, _vp, _i, _u, _u, _vp, _vp, _pu, _pu],
     "dfm2g_solve_pcg": [_vp, _vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
     "dfm2g_solve_cg": [_vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],
     "dfm2g_solve_pbicgstab": [_vp, _vp, _vp, _vp, _d, _u, _vp, _u, _pu, _i, _pstats],

@@ -64,6 +64,41 @@ def fd_loss_change(P, E, f, u0, u_star, tol=1e-12):
         return float(torch.dot(d, u0 - u_star) + 0.5 * torch.dot(d, d))
 
 
+def fd_rows(P, E, f, u0, u_star, tets, dofs, h, gE, gf, gE_mixed, gf_mixed):
+    """Central differences of L on the sampled tets and DOFs, next to the
+    FP64 and mixed adjoint gradients: two lists of (fd, g_fp64, g_mixed)."""
+    rowsE, rowsf = [], []
+    for e in tets:
+        Ep, Em = E.clone(), E.clone()
+        Ep[e] += h
+        Em[e] -= h
+        fd = (fd_loss_change(P, Ep, f, u0, u_star) - fd_loss_change(P, Em, f, u0, u_star)) / (2 * h)
+        rowsE.append((fd, float(gE[e]), float(gE_mixed[e])))
+    for i in dofs:
+        fp, fm = f.clone(), f.clone()
+        fp[i] += h
+        fm[i] -= h
+        fd = (fd_loss_change(P, E, fp, u0, u_star) - fd_loss_change(P, E, fm, u0, u_star)) / (2 * h)
+        rowsf.append((fd, float(gf[i]), float(gf_mixed[i])))
+    return rowsE, rowsf
+
+
+def fd_errors(rows, scale):
+    """(vector, entry) relative errors of the FP64 and mixed adjoints against
+    the differences: vector = max|g - fd| / max|g| (scale) over the samples;
+    entry = max|g - fd| / |fd| over the samples with |fd| >= 1e-2 scale
+    (smaller entries sit at the FP64 solves' accuracy floor). Also returns
+    the number of such significant samples."""
+    import numpy as np
+    r = np.array(rows)
+    sig = np.abs(r[:, 0]) >= 1e-2 * scale
+    out = {}
+    for col, tag in ((1, "fp64"), (2, "mixed")):
+        out[tag] = (float(np.abs(r[:, col] - r[:, 0]).max() / scale),
+                    float((np.abs(r[sig, col] - r[sig, 0]) / np.abs(r[sig, 0])).max()) if sig.any() else 0.0)
+    return out, int(sig.sum())
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=48)
@@ -92,19 +127,7 @@ def main():
     free = np.nonzero(a["bc"] == 0)[0]
     dofs = rng.choice(free, size=args.dofs, replace=False)
     h = args.h
-    rowsE, rowsf = [], []  # (fd, g_fp64, g_mixed)
-    for e in tets:
-        Ep, Em = E.clone(), E.clone()
-        Ep[e] += h
-        Em[e] -= h
-        fd = (fd_loss_change(P, Ep, f, u0, u_star) - fd_loss_change(P, Em, f, u0, u_star)) / (2 * h)
-        rowsE.append((fd, float(gE[e]), float(gE_mixed[e])))
-    for i in dofs:
-        fp, fm = f.clone(), f.clone()
-        fp[i] += h
-        fm[i] -= h
-        fd = (fd_loss_change(P, E, fp, u0, u_star) - fd_loss_change(P, E, fm, u0, u_star)) / (2 * h)
-        rowsf.append((fd, float(gf[i]), float(gf_mixed[i])))
+    rowsE, rowsf = fd_rows(P, E, f, u0, u_star, tets, dofs, h, gE, gf, gE_mixed, gf_mixed)
     out = {"n": args.n, "dof": a["np"] * 3, "tets": a["ntet"], "L": L, "L_fp64": L64, "h": h,
            "n_tet_samples": len(tets), "n_dof_samples": len(dofs),
            "mixed_vs_fp64_adjoint_dLdE_max_rel": float((gE_mixed - gE).abs().max() / gE.abs().max()),
@@ -113,12 +136,11 @@ def main():
            "errors": ("vector: max|g - fd| / max|g| over the samples; entry: max |g - fd| / |fd| over samples "
                       "with |fd| >= 1e-2 max|g| (smaller entries sit at the FP64 solves' accuracy floor)")}
     for name, rows, scale in (("dLdE", rowsE, float(gE.abs().max())), ("dLdf", rowsf, float(gf.abs().max()))):
-        r = np.array(rows)
-        sig = np.abs(r[:, 0]) >= 1e-2 * scale
-        for col, tag in ((1, "fp64"), (2, "mixed")):
-            out[f"{name}_{tag}_vs_fd_vector_rel"] = float(np.abs(r[:, col] - r[:, 0]).max() / scale)
-            out[f"{name}_{tag}_vs_fd_entry_rel"] = float((np.abs(r[sig, col] - r[sig, 0]) / np.abs(r[sig, 0])).max())
-        out[f"{name}_significant_samples"] = int(sig.sum())
+        errs, nsig = fd_errors(rows, scale)
+        for tag, (vec, ent) in errs.items():
+            out[f"{name}_{tag}_vs_fd_vector_rel"] = vec
+            out[f"{name}_{tag}_vs_fd_entry_rel"] = ent
+        out[f"{name}_significant_samples"] = nsig
     print(json.dumps(out))
 
 

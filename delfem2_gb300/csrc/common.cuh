@@ -168,6 +168,13 @@ __device__ __forceinline__ bool is_pending(float v) { return __float_as_uint(v) 
 __device__ __forceinline__ bool is_pending(double v) {
   return __double_as_longlong(v) == (long long)-1;
 }
+template <typename T>
+__device__ __forceinline__ T pending_value() {
+  if constexpr (sizeof(T) == 8)
+    return __longlong_as_double(-1ll);
+  else
+    return __uint_as_float(0xffffffffu);
+}
 
 // Default bound on every device-side wait.
 constexpr unsigned long long kWaitTimeoutNs = 1000000000ull;  // 1 s
@@ -285,6 +292,25 @@ struct ChainSched {
   dfm2g::DevBuf<unsigned> ctr;      // chain counter and done-ticket of the launch
 };
 
+// Tiles of one sweep direction (tiles.cu): tile and step descriptors, the
+// record of each row, group headers and codes, per-step halo lists, and the
+// records per value type (rewritten after each decomposition).
+struct TileSched {
+  bool built = false, ok = false;
+  unsigned ntiles = 0, nsteps = 0, M = 0, max_groups = 0, max_halo = 0;  // M: dependency slots per row
+  size_t ngroups = 0;
+  unsigned ver32 = ~0u, ver64 = ~0u;  // factor_version the records were written from
+  int coop[2] = {0, 0};               // resident CTAs of the sweep kernel [f64]
+  dfm2g::DevBuf<uint4> tiles;         // 2 per tile: {first step, steps, first group, groups}, {halo words}
+  dfm2g::DevBuf<uint4> steps;         // 2 per step: {first group, rows, local base, groups}, {halo list}
+  dfm2g::DevBuf<unsigned> halo;       // per step: the rows of other tiles it reads
+  dfm2g::DevBuf<unsigned> rec_of;     // 10 * group + position of each row
+  dfm2g::DevBuf<unsigned> gmeta;      // per group: 10 row ids, then codes [10][Mc]
+  dfm2g::DevBuf<unsigned char> bytes32, bytes64;
+  dfm2g::DevBuf<unsigned char> in32, in64;  // right-hand side in the records' row order
+  dfm2g::DevBuf<unsigned> ctr;        // tile counter and done-ticket of the launch
+};
+
 struct dfm2g_ilu_s {
   unsigned nblk = 0;
   unsigned ndim = 3;  // block size of the matrix the pattern was taken from
@@ -302,6 +328,7 @@ struct dfm2g_ilu_s {
   PartSched parts_f, parts_b;           // row-range partitions (forward, backward)
   StreamSched ss32_f, ss32_b, ss64_f, ss64_b;  // level streams of the single-CTA sweep
   ChainSched cs_f, cs_b;                // chain schedules (forward, backward)
+  TileSched ts_f, ts_b;                 // tile schedules (forward, backward)
   dfm2g::DevBuf<double> in_lv64;        // right-hand side gathered in level order
   dfm2g::DevBuf<float> in_lv32;
   unsigned factor_version = 0;          // incremented by each decomposition
@@ -351,6 +378,13 @@ template <typename T>
 int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                 unsigned long long timeout, bool may_alloc, bool *usable);
 void chain_schedules_reset(dfm2g_ilu_s *p);
+template <typename T>
+int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
+               unsigned long long timeout, bool may_alloc, bool *usable);
+void tile_schedules_reset(dfm2g_ilu_s *p);
+void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const unsigned *col, const unsigned *order,
+                    bool fwd, unsigned max_rows, unsigned max_width, std::vector<unsigned> &tile_of,
+                    std::vector<unsigned> &lev, unsigned &ntiles, unsigned &m);
 template <typename T>
 int part_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout);

@@ -864,9 +864,16 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     return part_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev);
   }
-  // sync-free, chain and blob schedules: `out` is filled with the pending marker
+  // sync-free, tile, chain and blob schedules: `out` is filled with the pending marker
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
-  if (p->sweep_mode == DFM2G_SWEEP_CHAINS) {
+  if (p->sweep_mode == DFM2G_SWEEP_TILES) {
+    const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+    bool usable = false;
+    DFM2G_TRY(tile_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
+                            &usable));
+    if (usable) return DFM2G_OK;  // else (rows too long for the tiles, or not built): the chains below
+  }
+  if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_TILES) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
@@ -1040,6 +1047,7 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, unsigned ndim, size_t nn
   DFM2G_TRY(compute_levels(p, true));
   stream_schedules_reset(p);
   chain_schedules_reset(p);
+  tile_schedules_reset(p);
   if (ndim == 3) {  // the blob and row-range schedules are written for 3x3 blocks
     DFM2G_TRY(group_schedules_build(p));
     DFM2G_TRY(part_schedules_build(p));
@@ -1260,7 +1268,8 @@ int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) { return 
 int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
-      mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS)
+      mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS &&
+      mode != DFM2G_SWEEP_TILES)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
   if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_CHAINS)
     return fail(DFM2G_ERR_UNSUPPORTED, "sweep mode %d needs 3x3 blocks (the pattern has ndim %u)", mode, p->ndim);

@@ -1,0 +1,950 @@
+// Tile-scheduled triangular sweep (DFM2G_SWEEP_TILES), 3x3 blocks, FP32 and FP64.
+//
+// The rows of one sweep direction are partitioned into tiles: compact sets of
+// rows grown breadth-first from a seed row, a row joining the tile only once
+// every row it depends on is in an earlier tile or already in this one. Seeds
+// are taken in the sweep's (level, row) order, so the tiles are numbered in a
+// dependency order that follows the wavefront. Inside a tile the rows are
+// grouped by their local level (1 + the highest local level of the rows of the
+// same tile they depend on): the tile's steps. On a structured mesh in its
+// natural order the tiles are small boxes of the grid (8x8x8 nodes on the
+// voxel meshes, whose dependencies all point to lower neighbours), and a
+// dependency path crosses a tile boundary once per tile instead of once per
+// row or pencil of rows.
+//
+// One CTA sweeps one tile at a time, step by step: ten rows per consumer
+// warp and step, three lanes per row (one per component a, lane 3q + a of row
+// q), each lane summing row a of the row's dependency blocks against their x
+// values. Nothing on a step's path reads global memory:
+//  - values of rows of the same tile come from a shared-memory copy of the
+//    tile's results (visible after the consumers' barrier of the step that
+//    wrote them);
+//  - values of rows of other tiles (the step's halo, listed per step) are
+//    copied from global memory into the step's slot ahead of the step
+//    (cp.async through L2, completing on the slot's halo mbarrier); a value
+//    still holding the pending marker (the sync-free schedules' NaN) is
+//    polled in global memory when the step runs;
+//  - the right-hand side arrives with the step's records: a gather kernel
+//    first writes it in the records' row order (group-major, 32 values per
+//    group of ten rows).
+// A producer warp streams each step's records, right-hand side and halo list
+// into a ring of shared-memory slots (cp.async.bulk, one mbarrier per slot),
+// issues the halo copies kTiHaloLag steps behind, takes the CTA's next tile
+// from a counter a few steps before the current one ends (so tiles go to CTAs
+// in the order CTAs become free) and then prefetches that tile's records into
+// L2.
+//
+// Progress: tiles are handed out in increasing number (the first by CTA
+// index, later ones from the counter), every CTA is resident (cooperative
+// launch), and every dependency of a tile's row lies in a lower-numbered tile
+// or in an earlier step of the same tile. The lowest-numbered unfinished tile
+// is the current tile of some CTA (a CTA's next tile is numbered above its
+// current one), and all its outside dependencies are finished, so the sweep
+// cannot deadlock. Every wait is bounded (DFM2G_ERR_WAIT_TIMEOUT); a CTA that
+// stops early first waits (bounded) for the copies it issued.
+//
+// Record layout of one group of ten rows (G = 10 rows, M = dependency slots
+// of the pattern, Mc = M rounded up to 4, S = value bytes, NV = 3M (+3 for
+// D^-1 in the forward sweep) values per lane):
+//   [0, 48)   u32 row id of each of the ten rows (~0u: none), padding
+//   [48, ..)  u32 code[G][Mc]: 0x80000000 | local index (a row of the same
+//             tile, or kTiZero for an unused slot); 0x40000000 | row (a row
+//             of another tile read in global memory: beyond the step's first
+//             kTiHalo, or so close to the end of the vector that its 32-byte
+//             copy would pass it); else a halo entry: bits 0-7 its index in
+//             the step's halo list, bits 8-9 / bit 10 the offset (in 4 / 8
+//             bytes) of the row's FP32 / FP64 values inside their copy
+//   [vo, ..)  the lanes' values in 16-byte chunks, chunk k of lane l at
+//             vo + (30 k + l) 16: lane 3q + a holds (forward) row a of D^-1,
+//             then L_b[a][0..2] for b < M
+// A step's groups are consecutive in the stream, so one copy moves a step.
+#include <algorithm>
+#include <functional>
+#include <mutex>
+#include <queue>
+#include <vector>
+
+#include "common.cuh"
+#include "tma.cuh"
+
+namespace dfm2g {
+
+namespace {
+
+#ifndef DFM2G_TILE_ROWS
+#define DFM2G_TILE_ROWS 512  // rows per tile at most
+#endif
+#ifndef DFM2G_TILE_WARPS
+#define DFM2G_TILE_WARPS 5  // consumer warps per CTA: at most 10 per warp rows per step
+#endif
+constexpr unsigned kTiRows = DFM2G_TILE_ROWS;
+constexpr unsigned kTiWarps = DFM2G_TILE_WARPS;
+constexpr unsigned kTiG = 10;                   // rows per group (30 lanes)
+constexpr unsigned kTiWidth = kTiG * kTiWarps;  // rows per step at most
+constexpr unsigned kTiThreads = 32 * (kTiWarps + 1);
+constexpr unsigned kTiCons = 32 * kTiWarps;     // consumer threads
+constexpr unsigned kTiHead = 48;
+constexpr unsigned kTiLocal = 0x80000000u;
+constexpr unsigned kTiGlobal = 0x40000000u;     // code: a row read in global memory (low 30 bits)
+constexpr unsigned kTiZero = kTiRows;           // local index of the all-zero row
+constexpr unsigned kTiEnd = 0xFFFFFFFFu;
+constexpr unsigned kTiMaxSlots = 12;
+constexpr unsigned kTiHalo = 128;               // halo rows copied per step (32 B each; index in 8 bits)
+constexpr unsigned kTiHaloLag = 4;              // steps between a step's records copy and its halo copies
+constexpr unsigned kTiGrabLead = 4;             // steps before a tile's end at which the next tile is taken
+constexpr size_t kTiSmemCap = 227u * 1024u;
+static_assert(kTiWarps >= 1 && kTiWarps <= 15, "named barrier of the consumer warps");
+static_assert(kTiHalo <= 256, "halo index in 8 bits");
+
+__host__ __device__ inline unsigned pad16u(unsigned x) { return (x + 15u) & ~15u; }
+__host__ __device__ inline unsigned round4u(unsigned x) { return (x + 3u) & ~3u; }
+
+struct TileGeom {
+  unsigned M, Mc, nv, nch, vo, gbytes;
+};
+
+inline TileGeom tile_geom(unsigned M, unsigned S, bool fwd) {
+  TileGeom g;
+  g.M = M;
+  g.Mc = round4u(M);
+  g.nv = 3u * M + (fwd ? 3u : 0u);
+  g.nch = (g.nv * S + 15u) / 16u;
+  g.vo = kTiHead + 4u * kTiG * g.Mc;
+  g.gbytes = g.vo + g.nch * 30u * 16u;
+  return g;
+}
+
+}  // namespace
+
+// Slot layout: records (max_groups groups), right-hand side (32 values per
+// group), halo list (kTiHalo u32), halo values (kTiHalo x 32 bytes).
+struct SlotGeom {
+  unsigned in_off, hl_off, hd_off, bytes;
+};
+
+namespace {
+
+inline SlotGeom slot_geom(unsigned max_groups, unsigned gbytes, unsigned S) {
+  SlotGeom s;
+  s.in_off = max_groups * gbytes;
+  s.hl_off = s.in_off + max_groups * 32u * S;
+  s.hd_off = s.hl_off + kTiHalo * 4u;
+  s.bytes = s.hd_off + kTiHalo * 32u;
+  return s;
+}
+
+// Shared memory of the sweep kernel: barriers [0, 288), slot descriptors
+// [512, 896), stop flags [960, 968), the tile's results (kTiRows + 1 rows),
+// the slot ring.
+__host__ __device__ inline size_t tile_xs_off() { return 1024; }
+__host__ __device__ inline size_t tile_ring_off(unsigned S) {
+  return tile_xs_off() + pad16u((kTiRows + 1u) * 3u * S);
+}
+inline size_t tile_smem(unsigned S, unsigned slots, unsigned slot_bytes) {
+  return tile_ring_off(S) + (size_t)slots * slot_bytes;
+}
+
+// The records of one value type: group headers and codes from `gmeta`
+// (10 + 10 Mc u32 per group), values from the factors.
+template <typename T, bool FWD>
+__global__ void k_tile_fill(unsigned n, size_t ngroups, const unsigned *__restrict__ rs,
+                            const unsigned *__restrict__ dia, const T *__restrict__ vcrs,
+                            const T *__restrict__ vdia, const unsigned *__restrict__ rec_of,
+                            const unsigned *__restrict__ gmeta, unsigned M, unsigned Mc, unsigned vo,
+                            unsigned gbytes, unsigned char *__restrict__ bytes) {
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nth = (size_t)gridDim.x * blockDim.x;
+  const size_t words = (size_t)kTiG * (Mc + 1u);
+  for (size_t e = tid; e < ngroups * words; e += nth) {
+    const size_t g = e / words, k = e - g * words;
+    unsigned *gp = reinterpret_cast<unsigned *>(bytes + g * gbytes);
+    const unsigned w = gmeta[e];
+    if (k < kTiG)
+      gp[k] = w;
+    else
+      gp[kTiHead / 4 + (k - kTiG)] = w;
+  }
+  const unsigned nv = 3u * M + (FWD ? 3u : 0u);
+  const size_t per_row = 3u * (size_t)nv;
+  for (size_t e = tid; e < (size_t)n * per_row; e += nth) {
+    const unsigned i = (unsigned)(e / per_row);
+    const unsigned r = (unsigned)(e - (size_t)i * per_row);
+    const unsigned a = r / nv, j = r - a * nv;
+    const unsigned s0 = FWD ? rs[i] : dia[i], s1 = FWD ? dia[i] : rs[i + 1];
+    T v;
+    if (FWD && j < 3u) {
+      v = vdia[(size_t)i * 9 + a * 3 + j];
+    } else {
+      const unsigned jb = FWD ? j - 3u : j;
+      const unsigned b = jb / 3u, c = jb - 3u * b;
+      v = (s0 + b < s1) ? vcrs[(size_t)(s0 + b) * 9 + a * 3 + c] : T(0);
+    }
+    const unsigned rec = rec_of[i];
+    const size_t g = rec / kTiG;
+    const unsigned q = rec - (unsigned)g * kTiG;
+    const unsigned lane = 3u * q + a;
+    const unsigned byte = j * (unsigned)sizeof(T);
+    *reinterpret_cast<T *>(bytes + g * gbytes + vo + ((byte >> 4) * 30u + lane) * 16u + (byte & 15u)) = v;
+  }
+}
+
+// The right-hand side in the records' row order: in_g[32 g + 3q + a] =
+// in[3 row(g, q) + a] (0 for lanes without a row).
+template <typename T>
+__global__ void k_tile_gather_in(size_t ngroups, const unsigned *__restrict__ gmeta, unsigned words,
+                                 const T *__restrict__ in, T *__restrict__ in_g) {
+  const size_t nth = (size_t)gridDim.x * blockDim.x;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < ngroups * 32u; e += nth) {
+    const size_t g = e >> 5;
+    const unsigned l = (unsigned)(e & 31u), q = l / 3u, a = l - 3u * q;
+    const unsigned row = l < 30u ? gmeta[g * words + q] : ~0u;
+    in_g[e] = row != ~0u ? in[(size_t)row * 3 + a] : T(0);
+  }
+}
+
+__device__ __forceinline__ void bar_consumers() {
+  asm volatile("bar.sync 1, %0;" ::"r"(kTiCons) : "memory");
+}
+
+// tiles[2t] = {first step, steps, first group, groups}, tiles[2t+1] = {first
+// halo word, halo words, 0, 0}; steps[2s] = {first group, rows, local index of
+// the step's first row, groups}, steps[2s+1] = {first halo word, halo rows, 0,
+// 0} (halo words of a step padded to four). ctr[0] hands out tiles beyond the
+// grid, ctr[1] counts finished CTAs (the last one resets both).
+template <typename T, bool FWD, unsigned MR>
+__global__ void __launch_bounds__(kTiThreads, 1)
+    k_sweep_tiles(unsigned ntiles, const uint4 *__restrict__ tiles, const uint4 *__restrict__ steps,
+                  const unsigned char *__restrict__ bytes, const T *__restrict__ in_g,
+                  const unsigned *__restrict__ halo, unsigned M, unsigned vo, unsigned gbytes, unsigned nslots,
+                  SlotGeom sg, T *out, unsigned *ctr, int *err, unsigned long long timeout_ns, const int *skip) {
+  extern __shared__ __align__(128) unsigned char ti_smem[];
+  if (skip && *skip) return;
+  uint64_t *full = reinterpret_cast<uint64_t *>(ti_smem);
+  uint64_t *empty = full + kTiMaxSlots;
+  uint64_t *hbar = empty + kTiMaxSlots;
+  uint4 *smeta = reinterpret_cast<uint4 *>(ti_smem + 512);  // 2 per slot
+  volatile int *sflag = reinterpret_cast<volatile int *>(ti_smem + 960);  // [2]
+  T *xs = reinterpret_cast<T *>(ti_smem + tile_xs_off());
+  unsigned char *ring = ti_smem + tile_ring_off((unsigned)sizeof(T));
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+
+  if (threadIdx.x == 0) {
+    for (unsigned k = 0; k < nslots; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], 1);
+      mbar_init(&hbar[k], 32);  // one cp.async arrival per producer lane
+    }
+    sflag[0] = sflag[1] = 0;
+    mbar_fence_init();
+  }
+  if (threadIdx.x < 3) xs[(size_t)kTiZero * 3 + threadIdx.x] = T(0);
+  __syncthreads();
+
+  if (warp == kTiWarps) {
+    // ---- producer warp: walks the CTA's tiles and copies their steps (lane
+    // 0 issues the bulk copies), then each step's halo values kTiHaloLag steps
+    // later (all lanes). Step descriptors come in batches of 32, one per lane.
+    auto shfl4 = [&](const uint4 &v, unsigned src) {
+      return make_uint4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                        __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+    };
+    auto load_batch = [&](const uint4 &t0, unsigned base, uint4 &sa, uint4 &sb) {
+      sa = sb = make_uint4(0u, 0u, 0u, 0u);
+      if (base + lane < t0.y) {
+        sa = steps[2 * (t0.x + base + lane)];
+        sb = steps[2 * (t0.x + base + lane) + 1];
+      }
+    };
+    // halo values of step u into its slot; every lane arrives on the slot's
+    // halo barrier once its copies are complete
+    auto halo_copy = [&](unsigned u) {
+      const unsigned su = u % nslots;
+      if (mbar_wait_bounded(&full[su], (u / nslots) & 1u, timeout_ns)) {
+        const uint4 m1 = smeta[2 * su + 1];
+        if (smeta[2 * su].w != kTiEnd) {
+          const unsigned hc = min(m1.y, kTiHalo);
+          unsigned char *sp = ring + (size_t)su * sg.bytes;
+          const unsigned *hl = reinterpret_cast<const unsigned *>(sp + sg.hl_off);
+          for (unsigned k = lane; k < 2u * hc; k += 32u) {
+            const unsigned h = k >> 1, hr = hl[h];
+            const size_t byte = ((size_t)hr * 3u * sizeof(T)) & ~(size_t)15;
+            cpa16_l2(sp + sg.hd_off + h * 32u + (k & 1u) * 16u,
+                     reinterpret_cast<const unsigned char *>(out) + byte + (k & 1u) * 16u);
+          }
+        }
+      } else if (lane == 0) {
+        atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
+      }
+      cpa_arrive_noinc(&hbar[su]);
+    };
+    unsigned cur = blockIdx.x, cs = 0, base = 0, issued = 0, halo_next = 0;
+    uint4 td = tiles[2 * cur], sa, sb;
+    load_batch(td, 0, sa, sb);
+    unsigned tok = 0;
+    int grab = 0;  // 0: next tile not taken, 1: taken, 2: its descriptors loaded
+    unsigned next = kTiEnd;
+    uint4 ntd = make_uint4(0u, 0u, 0u, 0u), nsa, nsb;
+    auto take_next = [&]() {
+      if (lane == 0) tok = atomicAdd(ctr, 1u);
+      grab = 1;
+    };
+    auto load_next = [&]() {
+      next = gridDim.x + __shfl_sync(0xffffffffu, tok, 0);
+      if (next < ntiles) {
+        ntd = tiles[2 * next];
+        load_batch(ntd, 0, nsa, nsb);
+        if (lane == 0) {
+          // the next tile's records and halo lists into L2
+          const uint4 n1 = tiles[2 * next + 1];
+          bulk_prefetch_l2(bytes + (size_t)ntd.z * gbytes, ntd.w * gbytes);
+          if (n1.y) bulk_prefetch_l2(halo + n1.x, n1.y * 4u);
+        }
+      }
+      grab = 2;
+    };
+    for (;;) {
+      if (cs == td.y) {  // the current tile is issued: switch to the next one
+        if (grab == 0) take_next();
+        if (grab == 1) load_next();
+        cur = next;
+        cs = base = 0;
+        grab = 0;
+        if (cur < ntiles) {
+          td = ntd;
+          sa = nsa;
+          sb = nsb;
+        }
+      }
+      const unsigned slot = issued % nslots;
+      int ok = 1;
+      if (lane == 0 && issued >= nslots &&
+          !mbar_wait_bounded(&empty[slot], ((issued / nslots) - 1u) & 1u, timeout_ns)) {
+        atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
+        ok = 0;
+      }
+      if (!__shfl_sync(0xffffffffu, ok, 0)) break;  // the consumers stop on their own bounded waits
+      if (cur >= ntiles) {
+        if (lane == 0) {
+          smeta[2 * slot] = make_uint4(0u, 0u, 0u, kTiEnd);
+          mbar_arrive(&full[slot]);
+        }
+        ++issued;
+        break;
+      }
+      if (cs - base == 32u) {
+        base += 32u;
+        load_batch(td, base, sa, sb);
+      }
+      if (grab == 0 && cs + kTiGrabLead >= td.y)
+        take_next();
+      else if (grab == 1 && cs + kTiGrabLead / 2 >= td.y)
+        load_next();
+      const uint4 st = shfl4(sa, cs - base), sh = shfl4(sb, cs - base);
+      if (lane == 0) {
+        smeta[2 * slot] = make_uint4(st.y, st.z, st.w, cur);
+        smeta[2 * slot + 1] = sh;
+        unsigned char *sp = ring + (size_t)slot * sg.bytes;
+        const unsigned nrec = st.w * gbytes, nin = st.w * 32u * (unsigned)sizeof(T);
+        const unsigned nhl = round4u(sh.y) * 4u;
+        mbar_arrive_expect_tx(&full[slot], nrec + nin + nhl);
+        tma_load_1d(sp, bytes + (size_t)st.x * gbytes, nrec, &full[slot]);
+        tma_load_1d(sp + sg.in_off, in_g + (size_t)st.x * 32u, nin, &full[slot]);
+        if (nhl) tma_load_1d(sp + sg.hl_off, halo + sh.x, nhl, &full[slot]);
+      }
+      ++cs;
+      ++issued;
+      while (halo_next + kTiHaloLag < issued) halo_copy(halo_next++);
+    }
+    // the halo copies of the steps issued last (the END slot needs none)
+    const unsigned last = issued > 0 ? issued - 1u : 0u;
+    while (halo_next < last) halo_copy(halo_next++);
+    cpa_wait<0>();
+    if (lane == 0) {
+      // wait (bounded) for the bulk copies of the last slots before leaving
+      const unsigned lo = issued > nslots ? issued - nslots : 0u;
+      for (unsigned i = lo; i < issued; ++i) mbar_wait_bounded(&full[i % nslots], (i / nslots) & 1u, timeout_ns);
+      __threadfence();
+      const unsigned done = atomicAdd(ctr + 1, 1u);
+      if (done == gridDim.x - 1u) {
+        atomicExch(ctr, 0u);
+        atomicExch(ctr + 1, 0u);
+      }
+    }
+    return;
+  }
+
+  // ---- consumers
+  const unsigned q = lane / 3u, a = lane - 3u * q;
+  const bool lane_ok = lane < 30u;
+  const unsigned Mc = round4u(M);
+  for (unsigned s = 0;; ++s) {
+    const unsigned slot = s % nslots;
+    const unsigned par = (s / nslots) & 1u;
+    bool ok = mbar_wait_bounded(&full[slot], par, timeout_ns);
+    const uint4 meta = smeta[2 * slot];  // {rows, local base, groups, tile}
+    const bool end = ok && meta.w == kTiEnd;
+    if (ok && !end) ok = mbar_wait_bounded(&hbar[slot], par, timeout_ns);
+    if (!ok) {
+      atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
+      sflag[s & 1u] = 1;
+    }
+    if (ok && !end && warp < meta.z) {
+      unsigned char *sp = ring + (size_t)slot * sg.bytes;
+      const unsigned char *gp = sp + (size_t)warp * gbytes;
+      const unsigned row = lane_ok ? reinterpret_cast<const unsigned *>(gp)[q] : ~0u;
+      const unsigned local = meta.y + warp * kTiG + q;
+      // the lane's values first (independent of the codes)
+      constexpr unsigned NVR = 3u * MR + 3u;
+      constexpr unsigned PER = 16u / sizeof(T);
+      const unsigned nv = FWD ? 3u * M + 3u : 3u * M;
+      T v[NVR];
+      const unsigned char *vp = gp + vo + (lane_ok ? lane : 0u) * 16u;
+#pragma unroll
+      for (unsigned k = 0; k < (NVR + PER - 1) / PER; ++k) {
+        if (k * PER < nv) {
+          if constexpr (sizeof(T) == 4) {
+            const float4 c = *reinterpret_cast<const float4 *>(vp + k * 480u);
+            if (k * 4 + 0 < NVR) v[k * 4 + 0] = c.x;
+            if (k * 4 + 1 < NVR) v[k * 4 + 1] = c.y;
+            if (k * 4 + 2 < NVR) v[k * 4 + 2] = c.z;
+            if (k * 4 + 3 < NVR) v[k * 4 + 3] = c.w;
+          } else {
+            const double2 c = *reinterpret_cast<const double2 *>(vp + k * 480u);
+            if (k * 2 + 0 < NVR) v[k * 2 + 0] = c.x;
+            if (k * 2 + 1 < NVR) v[k * 2 + 1] = c.y;
+          }
+        } else {
+#pragma unroll
+          for (unsigned e = 0; e < PER; ++e)
+            if (k * PER + e < NVR) v[k * PER + e] = T(0);
+        }
+      }
+      // dependency codes (Mc per row, 16-byte loads), then every x value with
+      // no branch: a row of the tile (xs), a halo copy (hd) or, for rows read
+      // in global memory, the pending marker (polled below)
+      unsigned cd[MR];
+      {
+        const uint4 *cw = reinterpret_cast<const uint4 *>(gp + kTiHead + (lane_ok ? q : 0u) * Mc * 4u);
+#pragma unroll
+        for (unsigned k = 0; k < MR / 4; ++k) {
+          const uint4 c = (4u * k < Mc) ? cw[k]
+                                        : make_uint4(kTiLocal | kTiZero, kTiLocal | kTiZero, kTiLocal | kTiZero,
+                                                     kTiLocal | kTiZero);
+          cd[4 * k + 0] = c.x;
+          cd[4 * k + 1] = c.y;
+          cd[4 * k + 2] = c.z;
+          cd[4 * k + 3] = c.w;
+        }
+      }
+      const unsigned char *hd = sp + sg.hd_off;
+      T xv[MR][3];
+#pragma unroll
+      for (unsigned b = 0; b < MR; ++b) {
+        const unsigned c = cd[b];
+        const bool loc = (c & kTiLocal) != 0u, glob = !loc && (c & kTiGlobal) != 0u;
+        const unsigned off = sizeof(T) == 4 ? ((c >> 8) & 3u) * 4u : ((c >> 10) & 1u) * 8u;
+        const T *xp = loc ? xs + (size_t)(c & ~kTiLocal) * 3
+                          : (glob ? xs + (size_t)kTiZero * 3
+                                  : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off));
+        const T x0 = xp[0], x1 = xp[1], x2 = xp[2];
+        const T pv = pending_value<T>();
+        xv[b][0] = glob ? pv : x0;
+        xv[b][1] = glob ? pv : x1;
+        xv[b][2] = glob ? pv : x2;
+      }
+      T acc = reinterpret_cast<const T *>(sp + sg.in_off)[warp * 32u + lane];
+      if (row != ~0u) {
+        // values still pending (a halo copy taken too early, or a row read in
+        // global memory): polled in global memory
+        bool pend = false;
+#pragma unroll
+        for (unsigned b = 0; b < MR; ++b)
+          pend |= is_pending(xv[b][0]) | is_pending(xv[b][1]) | is_pending(xv[b][2]);
+        if (pend) {
+          const unsigned *hl = reinterpret_cast<const unsigned *>(sp + sg.hl_off);
+          const unsigned long long t0 = globaltimer_ns();
+          unsigned spins = 0;
+          for (;;) {
+            pend = false;
+#pragma unroll
+            for (unsigned b = 0; b < MR; ++b) {
+              const unsigned c = cd[b];
+              if (c & kTiLocal) continue;
+              const unsigned r = (c & kTiGlobal) ? (c & ~kTiGlobal) : hl[c & 0xFFu];
+              const T *xp = out + (size_t)r * 3;
+#pragma unroll
+              for (unsigned k = 0; k < 3; ++k)
+                if (is_pending(xv[b][k])) {
+                  xv[b][k] = ld_relaxed(xp + k);
+                  pend |= is_pending(xv[b][k]);
+                }
+            }
+            if (!pend) break;
+            if ((++spins & 15u) == 0 && (ld_relaxed(err) != 0 || globaltimer_ns() - t0 > timeout_ns)) {
+              atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
+#pragma unroll
+              for (unsigned b = 0; b < MR; ++b)
+#pragma unroll
+                for (unsigned k = 0; k < 3; ++k)
+                  if (is_pending(xv[b][k])) xv[b][k] = T(0);
+              break;
+            }
+          }
+        }
+      }
+      // three partial sums (shorter dependent chains), then the lane's total
+      constexpr unsigned off = FWD ? 3u : 0u;
+      T p0 = T(0), p1 = T(0), p2 = T(0);
+#pragma unroll
+      for (unsigned b = 0; b < MR; ++b) {
+        if (b < M) {
+          p0 += v[off + 3 * b + 0] * xv[b][0];
+          p1 += v[off + 3 * b + 1] * xv[b][1];
+          p2 += v[off + 3 * b + 2] * xv[b][2];
+        }
+      }
+      acc -= (p0 + p1) + p2;
+      T z;
+      if constexpr (FWD) {
+        // z_a = sum_c Dinv[a][c] u_c, u_c on lane 3q + c (every lane takes part)
+        const unsigned base = 3u * q;
+        const T u0 = __shfl_sync(0xffffffffu, acc, base);
+        const T u1 = __shfl_sync(0xffffffffu, acc, base + 1u);
+        const T u2 = __shfl_sync(0xffffffffu, acc, base + 2u);
+        z = v[0] * u0 + v[1] * u1 + v[2] * u2;
+      } else {
+        z = acc;
+      }
+      if (row != ~0u) {
+        xs[(size_t)local * 3 + a] = z;
+        st_relaxed(out + (size_t)row * 3 + a, z);
+      }
+    }
+    bar_consumers();
+    if (sflag[s & 1u] != 0 || end) break;
+    if (threadIdx.x == 0) mbar_arrive(&empty[slot]);
+  }
+}
+
+// ---- host: the tile partition -----------------------------------------------
+
+template <typename V>
+int tile_to_host(std::vector<V> &h, const V *d, size_t n) {
+  h.resize(n);
+  if (n) DFM2G_CUDA(cudaMemcpy(h.data(), d, n * sizeof(V), cudaMemcpyDeviceToHost));
+  return DFM2G_OK;
+}
+
+}  // namespace
+
+// The tile partition of one direction (host only). `order` is the sweep's
+// (level, row) order. Each tile grows from the first unassigned row of that
+// order (its seed: every row it depends on has a lower level, so it is
+// assigned) in breadth-first layers: a row is offered at layer 1 + the lowest
+// layer of the rows of this tile it depends on, and offers are taken layer by
+// layer (in level order inside a layer); a row joins once all its dependencies
+// are assigned, as long as the tile has fewer than `max_rows` rows and the
+// row's local level fewer than `max_width` rows. On a grid whose dependencies
+// point to lower neighbours the layers are the shells of a box around the
+// seed, so a tile of 8^3 rows is an 8x8x8 box, and the tiles are numbered along
+// the wavefront. Outputs per row: its tile and local level; m = the most
+// dependencies of a row.
+void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const unsigned *col, const unsigned *order,
+                    bool fwd, unsigned max_rows, unsigned max_width, std::vector<unsigned> &tile_of,
+                    std::vector<unsigned> &lev, unsigned &ntiles, unsigned &m) {
+  const unsigned none = ~0u;
+  tile_of.assign(n, none);
+  lev.assign(n, 0u);
+  m = 0;
+  auto dep_range = [&](unsigned i, unsigned &s0, unsigned &s1) {
+    s0 = fwd ? rs[i] : dia[i];
+    s1 = fwd ? dia[i] : rs[i + 1];
+  };
+  std::vector<unsigned> pos(n);  // rank in the level order
+  for (unsigned k = 0; k < n; ++k) pos[order[k]] = k;
+  // successors: rows that depend on each row
+  std::vector<unsigned> sptr(n + 1, 0u), succ;
+  for (unsigned i = 0; i < n; ++i) {
+    unsigned s0, s1;
+    dep_range(i, s0, s1);
+    m = std::max(m, s1 - s0);
+    for (unsigned s = s0; s < s1; ++s) sptr[col[s] + 1]++;
+  }
+  for (unsigned i = 0; i < n; ++i) sptr[i + 1] += sptr[i];
+  succ.resize(sptr[n]);
+  {
+    std::vector<unsigned> fill(sptr.begin(), sptr.end() - 1);
+    for (unsigned i = 0; i < n; ++i) {
+      unsigned s0, s1;
+      dep_range(i, s0, s1);
+      for (unsigned s = s0; s < s1; ++s) succ[fill[col[s]]++] = i;
+    }
+  }
+  // offers (layer, rank), smallest first; layer_of[r]: the lowest layer r was offered at in this tile
+  using Offer = std::pair<unsigned, unsigned>;
+  std::priority_queue<Offer, std::vector<Offer>, std::greater<Offer>> heap;
+  std::vector<unsigned> layer_of(n, none), offered;  // offered: rows whose layer_of is set in this tile
+  std::vector<unsigned> width;
+  unsigned cursor = 0, t = 0;
+  for (;;) {
+    while (cursor < n && tile_of[order[cursor]] != none) ++cursor;
+    if (cursor >= n) break;
+    const unsigned seed = order[cursor];
+    for (unsigned r : offered) layer_of[r] = none;
+    offered.clear();
+    while (!heap.empty()) heap.pop();
+    heap.push(Offer(0u, pos[seed]));
+    layer_of[seed] = 0;
+    offered.push_back(seed);
+    width.assign(max_rows + 1u, 0u);
+    unsigned count = 0;
+    while (!heap.empty() && count < max_rows) {
+      const Offer o = heap.top();
+      heap.pop();
+      const unsigned r = order[o.second];
+      if (tile_of[r] != none) continue;
+      unsigned s0, s1;
+      dep_range(r, s0, s1);
+      bool ok = true;
+      unsigned lv = 0;
+      for (unsigned s = s0; s < s1; ++s) {
+        const unsigned d = col[s];
+        if (tile_of[d] == none) {
+          ok = false;
+          break;
+        }
+        if (tile_of[d] == t) lv = std::max(lv, lev[d] + 1u);
+      }
+      if (!ok || width[lv] >= max_width) continue;  // offered again when another dependency joins
+      tile_of[r] = t;
+      lev[r] = lv;
+      width[lv]++;
+      ++count;
+      const unsigned next = o.first + 1u;
+      for (unsigned k = sptr[r]; k < sptr[r + 1]; ++k) {
+        const unsigned u = succ[k];
+        if (tile_of[u] != none) continue;
+        if (layer_of[u] == none) offered.push_back(u);
+        layer_of[u] = std::min(layer_of[u], next);
+        heap.push(Offer(layer_of[u], pos[u]));
+      }
+    }
+    ++t;
+  }
+  ntiles = t;
+}
+
+namespace {
+
+// Register rounds of the kernel: dependency slots rounded up to 4 (codes are
+// loaded in fours), 8 or 16.
+unsigned tile_rounds(unsigned m) { return round4u(m) <= 8 ? 8u : 16u; }
+
+int tile_build(dfm2g_ilu_s *p, bool fwd, TileSched &ts) {
+  ts.ok = false;
+  const unsigned n = p->nblk;
+  if (n >= kTiGlobal) return DFM2G_OK;  // row ids must fit the codes' 30 bits
+  std::vector<unsigned> rs, col, dia, order;
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  DFM2G_TRY(tile_to_host(rs, p->row_start.p, (size_t)n + 1));
+  DFM2G_TRY(tile_to_host(col, p->col.p, p->nnz));
+  DFM2G_TRY(tile_to_host(dia, p->dia_ind.p, n));
+  DFM2G_TRY(tile_to_host(order, fwd ? p->order_f.p : p->order_b.p, n));
+  std::vector<unsigned> tile_of, lev;
+  unsigned ntiles = 0, m = 0;
+  tile_partition(n, rs.data(), dia.data(), col.data(), order.data(), fwd, kTiRows, kTiWidth, tile_of, lev, ntiles,
+                 m);
+  if (m > 16) return DFM2G_OK;  // rows too long for the register rounds
+  const unsigned M = std::max(m, 1u);
+  // rows of each tile by (local level, level order)
+  std::vector<unsigned> tstart(ntiles + 1, 0u), trows(n);
+  for (unsigned i = 0; i < n; ++i) tstart[tile_of[i] + 1]++;
+  for (unsigned t = 0; t < ntiles; ++t) tstart[t + 1] += tstart[t];
+  {
+    std::vector<unsigned> fill(tstart.begin(), tstart.end() - 1);
+    for (unsigned k = 0; k < n; ++k) trows[fill[tile_of[order[k]]]++] = order[k];
+  }
+  std::vector<unsigned> local(n);
+  for (unsigned t = 0; t < ntiles; ++t) {
+    unsigned *b = trows.data() + tstart[t], *e = trows.data() + tstart[t + 1];
+    std::stable_sort(b, e, [&](unsigned x, unsigned y) { return lev[x] < lev[y]; });
+    const unsigned nr = (unsigned)(e - b);
+    for (unsigned k = 0; k < nr; ++k) local[b[k]] = k;
+  }
+  // group records (row ids, codes) and per-step halo lists; rows whose 32-byte
+  // copy (FP32 or FP64) would pass the end of the vector are read in global
+  // memory instead (kTiGlobal codes), as are halo rows beyond kTiHalo
+  const unsigned Mc = round4u(M);
+  const size_t words = (size_t)kTiG * (Mc + 1u);
+  auto copyable = [&](unsigned d) {
+    return (((size_t)d * 12u) & ~(size_t)15) + 32u <= (size_t)n * 12u &&
+           (((size_t)d * 24u) & ~(size_t)15) + 32u <= (size_t)n * 24u;
+  };
+  std::vector<uint4> tiles(2 * (size_t)ntiles), steps;
+  std::vector<unsigned> rec_of(n), gmeta, halo, hidx(n, ~0u), hrows;
+  size_t ngroups = 0;
+  unsigned max_groups = 0, max_halo = 0;
+  for (unsigned t = 0; t < ntiles; ++t) {
+    const unsigned *b = trows.data() + tstart[t];
+    const unsigned nr = tstart[t + 1] - tstart[t];
+    tiles[2 * t] = make_uint4((unsigned)(steps.size() / 2), 0u, (unsigned)ngroups, 0u);
+    tiles[2 * t + 1] = make_uint4((unsigned)halo.size(), 0u, 0u, 0u);
+    unsigned k = 0;
+    while (k < nr) {
+      unsigned k1 = k;
+      while (k1 < nr && lev[b[k1]] == lev[b[k]]) ++k1;
+      const unsigned w = k1 - k, ng = (w + kTiG - 1) / kTiG;
+      hrows.clear();
+      for (unsigned u = k; u < k1; ++u) {
+        const unsigned i = b[u];
+        const unsigned s0 = fwd ? rs[i] : dia[i], s1 = fwd ? dia[i] : rs[i + 1];
+        for (unsigned s = s0; s < s1; ++s) {
+          const unsigned d = col[s];
+          if (tile_of[d] != t && hidx[d] == ~0u && copyable(d) && hrows.size() < kTiHalo) {
+            hidx[d] = (unsigned)hrows.size();
+            hrows.push_back(d);
+          }
+        }
+      }
+      const unsigned hoff = (unsigned)halo.size(), hc = (unsigned)hrows.size();
+      for (unsigned h = 0; h < hc; ++h) halo.push_back(hrows[h]);
+      while (halo.size() % 4u) halo.push_back(0u);
+      max_halo = std::max(max_halo, hc);
+      gmeta.resize((ngroups + ng) * words, 0u);
+      for (size_t g = ngroups; g < ngroups + ng; ++g)
+        for (unsigned q = 0; q < kTiG; ++q) {
+          gmeta[g * words + q] = ~0u;
+          for (unsigned bb = 0; bb < Mc; ++bb) gmeta[g * words + kTiG + q * Mc + bb] = kTiLocal | kTiZero;
+        }
+      for (unsigned u = 0; u < w; ++u) {
+        const unsigned i = b[k + u];
+        const size_t g = ngroups + u / kTiG;
+        const unsigned q = u % kTiG;
+        rec_of[i] = (unsigned)(g * kTiG + q);
+        gmeta[g * words + q] = i;
+        const unsigned s0 = fwd ? rs[i] : dia[i], s1 = fwd ? dia[i] : rs[i + 1];
+        for (unsigned s = s0; s < s1; ++s) {
+          const unsigned d = col[s];
+          unsigned code;
+          if (tile_of[d] == t) {
+            code = kTiLocal | local[d];
+          } else if (hidx[d] != ~0u) {
+            const unsigned o32 = (unsigned)(((size_t)d * 12u) & 15u) / 4u;
+            const unsigned o64 = (unsigned)(((size_t)d * 24u) & 15u) / 8u;
+            code = hidx[d] | (o32 << 8) | (o64 << 10);
+          } else {
+            code = kTiGlobal | d;
+          }
+          gmeta[g * words + kTiG + q * Mc + (s - s0)] = code;
+        }
+      }
+      for (unsigned d : hrows) hidx[d] = ~0u;
+      steps.push_back(make_uint4((unsigned)ngroups, w, k, ng));
+      steps.push_back(make_uint4(hoff, hc, 0u, 0u));
+      max_groups = std::max(max_groups, ng);
+      ngroups += ng;
+      k = k1;
+    }
+    tiles[2 * t].y = (unsigned)(steps.size() / 2) - tiles[2 * t].x;
+    tiles[2 * t].w = (unsigned)ngroups - tiles[2 * t].z;
+    tiles[2 * t + 1].y = (unsigned)halo.size() - tiles[2 * t + 1].x;
+  }
+  if ((ngroups + 1) * kTiG >= 0xFFFFFFFFull || halo.size() >= 0xFFFFFFFFull) return DFM2G_OK;
+  ts.ntiles = ntiles;
+  ts.nsteps = (unsigned)(steps.size() / 2);
+  ts.ngroups = ngroups;
+  ts.max_groups = max_groups;
+  ts.max_halo = max_halo;
+  ts.M = M;
+  DFM2G_TRY(ts.tiles.resize(tiles.size() + 2));
+  DFM2G_TRY(ts.steps.resize(steps.size() + 2));
+  DFM2G_TRY(ts.rec_of.resize((size_t)n + 1));
+  DFM2G_TRY(ts.gmeta.resize(gmeta.size() + 1));
+  DFM2G_TRY(ts.halo.resize(halo.size() + 4));
+  DFM2G_TRY(ts.ctr.resize(2));
+  DFM2G_CUDA(cudaMemcpy(ts.tiles.p, tiles.data(), sizeof(uint4) * tiles.size(), cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.steps.p, steps.data(), sizeof(uint4) * steps.size(), cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.rec_of.p, rec_of.data(), sizeof(unsigned) * n, cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.gmeta.p, gmeta.data(), sizeof(unsigned) * gmeta.size(), cudaMemcpyHostToDevice));
+  if (!halo.empty())
+    DFM2G_CUDA(cudaMemcpy(ts.halo.p, halo.data(), sizeof(unsigned) * halo.size(), cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemset(ts.ctr.p, 0, 2 * sizeof(unsigned)));
+  ts.ok = true;
+  return DFM2G_OK;
+}
+
+template <typename T, bool FWD>
+void *tile_kernel(unsigned MR) {
+  if (MR <= 8) return (void *)k_sweep_tiles<T, FWD, 8>;
+  return (void *)k_sweep_tiles<T, FWD, 16>;
+}
+
+// Lets `kernel` launch with `smem` bytes of dynamic shared memory. The
+// attribute belongs to the kernel, not to a pattern, so it only ever grows
+// (per kernel and device).
+int tile_allow_smem(void *kernel, size_t smem) {
+  struct Entry {
+    void *kernel;
+    int device;
+    size_t smem;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> done;
+  std::lock_guard<std::mutex> lock(mu);
+  const int dev = ctx().device;
+  for (auto &d : done) {
+    if (d.kernel != kernel || d.device != dev) continue;
+    if (d.smem >= smem) return DFM2G_OK;
+    DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    d.smem = smem;
+    return DFM2G_OK;
+  }
+  DFM2G_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  done.push_back(Entry{kernel, dev, smem});
+  return DFM2G_OK;
+}
+
+DevBuf<unsigned char> &tile_bytes(TileSched &ts, double) { return ts.bytes64; }
+DevBuf<unsigned char> &tile_bytes(TileSched &ts, float) { return ts.bytes32; }
+DevBuf<unsigned char> &tile_in(TileSched &ts, double) { return ts.in64; }
+DevBuf<unsigned char> &tile_in(TileSched &ts, float) { return ts.in32; }
+
+}  // namespace
+
+// Builds the tiles of one direction (first use), rewrites the records of the
+// value type after each decomposition, gathers the right-hand side into the
+// records' row order and launches the sweep; false in *usable when the
+// pattern does not suit the schedule (rows with more than 16 dependencies, or
+// a ring that does not fit), or when !may_alloc and the tiles or records do
+// not exist yet.
+template <typename T>
+int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
+               unsigned long long timeout, bool may_alloc, bool *usable) {
+  TileSched &ts = forward ? p->ts_f : p->ts_b;
+  *usable = false;
+  if (p->ndim != 3) return DFM2G_OK;
+  if (!may_alloc && (!ts.built || !ts.ok || !tile_bytes(ts, T(0)).p || !tile_in(ts, T(0)).p)) return DFM2G_OK;
+  if (!ts.built) {
+    ts.built = true;
+    DFM2G_TRY(tile_build(p, forward, ts));
+  }
+  if (!ts.ok) return DFM2G_OK;
+  const bool f64 = sizeof(T) == 8;
+  const unsigned S = (unsigned)sizeof(T);
+  const TileGeom g = tile_geom(ts.M, S, forward);
+  const SlotGeom sg = slot_geom(ts.max_groups, g.gbytes, S);
+  // ring slots: as many as fit (at most kTiMaxSlots); the halo copies of a
+  // step run kTiHaloLag steps behind its records, so at least kTiHaloLag + 2
+  unsigned nslots = kTiMaxSlots;
+  while (nslots > kTiHaloLag + 2 && tile_smem(S, nslots, sg.bytes) > kTiSmemCap) --nslots;
+  const size_t smem = tile_smem(S, nslots, sg.bytes);
+  if (smem > kTiSmemCap) return DFM2G_OK;
+  DevBuf<unsigned char> &bytes = tile_bytes(ts, T(0));
+  DevBuf<unsigned char> &in_g = tile_in(ts, T(0));
+  unsigned &ver = f64 ? ts.ver64 : ts.ver32;
+  if (!bytes.p) {
+    DFM2G_TRY(bytes.resize(ts.ngroups * g.gbytes + 16));
+    DFM2G_CUDA(cudaMemsetAsync(bytes.p, 0, ts.ngroups * g.gbytes + 16, stream()));
+    ver = ~0u;
+  }
+  if (!in_g.p) DFM2G_TRY(in_g.resize(ts.ngroups * 32u * S + 16));
+  if (ver != p->factor_version) {
+    const unsigned blocks = ctx().num_sms * 16;
+    if (forward)
+      k_tile_fill<T, true><<<blocks, 256, 0, stream()>>>(p->nblk, ts.ngroups, p->row_start.p, p->dia_ind.p, vcrs,
+                                                          vdia, ts.rec_of.p, ts.gmeta.p, ts.M, g.Mc, g.vo,
+                                                          g.gbytes, bytes.p);
+    else
+      k_tile_fill<T, false><<<blocks, 256, 0, stream()>>>(p->nblk, ts.ngroups, p->row_start.p, p->dia_ind.p, vcrs,
+                                                           vdia, ts.rec_of.p, ts.gmeta.p, ts.M, g.Mc, g.vo,
+                                                           g.gbytes, bytes.p);
+    DFM2G_LAUNCH_CHECK();
+    note_launches(1);
+    ver = p->factor_version;
+  }
+  const unsigned MR = tile_rounds(ts.M);
+  void *kernel = forward ? tile_kernel<T, true>(MR) : tile_kernel<T, false>(MR);
+  DFM2G_TRY(tile_allow_smem(kernel, smem));
+  int &cap = ts.coop[f64 ? 1 : 0];
+  if (cap <= 0) {
+    int per_sm = 0;
+    DFM2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTiThreads, smem));
+    if (per_sm <= 0) return DFM2G_OK;
+    cap = per_sm * ctx().num_sms;
+  }
+  // the right-hand side in the records' row order
+  k_tile_gather_in<T><<<ctx().num_sms * 8, 256, 0, stream()>>>(ts.ngroups, ts.gmeta.p, kTiG * (g.Mc + 1u), in,
+                                                                reinterpret_cast<T *>(in_g.p));
+  DFM2G_LAUNCH_CHECK();
+  const unsigned blocks = std::min<unsigned>((unsigned)cap, ts.ntiles);
+  unsigned ntiles = ts.ntiles, M = ts.M, vo = g.vo, gb = g.gbytes;
+  const uint4 *tiles = ts.tiles.p;
+  const uint4 *steps = ts.steps.p;
+  const unsigned char *bp = bytes.p;
+  const T *ing = reinterpret_cast<const T *>(in_g.p);
+  const unsigned *hl = ts.halo.p;
+  unsigned *ctr = ts.ctr.p;
+  int *err = p->err.p;
+  SlotGeom sgv = sg;
+  void *args[] = {(void *)&ntiles, (void *)&tiles, (void *)&steps,  (void *)&bp,  (void *)&ing,
+                  (void *)&hl,     (void *)&M,     (void *)&vo,     (void *)&gb,  (void *)&nslots,
+                  (void *)&sgv,    (void *)&out,   (void *)&ctr,    (void *)&err, (void *)&timeout,
+                  (void *)&skip};
+  DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(kTiThreads), args, smem, stream()));
+  note_launches(2);
+  *usable = true;
+  return DFM2G_OK;
+}
+
+template int tile_sweep<float>(dfm2g_ilu_s *, bool, const float *, float *, const float *, const float *,
+                               const int *, unsigned long long, bool, bool *);
+template int tile_sweep<double>(dfm2g_ilu_s *, bool, const double *, double *, const double *, const double *,
+                                const int *, unsigned long long, bool, bool *);
+
+// Drops the tiles and records (a new pattern); rebuilt on first use.
+void tile_schedules_reset(dfm2g_ilu_s *p) {
+  for (TileSched *ts : {&p->ts_f, &p->ts_b}) {
+    ts->built = ts->ok = false;
+    ts->ntiles = ts->nsteps = ts->M = ts->max_groups = ts->max_halo = 0;
+    ts->ngroups = 0;
+    ts->ver32 = ts->ver64 = ~0u;
+    ts->coop[0] = ts->coop[1] = 0;
+    ts->tiles.release();
+    ts->steps.release();
+    ts->rec_of.release();
+    ts->gmeta.release();
+    ts->halo.release();
+    ts->bytes32.release();
+    ts->bytes64.release();
+    ts->in32.release();
+    ts->in64.release();
+    ts->ctr.release();
+  }
+}
+
+}  // namespace dfm2g
+
+using namespace dfm2g;
+
+extern "C" {
+
+// Host-only: the tile partition the tile schedule uses. No device work.
+int dfm2g_tile_partition(unsigned n, const unsigned *row_start, const unsigned *col, const unsigned *dia_ind,
+                         const unsigned *order, int backward, unsigned max_rows, unsigned max_width,
+                         unsigned *tile_of, unsigned *level, unsigned *ntiles, unsigned *max_deps) {
+  if (n && (!row_start || !col || !dia_ind || !order || !tile_of || !level))
+    return fail(DFM2G_ERR_ARG, "tile_partition: null array");
+  if (max_rows == 0 || max_width == 0) return fail(DFM2G_ERR_ARG, "tile_partition: zero tile size");
+  std::vector<unsigned> t, lv;
+  unsigned nt = 0, m = 0;
+  tile_partition(n, row_start, dia_ind, col, order, backward == 0, max_rows, max_width, t, lv, nt, m);
+  if (n) {
+    std::copy(t.begin(), t.end(), tile_of);
+    std::copy(lv.begin(), lv.end(), level);
+  }
+  if (ntiles) *ntiles = nt;
+  if (max_deps) *max_deps = m;
+  return DFM2G_OK;
+}
+
+}  // extern "C"

@@ -67,4 +67,29 @@ __device__ __forceinline__ void tma_load_1d(void *dst_smem, const void *src_gmem
       : "memory");
 }
 
+// L2 prefetch of a global range (no shared-memory destination): 16-byte
+// aligned address, size a multiple of 16 bytes.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src_gmem, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src_gmem), "r"(bytes) : "memory");
+}
+
+// 16-byte asynchronous copy global -> shared that bypasses L1 (.cg: the line
+// comes from L2, so values another SM has just written are seen as L2 holds
+// them); completion by commit / wait groups of the issuing thread, or by
+// cpa_arrive_noinc on an mbarrier.
+__device__ __forceinline__ void cpa16_l2(void *dst_smem, const void *src_gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst_smem)), "l"(src_gmem) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Arrives (without raising the pending count) on `bar` once all cp.async
+// copies this thread has issued so far are complete.
+__device__ __forceinline__ void cpa_arrive_noinc(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 }  // namespace dfm2g

@@ -69,12 +69,19 @@ enum dfm2g_sweep {
                                polled in shared memory, only cross-range ones
                                in global memory (when a range's results fit
                                in shared memory)                            */
-  DFM2G_SWEEP_CHAINS = 5    /* sync-free over chains of consecutive rows in
+  DFM2G_SWEEP_CHAINS = 5,   /* sync-free over chains of consecutive rows in
                                which each row depends on the one before: one
                                warp per chain hands that dependency over in
                                registers and polls only the others; the
                                chain's factor blocks are TMA-streamed into
                                shared memory ahead of the warp               */
+  DFM2G_SWEEP_TILES = 6     /* 3x3: rows in compact tiles (grown breadth-
+                               first in dependency order), one CTA per tile
+                               walking the tile's local levels with shared-
+                               memory hand-offs inside the tile and polls
+                               only across tiles; records TMA-streamed per
+                               level. Patterns whose rows have more than 16
+                               blocks in a triangle use the chain schedule */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>       */
@@ -197,9 +204,10 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * The device current at the call must be the library's device
  * (DFM2G_ERR_STATE otherwise). Schedules whose data is built on first use
  * fall back to the sync-free schedule until an ordinary sweep of the same
- * precision has built that data: DFM2G_SWEEP_CHAINS (chain records) and
- * DFM2G_SWEEP_BLOCK (the level-ordered stream and its input buffer). The
- * other schedules (sync-free, levels, groups, parts) need nothing built. */
+ * precision has built that data: DFM2G_SWEEP_TILES (tile records),
+ * DFM2G_SWEEP_CHAINS (chain records) and DFM2G_SWEEP_BLOCK (the level-ordered
+ * stream and its input buffer). The other schedules (sync-free, levels,
+ * groups, parts) need nothing built. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
 /* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE, DFM2G_SWEEP_LEVELS and DFM2G_SWEEP_CHAINS. */
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
@@ -224,6 +232,17 @@ DFM2G_API int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, u
 DFM2G_API int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const unsigned *col,
                                     const unsigned *dia_ind, const unsigned *order, int backward,
                                     unsigned *chain_of, unsigned *nchain, unsigned *max_cross);
+/* Diagnostic, host only (no counterpart in the reference): the tile partition
+ * DFM2G_SWEEP_TILES uses, from a sorted ILU pattern (row offsets, columns,
+ * dia_ind) and the sweep's level order (dfm2g_ilu_get_levels). tile_of[i] is
+ * row i's tile (numbered in dependency order), level[i] its local level inside
+ * the tile; tiles hold at most max_rows rows and max_width rows per local
+ * level; *max_deps the most blocks of a row's triangle (forward: strictly
+ * lower, backward: strictly upper). */
+DFM2G_API int dfm2g_tile_partition(unsigned n, const unsigned *row_start, const unsigned *col,
+                                   const unsigned *dia_ind, const unsigned *order, int backward,
+                                   unsigned max_rows, unsigned max_width, unsigned *tile_of,
+                                   unsigned *level, unsigned *ntiles, unsigned *max_deps);
 
 /* ---- Krylov solvers -------------------------------------------------------- */
 /* Solve_PCG, include/delfem2/lsitrsol.h:80-148, in FP64: x starts at 0; r is

@@ -12,8 +12,8 @@ checked three ways on two calls in a row:
 - through the library's allocation counter (dfm2g_alloc_count), which must
   not move across a no-alloc call, and through the device's free memory.
 A fresh handle is also swept before any ordinary sweep has built a
-schedule's data: the schedules that build on first use (chains, block) then
-sweep sync-free, still without allocating.
+schedule's data: the schedules that build on first use (tiles, chains,
+block) then sweep sync-free, still without allocating.
 This file is named so that pytest collects it last."""
 import ctypes as C
 
@@ -26,7 +26,7 @@ pytestmark = pytest.mark.gpu
 
 SWEEP_TOL_F64 = 1e-10  # as tests/test_gpu_parity.py::test_sweeps_match_oracle
 SWEEP_TOL_F32 = 1e-4   # FP32 sweeps against the FP64 oracle, as there
-MODES = [0, 1, 2, 3, 4, 5]  # sync-free, levels, groups, block, parts, chains
+MODES = [0, 1, 2, 3, 4, 5, 6]  # sync-free, levels, groups, block, parts, chains, tiles
 NU, RHO, G = 0.3, 1.0, (0.0, 0.0, -1e-3)
 
 
@@ -91,8 +91,8 @@ def problem(gpu, port):
 
 def test_noalloc_fresh_handle_before_any_sweep(gpu, port):
     """No ordinary sweep has run on this handle, so no schedule has built its
-    data: every schedule sweeps without allocating (chains and block fall back
-    to sync-free) and matches the oracle."""
+    data: every schedule sweeps without allocating (tiles, chains and block
+    fall back to sync-free) and matches the oracle."""
     import torch
     from delfem2_gb300 import _native as N
     P, o = _system(port, 8, seed=1)
