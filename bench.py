@@ -182,6 +182,7 @@ def cpu_port_ms_per_iter(P, b_host, iters: int):
     vc, vd = P.K.get_values()
     col, dia = P.ilu.pattern()
     ivc, ivd = P.ilu.values()
+    O.solve_pcg(a["psup_ind"], a["psup"], vc, vd, col, dia, ivc, ivd, b_host, 1e-300, 1)  # warm-up
     t = time.perf_counter()
     O.solve_pcg(a["psup_ind"], a["psup"], vc, vd, col, dia, ivc, ivd, b_host, 1e-300, iters)
     return (time.perf_counter() - t) * 1e3 / iters
@@ -205,6 +206,7 @@ def cpu_full_solve_cfg2(iters_sample: int):
     col, dia = O.ilu_pattern0(ind, psup)
     ivc, ivd = O.ilu_copy_value(ind, col, psup, vc, vd)
     O.ilu_decompose(ind, col, dia, ivc, ivd)
+    O.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, 1e-300, 1)  # warm-up, as the headline's sample
     t = time.perf_counter()
     O.solve_pcg(ind, psup, vc, vd, col, dia, ivc, ivd, b, 1e-300, iters_sample)
     per = (time.perf_counter() - t) * 1e3 / iters_sample
