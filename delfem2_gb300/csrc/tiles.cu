@@ -13,9 +13,10 @@
 // row or pencil of rows.
 //
 // One CTA sweeps one tile at a time, step by step: ten rows per consumer
-// warp and step, three lanes per row (one per component a, lane 3q + a of row
-// q), each lane summing row a of the row's dependency blocks against their x
-// values. Nothing on a step's path reads global memory:
+// warp and step, three lanes per row (lane 3q + c of row q): lane c reads
+// component c of each dependency's x and sums column c of the blocks into the
+// three row components, the three lanes' sums are exchanged by shuffles, and
+// lane c keeps row component c. Nothing on a step's path reads global memory:
 //  - values of rows of the same tile come from a shared-memory copy of the
 //    tile's results (visible after the consumers' barrier of the step that
 //    wrote them);
@@ -29,7 +30,8 @@
 //    group of ten rows).
 // A producer warp streams each step's records, right-hand side and halo list
 // into a ring of shared-memory slots (cp.async.bulk, one mbarrier per slot),
-// issues the halo copies kTiHaloLag steps behind, takes the CTA's next tile
+// issues each step's halo copies kTiHaloLead steps before the consumers reach
+// it (late enough that the values are usually written), takes the CTA's next tile
 // from a counter a few steps before the current one ends (so tiles go to CTAs
 // in the order CTAs become free) and then prefetches that tile's records into
 // L2.
@@ -55,8 +57,8 @@
 //             the step's halo list, bits 8-9 / bit 10 the offset (in 4 / 8
 //             bytes) of the row's FP32 / FP64 values inside their copy
 //   [vo, ..)  the lanes' values in 16-byte chunks, chunk k of lane l at
-//             vo + (30 k + l) 16: lane 3q + a holds (forward) row a of D^-1,
-//             then L_b[a][0..2] for b < M
+//             vo + (30 k + l) 16: lane 3q + c holds (forward) row c of D^-1,
+//             then column c of each block, L_b[0..2][c] for b < M
 // A step's groups are consecutive in the stream, so one copy moves a step.
 #include <algorithm>
 #include <functional>
@@ -90,7 +92,10 @@ constexpr unsigned kTiZero = kTiRows;           // local index of the all-zero r
 constexpr unsigned kTiEnd = 0xFFFFFFFFu;
 constexpr unsigned kTiMaxSlots = 12;
 constexpr unsigned kTiHalo = 128;               // halo rows copied per step (32 B each; index in 8 bits)
-constexpr unsigned kTiHaloLag = 4;              // steps between a step's records copy and its halo copies
+#ifndef DFM2G_TILE_HALO_LEAD
+#define DFM2G_TILE_HALO_LEAD 3  // steps between a step's halo copies and its use
+#endif
+constexpr unsigned kTiHaloLead = DFM2G_TILE_HALO_LEAD;
 constexpr unsigned kTiGrabLead = 4;             // steps before a tile's end at which the next tile is taken
 constexpr size_t kTiSmemCap = 227u * 1024u;
 static_assert(kTiWarps >= 1 && kTiWarps <= 15, "named barrier of the consumer warps");
@@ -173,11 +178,11 @@ __global__ void k_tile_fill(unsigned n, size_t ngroups, const unsigned *__restri
     const unsigned s0 = FWD ? rs[i] : dia[i], s1 = FWD ? dia[i] : rs[i + 1];
     T v;
     if (FWD && j < 3u) {
-      v = vdia[(size_t)i * 9 + a * 3 + j];
+      v = vdia[(size_t)i * 9 + a * 3 + j];  // row a of D^-1
     } else {
       const unsigned jb = FWD ? j - 3u : j;
-      const unsigned b = jb / 3u, c = jb - 3u * b;
-      v = (s0 + b < s1) ? vcrs[(size_t)(s0 + b) * 9 + a * 3 + c] : T(0);
+      const unsigned b = jb / 3u, r2 = jb - 3u * b;
+      v = (s0 + b < s1) ? vcrs[(size_t)(s0 + b) * 9 + r2 * 3 + a] : T(0);  // column a of block b
     }
     const unsigned rec = rec_of[i];
     const size_t g = rec / kTiG;
@@ -242,8 +247,9 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 
   if (warp == kTiWarps) {
     // ---- producer warp: walks the CTA's tiles and copies their steps (lane
-    // 0 issues the bulk copies), then each step's halo values kTiHaloLag steps
-    // later (all lanes). Step descriptors come in batches of 32, one per lane.
+    // 0 issues the bulk copies), and each step's halo values kTiHaloLead steps
+    // before the consumers reach it (all lanes). Step descriptors come in
+    // batches of 32, one per lane.
     auto shfl4 = [&](const uint4 &v, unsigned src) {
       return make_uint4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
                         __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
@@ -278,6 +284,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       cpa_arrive_noinc(&hbar[su]);
     };
     unsigned cur = blockIdx.x, cs = 0, base = 0, issued = 0, halo_next = 0;
+    const unsigned halo_lag = nslots - kTiHaloLead;
     uint4 td = tiles[2 * cur], sa, sb;
     load_batch(td, 0, sa, sb);
     unsigned tok = 0;
@@ -353,7 +360,9 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       }
       ++cs;
       ++issued;
-      while (halo_next + kTiHaloLag < issued) halo_copy(halo_next++);
+      // step u's halo is copied when the producer issues step u + nslots -
+      // kTiHaloLead, i.e. once the consumers are kTiHaloLead steps before u
+      while (halo_next + halo_lag < issued) halo_copy(halo_next++);
     }
     // the halo copies of the steps issued last (the END slot needs none)
     const unsigned last = issued > 0 ? issued - 1u : 0u;
@@ -437,7 +446,10 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         }
       }
       const unsigned char *hd = sp + sg.hd_off;
-      T xv[MR][3];
+      // component c (= a) of every dependency's x, with no branch: a row of
+      // the tile (xs), a halo copy (hd) or, for rows read in global memory,
+      // the pending marker (polled below)
+      T xv[MR];
 #pragma unroll
       for (unsigned b = 0; b < MR; ++b) {
         const unsigned c = cd[b];
@@ -446,11 +458,8 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         const T *xp = loc ? xs + (size_t)(c & ~kTiLocal) * 3
                           : (glob ? xs + (size_t)kTiZero * 3
                                   : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off));
-        const T x0 = xp[0], x1 = xp[1], x2 = xp[2];
-        const T pv = pending_value<T>();
-        xv[b][0] = glob ? pv : x0;
-        xv[b][1] = glob ? pv : x1;
-        xv[b][2] = glob ? pv : x2;
+        const T x = xp[a];
+        xv[b] = glob ? pending_value<T>() : x;
       }
       T acc = reinterpret_cast<const T *>(sp + sg.in_off)[warp * 32u + lane];
       if (row != ~0u) {
@@ -458,8 +467,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         // global memory): polled in global memory
         bool pend = false;
 #pragma unroll
-        for (unsigned b = 0; b < MR; ++b)
-          pend |= is_pending(xv[b][0]) | is_pending(xv[b][1]) | is_pending(xv[b][2]);
+        for (unsigned b = 0; b < MR; ++b) pend |= is_pending(xv[b]);
         if (pend) {
           const unsigned *hl = reinterpret_cast<const unsigned *>(sp + sg.hl_off);
           const unsigned long long t0 = globaltimer_ns();
@@ -469,45 +477,46 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 #pragma unroll
             for (unsigned b = 0; b < MR; ++b) {
               const unsigned c = cd[b];
-              if (c & kTiLocal) continue;
+              if ((c & kTiLocal) || !is_pending(xv[b])) continue;
               const unsigned r = (c & kTiGlobal) ? (c & ~kTiGlobal) : hl[c & 0xFFu];
-              const T *xp = out + (size_t)r * 3;
-#pragma unroll
-              for (unsigned k = 0; k < 3; ++k)
-                if (is_pending(xv[b][k])) {
-                  xv[b][k] = ld_relaxed(xp + k);
-                  pend |= is_pending(xv[b][k]);
-                }
+              xv[b] = ld_relaxed(out + (size_t)r * 3 + a);
+              pend |= is_pending(xv[b]);
             }
             if (!pend) break;
             if ((++spins & 15u) == 0 && (ld_relaxed(err) != 0 || globaltimer_ns() - t0 > timeout_ns)) {
               atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
 #pragma unroll
               for (unsigned b = 0; b < MR; ++b)
-#pragma unroll
-                for (unsigned k = 0; k < 3; ++k)
-                  if (is_pending(xv[b][k])) xv[b][k] = T(0);
+                if (is_pending(xv[b])) xv[b] = T(0);
               break;
             }
           }
         }
       }
-      // three partial sums (shorter dependent chains), then the lane's total
+      // column a of each block against x_b[a], into the three row sums
       constexpr unsigned off = FWD ? 3u : 0u;
       T p0 = T(0), p1 = T(0), p2 = T(0);
 #pragma unroll
       for (unsigned b = 0; b < MR; ++b) {
         if (b < M) {
-          p0 += v[off + 3 * b + 0] * xv[b][0];
-          p1 += v[off + 3 * b + 1] * xv[b][1];
-          p2 += v[off + 3 * b + 2] * xv[b][2];
+          p0 += v[off + 3 * b + 0] * xv[b];
+          p1 += v[off + 3 * b + 1] * xv[b];
+          p2 += v[off + 3 * b + 2] * xv[b];
         }
       }
-      acc -= (p0 + p1) + p2;
+      // row a's sum over the three lanes of the row: in round r each lane
+      // sends its sum for row (a + r) % 3 and receives row a's from lane (a - r) % 3
+      const unsigned base = 3u * q;
+      const unsigned a1 = a == 2u ? 0u : a + 1u, a2 = a == 0u ? 2u : a - 1u;  // a + 1, a - 1 (mod 3)
+      const T own = a == 0u ? p0 : (a == 1u ? p1 : p2);
+      const T s1 = a1 == 0u ? p0 : (a1 == 1u ? p1 : p2);  // row a + 1, sent in round 1
+      const T s2 = a2 == 0u ? p0 : (a2 == 1u ? p1 : p2);  // row a + 2 = a - 1, sent in round 2
+      const T r1 = __shfl_sync(0xffffffffu, s1, base + a2);  // from lane a - 1: its row (a - 1) + 1 = a
+      const T r2 = __shfl_sync(0xffffffffu, s2, base + a1);  // from lane a + 1: its row (a + 1) - 1 = a
+      acc -= (own + r1) + r2;
       T z;
       if constexpr (FWD) {
         // z_a = sum_c Dinv[a][c] u_c, u_c on lane 3q + c (every lane takes part)
-        const unsigned base = 3u * q;
         const T u0 = __shfl_sync(0xffffffffu, acc, base);
         const T u1 = __shfl_sync(0xffffffffu, acc, base + 1u);
         const T u2 = __shfl_sync(0xffffffffu, acc, base + 2u);
@@ -833,10 +842,9 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   const unsigned S = (unsigned)sizeof(T);
   const TileGeom g = tile_geom(ts.M, S, forward);
   const SlotGeom sg = slot_geom(ts.max_groups, g.gbytes, S);
-  // ring slots: as many as fit (at most kTiMaxSlots); the halo copies of a
-  // step run kTiHaloLag steps behind its records, so at least kTiHaloLag + 2
+  // ring slots: as many as fit (at most kTiMaxSlots, at least kTiHaloLead + 3)
   unsigned nslots = kTiMaxSlots;
-  while (nslots > kTiHaloLag + 2 && tile_smem(S, nslots, sg.bytes) > kTiSmemCap) --nslots;
+  while (nslots > kTiHaloLead + 3 && tile_smem(S, nslots, sg.bytes) > kTiSmemCap) --nslots;
   const size_t smem = tile_smem(S, nslots, sg.bytes);
   if (smem > kTiSmemCap) return DFM2G_OK;
   DevBuf<unsigned char> &bytes = tile_bytes(ts, T(0));
