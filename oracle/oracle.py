@@ -465,6 +465,63 @@ class Oracle:
         assert st == 0
         return vc[: col.size * 9], vd, b
 
+    # ---- deformers (reference only: oracle/ref_driver_deform.cpp) ---------------
+    def arap_elements(self, xyz0, tri, xyz1, quat1):
+        """Deformer_Arap's per-point elements: (ptr[np+1], idx, eM (9 n^2 each), eR (3 per entry))."""
+        np_ = xyz0.size // 3
+        tri = np.ascontiguousarray(tri, np.uint32)
+        fs = self._f("arap_sizes")
+        fs.argtypes = [C.c_uint32, C.c_uint32, _u32p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        ni, nm = C.c_uint64(), C.c_uint64()
+        fs(np_, tri.size // 3, tri, C.byref(ni), C.byref(nm))
+        ptr = np.zeros(np_ + 1, np.uint32)
+        idx = np.zeros(ni.value, np.uint32)
+        eM = np.zeros(nm.value, np.float64)
+        eR = np.zeros(ni.value * 3, np.float64)
+        f = self._f("arap_elements")
+        f.argtypes = [C.c_uint32, _f64p, C.c_uint32, _u32p, _f64p, _f64p, _u32p, _u32p, _f64p, _f64p]
+        f(np_, np.ascontiguousarray(xyz0, np.float64), tri.size // 3, tri, np.ascontiguousarray(xyz1, np.float64),
+          np.ascontiguousarray(quat1, np.float64), ptr, idx, eM, eR)
+        return ptr, idx, eM, eR
+
+    def arap_deform(self, xyz0, tri, xyz1, quat1, bc):
+        """One Deformer_Arap::Deform with ILU(0)-PCG: (new xyz1, history)."""
+        np_ = xyz0.size // 3
+        tri = np.ascontiguousarray(tri, np.uint32)
+        x1 = np.array(xyz1, np.float64)
+        q1 = np.array(quat1, np.float64)
+        hist = np.zeros(1000, np.float64)
+        f = self._f("arap_deform")
+        f.argtypes = [C.c_uint32, _f64p, C.c_uint32, _u32p, _f64p, _f64p, _i32p, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        nh = f(np_, np.ascontiguousarray(xyz0, np.float64), tri.size // 3, tri, x1, q1,
+               np.ascontiguousarray(bc, np.int32), hist, hist.size)
+        return x1, hist[:nh]
+
+    def lap_deform(self, xyz0, tri, bc, xyz_def):
+        """CDef_LaplacianLinear (ILU(20)): its matrix pattern, dual-Laplacian elements, ILU(20) pattern, and one
+        Deform from xyz_def: dict(pat_start, pat_col, ptr, idx, eM, ilu_start, ilu_col, xyz_def, hist)."""
+        np_ = xyz0.size // 3
+        tri = np.ascontiguousarray(tri, np.uint32)
+        fs = self._f("lap_sizes")
+        fs.argtypes = [C.c_uint32, C.c_uint32, _u32p] + [C.POINTER(C.c_uint64)] * 4
+        npat, ni, nm, nilu = (C.c_uint64() for _ in range(4))
+        fs(np_, tri.size // 3, tri, C.byref(npat), C.byref(ni), C.byref(nm), C.byref(nilu))
+        out = dict(pat_start=np.zeros(np_ + 1, np.uint32), pat_col=np.zeros(npat.value, np.uint32),
+                   ptr=np.zeros(np_ + 1, np.uint32), idx=np.zeros(ni.value, np.uint32),
+                   eM=np.zeros(nm.value, np.float64), ilu_start=np.zeros(np_ + 1, np.uint32),
+                   ilu_col=np.zeros(nilu.value, np.uint32), xyz_def=np.array(xyz_def, np.float64))
+        hist = np.zeros(1000, np.float64)
+        f = self._f("lap_deform")
+        f.argtypes = [C.c_uint32, _f64p, C.c_uint32, _u32p, _i32p, _f64p, _u32p, _u32p, _u32p, _u32p, _f64p, _u32p,
+                      _u32p, _f64p, C.c_uint32]
+        f.restype = C.c_uint32
+        nh = f(np_, np.ascontiguousarray(xyz0, np.float64), tri.size // 3, tri, np.ascontiguousarray(bc, np.int32),
+               out["xyz_def"], out["pat_start"], out["pat_col"], out["ptr"], out["idx"], out["eM"],
+               out["ilu_start"], out["ilu_col"], hist, hist.size)
+        out["hist"] = hist[:nh]
+        return out
+
 
 def hex_grid(nx: int, ny: int, nz: int, h: float, seed: int | None = None, jitter: float = 0.0):
     """A structured nx x ny x nz hex mesh of spacing h (node (ix,iy,iz) = ix*(ny+1)*(nz+1) + iy*(nz+1) + iz), each

@@ -5,7 +5,7 @@ oracle/Makefile), so it only works where the reference source tree exists.
 The outputs are small .npz files committed next to this script; the tests
 read them on machines without the reference.
 
-  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab nd dynamic]
+  python tests/golden/make_golden.py [tiny cfg1 cfg1e cfg2 cfg3 cfg4 cloth iluk bicgstab nd dynamic deform]
 """
 from __future__ import annotations
 
@@ -268,6 +268,27 @@ def make_dynamic(R):
     np.savez_compressed(os.path.join(HERE, "dynamic.npz"), **out)
 
 
+def make_deform(R):
+    """The ARAP deformer (Deformer_Arap: per-point elements, ILU(0)-PCG to 1e-7) and the linear Laplacian deformer
+    (CDef_LaplacianLinear: dual-Laplacian elements, ILU(20)-PCG to 1e-5) on the cylinder of tests/deform_systems.py,
+    each run once by the reference: the element matrices they hand to Merge, the ILU(20) pattern, the results."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from deform_systems import cylinder, handles
+    xyz0, tri = cylinder()
+    bc, xdef = handles(xyz0)
+    np_ = xyz0.size // 3
+    quat = np.tile(np.array([0.0, 0.0, 0.0, 1.0]), np_)  # identity rotations (x, y, z, w)
+    ptr, idx, eM, eR = R.arap_elements(xyz0, tri, xdef, quat)
+    x_arap, h_arap = R.arap_deform(xyz0, tri, xdef, quat, bc)
+    lap = R.lap_deform(xyz0, tri, bc, xdef)
+    out = dict(xyz0=xyz0, tri=tri, bc=bc, xdef=xdef, quat=quat, arap_ptr=ptr, arap_idx=idx, arap_eM=eM, arap_eR=eR,
+               arap_x=x_arap, arap_hist=h_arap)
+    out.update({"lap_" + k: v for k, v in lap.items()})
+    np.savez_compressed(os.path.join(HERE, "deform.npz"), **out)
+    print(f"deform: {np_} points, ARAP {len(h_arap) - 1} iterations, Laplacian {len(lap['hist']) - 1} iterations, "
+          f"ILU(20) {lap['ilu_col'].size} blocks (matrix {lap['pat_col'].size})")
+
+
 def main(which):
     build(quiet=True)
     R = reference()
@@ -294,6 +315,8 @@ def main(which):
         make_nd(R)
     if "dynamic" in which:
         make_dynamic(R)
+    if "deform" in which:
+        make_deform(R)
 
 
 if __name__ == "__main__":
