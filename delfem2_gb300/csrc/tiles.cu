@@ -382,86 +382,105 @@ __global__ void __launch_bounds__(kTiThreads, 1)
     return;
   }
 
-  // ---- consumers
+  // ---- consumers. Software-pipelined over the steps: everything a step
+  // reads that does not depend on the step before it (its slot's barriers and
+  // descriptor, the lane's row, codes, values and right-hand side, and the x
+  // values of halo rows) is loaded before the previous step's barrier; after
+  // it, only the x values of the tile's own rows, the products, the three-lane
+  // exchange and the store remain on the path from one step to the next.
   const unsigned q = lane / 3u, a = lane - 3u * q;
   const bool lane_ok = lane < 30u;
   const unsigned Mc = round4u(M);
-  for (unsigned s = 0;; ++s) {
-    const unsigned slot = s % nslots;
-    const unsigned par = (s / nslots) & 1u;
-    bool ok = mbar_wait_bounded(&full[slot], par, timeout_ns);
-    const uint4 meta = smeta[2 * slot];  // {rows, local base, groups, tile}
-    const bool end = ok && meta.w == kTiEnd;
-    if (ok && !end) ok = mbar_wait_bounded(&hbar[slot], par, timeout_ns);
-    if (!ok) {
+  constexpr unsigned NVR = 3u * MR + 3u;
+  constexpr unsigned PER = 16u / sizeof(T);
+  const unsigned nv = FWD ? 3u * M + 3u : 3u * M;
+  // the next step's data, loaded ahead
+  struct Pre {
+    bool ok, end, work;
+    unsigned slot, row, local;
+    unsigned cd[MR];
+    T v[NVR];
+    T xh[MR];  // halo x values (component a); the tile's own rows are read later
+    T in;
+  } P;
+  auto preload = [&](unsigned u) {
+    P.slot = u % nslots;
+    const unsigned par = (u / nslots) & 1u;
+    P.ok = mbar_wait_bounded(&full[P.slot], par, timeout_ns);
+    const uint4 meta = smeta[2 * P.slot];  // {rows, local base, groups, tile}
+    P.end = P.ok && meta.w == kTiEnd;
+    if (P.ok && !P.end) P.ok = mbar_wait_bounded(&hbar[P.slot], par, timeout_ns);
+    if (!P.ok) {
       atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
-      sflag[s & 1u] = 1;
+      sflag[u & 1u] = 1;
     }
-    if (ok && !end && warp < meta.z) {
-      unsigned char *sp = ring + (size_t)slot * sg.bytes;
-      const unsigned char *gp = sp + (size_t)warp * gbytes;
-      const unsigned row = lane_ok ? reinterpret_cast<const unsigned *>(gp)[q] : ~0u;
-      const unsigned local = meta.y + warp * kTiG + q;
-      // the lane's values first (independent of the codes)
-      constexpr unsigned NVR = 3u * MR + 3u;
-      constexpr unsigned PER = 16u / sizeof(T);
-      const unsigned nv = FWD ? 3u * M + 3u : 3u * M;
-      T v[NVR];
-      const unsigned char *vp = gp + vo + (lane_ok ? lane : 0u) * 16u;
+    P.work = P.ok && !P.end && warp < meta.z;
+    P.row = ~0u;
+    if (!P.work) return;
+    unsigned char *sp = ring + (size_t)P.slot * sg.bytes;
+    const unsigned char *gp = sp + (size_t)warp * gbytes;
+    P.row = lane_ok ? reinterpret_cast<const unsigned *>(gp)[q] : ~0u;
+    P.local = meta.y + warp * kTiG + q;
+    const unsigned char *vp = gp + vo + (lane_ok ? lane : 0u) * 16u;
 #pragma unroll
-      for (unsigned k = 0; k < (NVR + PER - 1) / PER; ++k) {
-        if (k * PER < nv) {
-          if constexpr (sizeof(T) == 4) {
-            const float4 c = *reinterpret_cast<const float4 *>(vp + k * 480u);
-            if (k * 4 + 0 < NVR) v[k * 4 + 0] = c.x;
-            if (k * 4 + 1 < NVR) v[k * 4 + 1] = c.y;
-            if (k * 4 + 2 < NVR) v[k * 4 + 2] = c.z;
-            if (k * 4 + 3 < NVR) v[k * 4 + 3] = c.w;
-          } else {
-            const double2 c = *reinterpret_cast<const double2 *>(vp + k * 480u);
-            if (k * 2 + 0 < NVR) v[k * 2 + 0] = c.x;
-            if (k * 2 + 1 < NVR) v[k * 2 + 1] = c.y;
-          }
+    for (unsigned k = 0; k < (NVR + PER - 1) / PER; ++k) {
+      if (k * PER < nv) {
+        if constexpr (sizeof(T) == 4) {
+          const float4 c = *reinterpret_cast<const float4 *>(vp + k * 480u);
+          if (k * 4 + 0 < NVR) P.v[k * 4 + 0] = c.x;
+          if (k * 4 + 1 < NVR) P.v[k * 4 + 1] = c.y;
+          if (k * 4 + 2 < NVR) P.v[k * 4 + 2] = c.z;
+          if (k * 4 + 3 < NVR) P.v[k * 4 + 3] = c.w;
         } else {
-#pragma unroll
-          for (unsigned e = 0; e < PER; ++e)
-            if (k * PER + e < NVR) v[k * PER + e] = T(0);
+          const double2 c = *reinterpret_cast<const double2 *>(vp + k * 480u);
+          if (k * 2 + 0 < NVR) P.v[k * 2 + 0] = c.x;
+          if (k * 2 + 1 < NVR) P.v[k * 2 + 1] = c.y;
         }
-      }
-      // dependency codes (Mc per row, 16-byte loads), then every x value with
-      // no branch: a row of the tile (xs), a halo copy (hd) or, for rows read
-      // in global memory, the pending marker (polled below)
-      unsigned cd[MR];
-      {
-        const uint4 *cw = reinterpret_cast<const uint4 *>(gp + kTiHead + (lane_ok ? q : 0u) * Mc * 4u);
+      } else {
 #pragma unroll
-        for (unsigned k = 0; k < MR / 4; ++k) {
-          const uint4 c = (4u * k < Mc) ? cw[k]
-                                        : make_uint4(kTiLocal | kTiZero, kTiLocal | kTiZero, kTiLocal | kTiZero,
-                                                     kTiLocal | kTiZero);
-          cd[4 * k + 0] = c.x;
-          cd[4 * k + 1] = c.y;
-          cd[4 * k + 2] = c.z;
-          cd[4 * k + 3] = c.w;
-        }
+        for (unsigned e = 0; e < PER; ++e)
+          if (k * PER + e < NVR) P.v[k * PER + e] = T(0);
       }
-      const unsigned char *hd = sp + sg.hd_off;
-      // component c (= a) of every dependency's x, with no branch: a row of
-      // the tile (xs), a halo copy (hd) or, for rows read in global memory,
-      // the pending marker (polled below)
+    }
+    const uint4 *cw = reinterpret_cast<const uint4 *>(gp + kTiHead + (lane_ok ? q : 0u) * Mc * 4u);
+#pragma unroll
+    for (unsigned k = 0; k < MR / 4; ++k) {
+      const uint4 c = (4u * k < Mc) ? cw[k]
+                                    : make_uint4(kTiLocal | kTiZero, kTiLocal | kTiZero, kTiLocal | kTiZero,
+                                                 kTiLocal | kTiZero);
+      P.cd[4 * k + 0] = c.x;
+      P.cd[4 * k + 1] = c.y;
+      P.cd[4 * k + 2] = c.z;
+      P.cd[4 * k + 3] = c.w;
+    }
+    // halo copies of this step (the pending marker for rows read in global memory)
+    const unsigned char *hd = sp + sg.hd_off;
+#pragma unroll
+    for (unsigned b = 0; b < MR; ++b) {
+      const unsigned c = P.cd[b];
+      const bool loc = (c & kTiLocal) != 0u, glob = !loc && (c & kTiGlobal) != 0u;
+      const unsigned off = sizeof(T) == 4 ? ((c >> 8) & 3u) * 4u : ((c >> 10) & 1u) * 8u;
+      const T *xp = (loc || glob) ? xs + (size_t)kTiZero * 3 : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off);
+      const T x = xp[a];
+      P.xh[b] = glob ? pending_value<T>() : x;
+    }
+    P.in = reinterpret_cast<const T *>(sp + sg.in_off)[warp * 32u + lane];
+  };
+
+  preload(0);
+  for (unsigned s = 0;; ++s) {
+    const bool end = P.end;
+    const unsigned slot = P.slot;
+    if (P.work) {
+      // the tile's own rows: written by earlier steps, visible after their barriers
       T xv[MR];
 #pragma unroll
       for (unsigned b = 0; b < MR; ++b) {
-        const unsigned c = cd[b];
-        const bool loc = (c & kTiLocal) != 0u, glob = !loc && (c & kTiGlobal) != 0u;
-        const unsigned off = sizeof(T) == 4 ? ((c >> 8) & 3u) * 4u : ((c >> 10) & 1u) * 8u;
-        const T *xp = loc ? xs + (size_t)(c & ~kTiLocal) * 3
-                          : (glob ? xs + (size_t)kTiZero * 3
-                                  : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off));
-        const T x = xp[a];
-        xv[b] = glob ? pending_value<T>() : x;
+        const unsigned c = P.cd[b];
+        const T x = xs[(size_t)(c & ~kTiLocal) * 3 + a];
+        xv[b] = (c & kTiLocal) ? x : P.xh[b];
       }
-      T acc = reinterpret_cast<const T *>(sp + sg.in_off)[warp * 32u + lane];
+      const unsigned row = P.row;
       if (row != ~0u) {
         // values still pending (a halo copy taken too early, or a row read in
         // global memory): polled in global memory
@@ -469,14 +488,14 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 #pragma unroll
         for (unsigned b = 0; b < MR; ++b) pend |= is_pending(xv[b]);
         if (pend) {
-          const unsigned *hl = reinterpret_cast<const unsigned *>(sp + sg.hl_off);
+          const unsigned *hl = reinterpret_cast<const unsigned *>(ring + (size_t)slot * sg.bytes + sg.hl_off);
           const unsigned long long t0 = globaltimer_ns();
           unsigned spins = 0;
           for (;;) {
             pend = false;
 #pragma unroll
             for (unsigned b = 0; b < MR; ++b) {
-              const unsigned c = cd[b];
+              const unsigned c = P.cd[b];
               if ((c & kTiLocal) || !is_pending(xv[b])) continue;
               const unsigned r = (c & kTiGlobal) ? (c & ~kTiGlobal) : hl[c & 0xFFu];
               xv[b] = ld_relaxed(out + (size_t)r * 3 + a);
@@ -499,9 +518,9 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 #pragma unroll
       for (unsigned b = 0; b < MR; ++b) {
         if (b < M) {
-          p0 += v[off + 3 * b + 0] * xv[b];
-          p1 += v[off + 3 * b + 1] * xv[b];
-          p2 += v[off + 3 * b + 2] * xv[b];
+          p0 += P.v[off + 3 * b + 0] * xv[b];
+          p1 += P.v[off + 3 * b + 1] * xv[b];
+          p2 += P.v[off + 3 * b + 2] * xv[b];
         }
       }
       // row a's sum over the three lanes of the row: in round r each lane
@@ -513,22 +532,25 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       const T s2 = a2 == 0u ? p0 : (a2 == 1u ? p1 : p2);  // row a + 2 = a - 1, sent in round 2
       const T r1 = __shfl_sync(0xffffffffu, s1, base + a2);  // from lane a - 1: its row (a - 1) + 1 = a
       const T r2 = __shfl_sync(0xffffffffu, s2, base + a1);  // from lane a + 1: its row (a + 1) - 1 = a
-      acc -= (own + r1) + r2;
+      const T acc = P.in - ((own + r1) + r2);
       T z;
       if constexpr (FWD) {
         // z_a = sum_c Dinv[a][c] u_c, u_c on lane 3q + c (every lane takes part)
         const T u0 = __shfl_sync(0xffffffffu, acc, base);
         const T u1 = __shfl_sync(0xffffffffu, acc, base + 1u);
         const T u2 = __shfl_sync(0xffffffffu, acc, base + 2u);
-        z = v[0] * u0 + v[1] * u1 + v[2] * u2;
+        z = P.v[0] * u0 + P.v[1] * u1 + P.v[2] * u2;
       } else {
         z = acc;
       }
       if (row != ~0u) {
-        xs[(size_t)local * 3 + a] = z;
+        xs[(size_t)P.local * 3 + a] = z;
         st_relaxed(out + (size_t)row * 3 + a, z);
       }
     }
+    // the next step's data before the barrier (not past the CTA's last step,
+    // where the producer stops)
+    if (!end && sflag[s & 1u] == 0) preload(s + 1);
     bar_consumers();
     if (sflag[s & 1u] != 0 || end) break;
     if (threadIdx.x == 0) mbar_arrive(&empty[slot]);

@@ -7,9 +7,11 @@ are on the result: converged below tol, true residual within 10 tol, x within
 1e-6 relative of the reference's x at tol 1e-10, iteration count within 30%
 of the reference's. Against the oracle run on the GPU's own matrix and
 factors, the history is followed entry by entry while rounding has not yet
-diverged (the first ten iterations within 1e-8), and a solve to 1e-13 matches
-a direct sparse solve of the same system within 1e-9. Semantics (early
-return, exhaustion length) are exact."""
+diverged (the first three iterations within 1e-10, the next two within 1e-6;
+this system amplifies a 1e-16 change of b about 500-fold per iteration, which
+the test shows on the oracle itself), and a solve to 1e-13 matches a direct sparse
+solve of the same system within 1e-9. Semantics (early return, exhaustion
+length) are exact."""
 import numpy as np
 import pytest
 
@@ -88,9 +90,12 @@ def test_bicgstab_on_device_tensors(gpu):
 @pytest.mark.parametrize("k", [0, 1])
 def test_bicgstab_follows_oracle_on_the_same_matrix(gpu, port, k):
     """The GPU's matrix and ILU(k) factors fed to the oracle's Solve_PBiCGStab:
-    the two relative histories agree to 1e-8 over the first ten iterations
-    (the same algorithm, step for step, before summation-order differences
-    grow), and the GPU solution to 1e-13 agrees with a direct solve to 1e-9."""
+    the two relative histories agree to 1e-10 over the first three iterations
+    and to 1e-6 over the next two (the same algorithm, step for step, while
+    summation-order differences grow). Past them the oracle alone, given b changed by 1e-16 relative,
+    moves its own fifth or a later entry by more than 1e-9: entries there
+    are rounding, not algorithm, so the rest of the check is on the answer:
+    the GPU solution to 1e-13 agrees with a direct solve to 1e-9."""
     import scipy.sparse as sp
     import scipy.sparse.linalg as spla
     import delfem2_gb300 as D
@@ -107,7 +112,13 @@ def test_bicgstab_follows_oracle_on_the_same_matrix(gpu, port, k):
     _, _, ho = port.solve_pbicgstab(ind, psup, vc, vd, rs_i, col, dia, ivc, ivd, b, 1e-30, 11)
     hg = D.Solve_PBiCGStab(b.copy(), np.zeros_like(b), 1e-30, 11, P.K, ilu)
     assert len(hg) == len(ho) == 10
-    assert np.max(np.abs(np.array(hg) - ho) / ho) < 1e-8
+    dev = np.abs(np.array(hg) - ho) / ho
+    assert np.max(dev[:3]) < 1e-10, dev
+    assert np.max(dev[3:5]) < 1e-6, dev
+    # the oracle's own sensitivity: b scaled entrywise by 1 + 1e-16 N(0, 1)
+    bp = b * (1.0 + 1e-16 * np.random.default_rng(1).standard_normal(b.size))
+    _, _, hp = port.solve_pbicgstab(ind, psup, vc, vd, rs_i, col, dia, ivc, ivd, bp, 1e-30, 11)
+    assert np.max(np.abs(hp - ho)[4:] / ho[4:]) > 1e-9
     # direct solve of the same (non-symmetric) system
     n = b.size
     nb = n // 3
