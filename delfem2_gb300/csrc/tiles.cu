@@ -1,16 +1,17 @@
 // Tile-scheduled triangular sweep (DFM2G_SWEEP_TILES), 3x3 blocks, FP32 and FP64.
 //
-// The rows of one sweep direction are partitioned into tiles: compact sets of
-// rows grown breadth-first from a seed row, a row joining the tile only once
-// every row it depends on is in an earlier tile or already in this one. Seeds
-// are taken in the sweep's (level, row) order, so the tiles are numbered in a
-// dependency order that follows the wavefront. Inside a tile the rows are
-// grouped by their local level (1 + the highest local level of the rows of the
-// same tile they depend on): the tile's steps. On a structured mesh in its
-// natural order the tiles are small boxes of the grid (8x8x8 nodes on the
-// voxel meshes, whose dependencies all point to lower neighbours), and a
-// dependency path crosses a tile boundary once per tile instead of once per
-// row or pencil of rows.
+// The rows of one sweep direction are partitioned into tiles: bundles of up
+// to 49 segments of dependency chains (strands), grown from a seed row, a row
+// joining the tile only once every row it depends on is in an earlier tile or
+// already in this one. Seeds are taken in the sweep's (level, row) order, so
+// the tiles are numbered in a dependency order that follows the wavefront.
+// Inside a tile the rows are grouped by their local level (1 + the highest
+// local level of the rows of the same tile they depend on): the tile's steps,
+// at most one row per segment each. On a structured mesh in its natural order
+// the tiles are columns of the grid (7 x 7 z lines, 33 rows deep, on the voxel
+// meshes, whose dependencies all point to lower neighbours): about 45 steps
+// of up to 49 rows per tile, and a dependency path crosses a tile boundary
+// once per tile instead of once per row or pencil of rows.
 //
 // One CTA sweeps one tile at a time, step by step: ten rows per consumer
 // warp and step, three lanes per row (lane 3q + c of row q): lane c reads
@@ -30,7 +31,7 @@
 //    group of ten rows).
 // A producer warp streams each step's records, right-hand side and halo list
 // into a ring of shared-memory slots (cp.async.bulk, one mbarrier per slot),
-// issues each step's halo copies kTiHaloLead steps before the consumers reach
+// issues each step's halo copies `lead` steps before the consumers reach
 // it (late enough that the values are usually written), takes the CTA's next tile
 // from a counter a few steps before the current one ends (so tiles go to CTAs
 // in the order CTAs become free) and then prefetches that tile's records into
@@ -74,7 +75,7 @@ namespace dfm2g {
 namespace {
 
 #ifndef DFM2G_TILE_ROWS
-#define DFM2G_TILE_ROWS 512  // rows per tile at most
+#define DFM2G_TILE_ROWS 1617  // rows per tile at most: 49 segments of 33 rows
 #endif
 #ifndef DFM2G_TILE_WARPS
 #define DFM2G_TILE_WARPS 5  // consumer warps per CTA: at most 10 per warp rows per step
@@ -83,6 +84,9 @@ constexpr unsigned kTiRows = DFM2G_TILE_ROWS;
 constexpr unsigned kTiWarps = DFM2G_TILE_WARPS;
 constexpr unsigned kTiG = 10;                   // rows per group (30 lanes)
 constexpr unsigned kTiWidth = kTiG * kTiWarps;  // rows per step at most
+// segments per tile (so rows per step) the partition takes: 49 = 7 x 7 z lines,
+// a full square of them on the voxel grids, where a 50th would stick out
+constexpr unsigned kTiSegs = kTiWidth - 1;
 constexpr unsigned kTiThreads = 32 * (kTiWarps + 1);
 constexpr unsigned kTiCons = 32 * kTiWarps;     // consumer threads
 constexpr unsigned kTiHead = 48;
@@ -93,13 +97,18 @@ constexpr unsigned kTiEnd = 0xFFFFFFFFu;
 constexpr unsigned kTiMaxSlots = 12;
 constexpr unsigned kTiHalo = 128;               // halo rows copied per step (32 B each; index in 8 bits)
 #ifndef DFM2G_TILE_HALO_LEAD
-#define DFM2G_TILE_HALO_LEAD 3  // steps between a step's halo copies and its use
+#define DFM2G_TILE_HALO_LEAD 4  // steps between a step's halo copies and its use, where the ring allows
 #endif
 constexpr unsigned kTiHaloLead = DFM2G_TILE_HALO_LEAD;
+constexpr unsigned kTiMinLead = 2;  // consumers wait for step s + 1's halo before step s's barrier
+#ifndef DFM2G_TILE_EARLY
+#define DFM2G_TILE_EARLY 0  // 1: consumers load step s + 1 before step s's products
+#endif
 constexpr unsigned kTiGrabLead = 4;             // steps before a tile's end at which the next tile is taken
 constexpr size_t kTiSmemCap = 227u * 1024u;
 static_assert(kTiWarps >= 1 && kTiWarps <= 15, "named barrier of the consumer warps");
 static_assert(kTiHalo <= 256, "halo index in 8 bits");
+static_assert(kTiHaloLead >= kTiMinLead, "halo lead");
 
 __host__ __device__ inline unsigned pad16u(unsigned x) { return (x + 15u) & ~15u; }
 __host__ __device__ inline unsigned round4u(unsigned x) { return (x + 3u) & ~3u; }
@@ -221,7 +230,8 @@ __global__ void __launch_bounds__(kTiThreads, 1)
     k_sweep_tiles(unsigned ntiles, const uint4 *__restrict__ tiles, const uint4 *__restrict__ steps,
                   const unsigned char *__restrict__ bytes, const T *__restrict__ in_g,
                   const unsigned *__restrict__ halo, unsigned M, unsigned vo, unsigned gbytes, unsigned nslots,
-                  SlotGeom sg, T *out, unsigned *ctr, int *err, unsigned long long timeout_ns, const int *skip) {
+                  unsigned lead, SlotGeom sg, T *out, unsigned *ctr, int *err, unsigned long long timeout_ns,
+                  const int *skip) {
   extern __shared__ __align__(128) unsigned char ti_smem[];
   if (skip && *skip) return;
   uint64_t *full = reinterpret_cast<uint64_t *>(ti_smem);
@@ -247,7 +257,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 
   if (warp == kTiWarps) {
     // ---- producer warp: walks the CTA's tiles and copies their steps (lane
-    // 0 issues the bulk copies), and each step's halo values kTiHaloLead steps
+    // 0 issues the bulk copies), and each step's halo values `lead` steps
     // before the consumers reach it (all lanes). Step descriptors come in
     // batches of 32, one per lane.
     auto shfl4 = [&](const uint4 &v, unsigned src) {
@@ -284,7 +294,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       cpa_arrive_noinc(&hbar[su]);
     };
     unsigned cur = blockIdx.x, cs = 0, base = 0, issued = 0, halo_next = 0;
-    const unsigned halo_lag = nslots - kTiHaloLead;
+    const unsigned halo_lag = nslots - lead;
     uint4 td = tiles[2 * cur], sa, sb;
     load_batch(td, 0, sa, sb);
     unsigned tok = 0;
@@ -361,7 +371,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       ++cs;
       ++issued;
       // step u's halo is copied when the producer issues step u + nslots -
-      // kTiHaloLead, i.e. once the consumers are kTiHaloLead steps before u
+      // lead, i.e. once the consumers are `lead` steps before u
       while (halo_next + halo_lag < issued) halo_copy(halo_next++);
     }
     // the halo copies of the steps issued last (the END slot needs none)
@@ -402,8 +412,8 @@ __global__ void __launch_bounds__(kTiThreads, 1)
     T v[NVR];
     T xh[MR];  // halo x values (component a); the tile's own rows are read later
     T in;
-  } P;
-  auto preload = [&](unsigned u) {
+  };
+  auto preload = [&](Pre &P, unsigned u) {
     P.slot = u % nslots;
     const unsigned par = (u / nslots) & 1u;
     P.ok = mbar_wait_bounded(&full[P.slot], par, timeout_ns);
@@ -453,24 +463,41 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       P.cd[4 * k + 2] = c.z;
       P.cd[4 * k + 3] = c.w;
     }
-    // halo copies of this step (the pending marker for rows read in global memory)
+    // halo copies of this step. A copy still holding the pending marker was
+    // taken before its row was written (the tile runs close behind the one it
+    // depends on): the row is read again in global memory now, a step before
+    // its use, as are rows without a copy, so the read's round trip overlaps
+    // this step's barrier instead of delaying the next step.
     const unsigned char *hd = sp + sg.hd_off;
+    const unsigned *hl = reinterpret_cast<const unsigned *>(sp + sg.hl_off);
 #pragma unroll
     for (unsigned b = 0; b < MR; ++b) {
       const unsigned c = P.cd[b];
       const bool loc = (c & kTiLocal) != 0u, glob = !loc && (c & kTiGlobal) != 0u;
       const unsigned off = sizeof(T) == 4 ? ((c >> 8) & 3u) * 4u : ((c >> 10) & 1u) * 8u;
       const T *xp = (loc || glob) ? xs + (size_t)kTiZero * 3 : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off);
-      const T x = xp[a];
-      P.xh[b] = glob ? pending_value<T>() : x;
+      T x = xp[a];
+      if (!loc && (glob || is_pending(x))) {
+        const unsigned r = glob ? (c & ~kTiGlobal) : hl[c & 0xFFu];
+        x = ld_relaxed(out + (size_t)r * 3 + a);
+      }
+      P.xh[b] = x;
     }
     P.in = reinterpret_cast<const T *>(sp + sg.in_off)[warp * 32u + lane];
   };
 
-  preload(0);
+  // The next step's loads follow this step's products (issuing them before
+  // the products, which two steps' registers allow at 8 dependency slots,
+  // measured slower: the step's shared-memory reads then queue behind them).
+  constexpr bool kEarly = DFM2G_TILE_EARLY != 0 && MR <= 8;
+  Pre P, Q;
+  preload(P, 0);
   for (unsigned s = 0;; ++s) {
     const bool end = P.end;
     const unsigned slot = P.slot;
+    // not past the CTA's last step, where the producer stops
+    const bool more = !end && sflag[s & 1u] == 0;
+    if (kEarly && more) preload(Q, s + 1);
     if (P.work) {
       // the tile's own rows: written by earlier steps, visible after their barriers
       T xv[MR];
@@ -548,12 +575,11 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         st_relaxed(out + (size_t)row * 3 + a, z);
       }
     }
-    // the next step's data before the barrier (not past the CTA's last step,
-    // where the producer stops)
-    if (!end && sflag[s & 1u] == 0) preload(s + 1);
+    if (!kEarly && more) preload(Q, s + 1);
     bar_consumers();
     if (sflag[s & 1u] != 0 || end) break;
     if (threadIdx.x == 0) mbar_arrive(&empty[slot]);
+    P = Q;
   }
 }
 
@@ -569,17 +595,31 @@ int tile_to_host(std::vector<V> &h, const V *d, size_t n) {
 }  // namespace
 
 // The tile partition of one direction (host only). `order` is the sweep's
-// (level, row) order. Each tile grows from the first unassigned row of that
-// order (its seed: every row it depends on has a lower level, so it is
-// assigned) in breadth-first layers: a row is offered at layer 1 + the lowest
-// layer of the rows of this tile it depends on, and offers are taken layer by
-// layer (in level order inside a layer); a row joins once all its dependencies
-// are assigned, as long as the tile has fewer than `max_rows` rows and the
-// row's local level fewer than `max_width` rows. On a grid whose dependencies
-// point to lower neighbours the layers are the shells of a box around the
-// seed, so a tile of 8^3 rows is an 8x8x8 box, and the tiles are numbered along
+// (level, row) order.
+//
+// Strands first: a row continues the strand of the dependency nearest to it
+// in row number when it is also that row's successor nearest to it (on a grid
+// numbered z fastest: its z neighbour, so the strands are the grid's z lines);
+// any other row starts a strand. Each strand is cut into segments of nearly equal
+// length, at most max_rows / max_width rows. The rows of a segment depend on
+// one another in a chain, so a segment has at most one row on each local
+// level of a tile.
+//
+// Then the tiles: each grows from the first unassigned row of the level order
+// (its seed: every row it depends on has a lower level, so it is assigned) by
+// offers (layer, rank in the level order), smallest first. A row's successors
+// are offered at the row's layer when they are in its segment, one layer
+// further when they are in another strand, and after every other offer within
+// reach when they start the next segment of its strand, so a tile takes the
+// seed's segment, then the segments next to it at the same depth, and so on: on the voxel grids, columns of 7 x 7 z lines 33 rows
+// deep. A row joins once every row it depends on is assigned (to an earlier
+// tile or this one), as long as the tile has fewer than max_rows rows, its
+// segment is in the tile or the tile has fewer than max_width segments, and
+// its local level has fewer than max_width rows. The tiles are numbered along
 // the wavefront. Outputs per row: its tile and local level; m = the most
 // dependencies of a row.
+constexpr unsigned kTiSegFar = 1u << 20;  // layer step to the next segment of the same strand
+
 void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const unsigned *col, const unsigned *order,
                     bool fwd, unsigned max_rows, unsigned max_width, std::vector<unsigned> &tile_of,
                     std::vector<unsigned> &lev, unsigned &ntiles, unsigned &m) {
@@ -611,11 +651,47 @@ void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const u
       for (unsigned s = s0; s < s1; ++s) succ[fill[col[s]]++] = i;
     }
   }
+  // strands: r continues the strand of d when d is the dependency of r
+  // nearest to it in row number and r the successor of d nearest to d (ties:
+  // the earlier in the level order), so a row cannot take another's strand
+  std::vector<unsigned> next(n, none), prev(n, none), near_succ(n, none);
+  auto nearer = [&](unsigned r, unsigned cand, unsigned cur) {  // cand nearer to r than cur
+    if (cur == none) return true;
+    const unsigned dc = cand > r ? cand - r : r - cand, du = cur > r ? cur - r : r - cur;
+    return dc < du || (dc == du && pos[cand] < pos[cur]);
+  };
+  for (unsigned d = 0; d < n; ++d)
+    for (unsigned k = sptr[d]; k < sptr[d + 1]; ++k)
+      if (nearer(d, succ[k], near_succ[d])) near_succ[d] = succ[k];
+  for (unsigned r = 0; r < n; ++r) {
+    unsigned s0, s1;
+    dep_range(r, s0, s1);
+    unsigned best = none;
+    for (unsigned s = s0; s < s1; ++s)
+      if (nearer(r, col[s], best)) best = col[s];
+    if (best != none && near_succ[best] == r) {
+      next[best] = r;
+      prev[r] = best;
+    }
+  }
+  // segments: strands cut into ceil(len / seg_max) pieces of nearly equal length
+  const unsigned seg_max = std::max(1u, max_rows / std::max(1u, max_width));
+  std::vector<unsigned> seg_of(n, none);
+  unsigned nseg_total = 0;
+  for (unsigned r = 0; r < n; ++r) {
+    if (prev[r] != none) continue;
+    unsigned len = 0;
+    for (unsigned u = r; u != none; u = next[u]) ++len;
+    const unsigned pieces = (len + seg_max - 1u) / seg_max;
+    unsigned k = 0;
+    for (unsigned u = r; u != none; u = next[u], ++k) seg_of[u] = nseg_total + (unsigned)((uint64_t)k * pieces / len);
+    nseg_total += pieces;
+  }
   // offers (layer, rank), smallest first; layer_of[r]: the lowest layer r was offered at in this tile
   using Offer = std::pair<unsigned, unsigned>;
   std::priority_queue<Offer, std::vector<Offer>, std::greater<Offer>> heap;
   std::vector<unsigned> layer_of(n, none), offered;  // offered: rows whose layer_of is set in this tile
-  std::vector<unsigned> width;
+  std::vector<unsigned> width, seg_tile(nseg_total, none);
   unsigned cursor = 0, t = 0;
   for (;;) {
     while (cursor < n && tile_of[order[cursor]] != none) ++cursor;
@@ -628,12 +704,14 @@ void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const u
     layer_of[seed] = 0;
     offered.push_back(seed);
     width.assign(max_rows + 1u, 0u);
-    unsigned count = 0;
+    unsigned count = 0, nseg = 0;
     while (!heap.empty() && count < max_rows) {
       const Offer o = heap.top();
       heap.pop();
       const unsigned r = order[o.second];
       if (tile_of[r] != none) continue;
+      const bool new_seg = seg_tile[seg_of[r]] != t;
+      if (new_seg && nseg >= max_width) continue;
       unsigned s0, s1;
       dep_range(r, s0, s1);
       bool ok = true;
@@ -651,12 +729,18 @@ void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const u
       lev[r] = lv;
       width[lv]++;
       ++count;
-      const unsigned next = o.first + 1u;
+      if (new_seg) {
+        seg_tile[seg_of[r]] = t;
+        ++nseg;
+      }
       for (unsigned k = sptr[r]; k < sptr[r + 1]; ++k) {
         const unsigned u = succ[k];
         if (tile_of[u] != none) continue;
+        // same segment: same layer; another strand: one layer further; the
+        // strand's next segment: after every other segment in reach
+        const unsigned lay = o.first + (seg_of[u] == seg_of[r] ? 0u : prev[u] == r ? kTiSegFar : 1u);
         if (layer_of[u] == none) offered.push_back(u);
-        layer_of[u] = std::min(layer_of[u], next);
+        layer_of[u] = std::min(layer_of[u], lay);
         heap.push(Offer(layer_of[u], pos[u]));
       }
     }
@@ -683,7 +767,7 @@ int tile_build(dfm2g_ilu_s *p, bool fwd, TileSched &ts) {
   DFM2G_TRY(tile_to_host(order, fwd ? p->order_f.p : p->order_b.p, n));
   std::vector<unsigned> tile_of, lev;
   unsigned ntiles = 0, m = 0;
-  tile_partition(n, rs.data(), dia.data(), col.data(), order.data(), fwd, kTiRows, kTiWidth, tile_of, lev, ntiles,
+  tile_partition(n, rs.data(), dia.data(), col.data(), order.data(), fwd, kTiRows, kTiSegs, tile_of, lev, ntiles,
                  m);
   if (m > 16) return DFM2G_OK;  // rows too long for the register rounds
   const unsigned M = std::max(m, 1u);
@@ -864,9 +948,12 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   const unsigned S = (unsigned)sizeof(T);
   const TileGeom g = tile_geom(ts.M, S, forward);
   const SlotGeom sg = slot_geom(ts.max_groups, g.gbytes, S);
-  // ring slots: as many as fit (at most kTiMaxSlots, at least kTiHaloLead + 3)
+  // ring slots: as many as fit (at most kTiMaxSlots, at least kTiMinLead + 2);
+  // the halo lead: kTiHaloLead where the ring has two slots more (a step's
+  // records land at least two issues before its halo copies start)
   unsigned nslots = kTiMaxSlots;
-  while (nslots > kTiHaloLead + 3 && tile_smem(S, nslots, sg.bytes) > kTiSmemCap) --nslots;
+  while (nslots > kTiMinLead + 2 && tile_smem(S, nslots, sg.bytes) > kTiSmemCap) --nslots;
+  unsigned lead = std::min(kTiHaloLead, nslots - 2u);
   const size_t smem = tile_smem(S, nslots, sg.bytes);
   if (smem > kTiSmemCap) return DFM2G_OK;
   DevBuf<unsigned char> &bytes = tile_bytes(ts, T(0));
@@ -916,10 +1003,10 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   unsigned *ctr = ts.ctr.p;
   int *err = p->err.p;
   SlotGeom sgv = sg;
-  void *args[] = {(void *)&ntiles, (void *)&tiles, (void *)&steps,  (void *)&bp,  (void *)&ing,
-                  (void *)&hl,     (void *)&M,     (void *)&vo,     (void *)&gb,  (void *)&nslots,
-                  (void *)&sgv,    (void *)&out,   (void *)&ctr,    (void *)&err, (void *)&timeout,
-                  (void *)&skip};
+  void *args[] = {(void *)&ntiles, (void *)&tiles, (void *)&steps, (void *)&bp,   (void *)&ing,
+                  (void *)&hl,     (void *)&M,     (void *)&vo,    (void *)&gb,   (void *)&nslots,
+                  (void *)&lead,   (void *)&sgv,   (void *)&out,   (void *)&ctr,  (void *)&err,
+                  (void *)&timeout, (void *)&skip};
   DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(kTiThreads), args, smem, stream()));
   note_launches(2);
   *usable = true;

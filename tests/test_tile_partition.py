@@ -8,9 +8,8 @@ a row's local level is 1 + the highest local level of its dependencies in
 the same tile (0 if none); tiles hold at most max_rows rows and max_width
 rows per local level; tiles are numbered in the level order of their seeds.
 On the natural ordering of a voxel mesh (nodes numbered z fastest, every
-dependency on a lower neighbour) the tiles are boxes of the node grid
-(8 x 8 x 8 nodes) where the grid allows, and grow past the box at the grid's
-edges."""
+dependency on a lower neighbour) the tiles are columns of the node grid
+(7 x 7 z lines, one segment deep) where the grid allows."""
 import ctypes as C
 
 import numpy as np
@@ -62,27 +61,34 @@ def _check(ind, col, dia, order, tile_of, level, nt, m, backward, max_rows, max_
 
 
 @pytest.mark.parametrize("backward", [False, True])
-def test_voxel_mesh_tiles_are_boxes(built_lib, port, backward):
+def test_voxel_mesh_tiles_are_columns(built_lib, port, backward):
+    """With the sweep kernel's sizes (1617 rows, 49 segments of 33 rows) the
+    strands are the grid's z lines (41 nodes: two segments, 21 + 20 rows) and
+    the tiles are full boxes of them: 7 x 7 columns where the grid holds them,
+    wider flat boxes at its edges."""
     import delfem2_gb300 as D
-    nx, ny, nz = 16, 9, 12  # nodes 17 x 10 x 13
+    nx, ny, nz = 16, 9, 40  # nodes 17 x 10 x 41
     a = D.voxel_problem_arrays(nx, ny, nz, 1.0 / nx, young=1.0)
     ind, psup = a["psup_ind"], a["psup"]
     col, dia = port.ilu_pattern0(ind, psup)
-    tile_of, level, nt, m, order = _partition(built_lib, port, ind, col, dia, backward, 512, 50)
-    _check(ind, col, dia, order, tile_of, level, nt, m, backward, 512, 50)
+    tile_of, level, nt, m, order = _partition(built_lib, port, ind, col, dia, backward, 1617, 49)
+    _check(ind, col, dia, order, tile_of, level, nt, m, backward, 1617, 49)
     assert m == 7
     # node (x, y, z) is row (x * (ny + 1) + y) * (nz + 1) + z
     x, y, z = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
     x, y, z = x.ravel(), y.ravel(), z.ravel()
-    boxes = 0
+    columns = 0
     for t in range(nt):
         r = tile_of == t
         ext = [int(v[r].max() - v[r].min() + 1) for v in (x, y, z)]
-        assert max(ext) <= 16, (t, ext)  # compact
-        if ext == [8, 8, 8]:
-            assert int(r.sum()) == 512
-            boxes += 1
-    assert boxes >= 2  # full 8^3 boxes where the grid holds them (the first tile's at least)
+        assert int(r.sum()) == ext[0] * ext[1] * ext[2], (t, ext)  # a full box
+        assert ext[2] in (20, 21) and ext[0] * ext[1] <= 49, (t, ext)  # whole segments, at most 49
+        assert int(level[r].max()) + 1 == ext[0] + ext[1] + ext[2] - 2  # a plane of the box per step
+        columns += ext[:2] == [7, 7]
+    assert columns >= 4
+    first = tile_of == 0
+    corner = (x >= nx + 1 - 7, y >= ny + 1 - 7, z >= nz + 1 - 21) if backward else (x < 7, y < 7, z < 21)
+    assert np.array_equal(first, corner[0] & corner[1] & corner[2])  # the seed's column
 
 
 @pytest.mark.parametrize("seed", [0, 1])
