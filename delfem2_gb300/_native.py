@@ -35,6 +35,7 @@ SWEEP_BLOCK = 3
 SWEEP_PARTS = 4
 SWEEP_CHAINS = 5
 SWEEP_TILES = 6
+SWEEP_AUTO = 7
 
 
 class SolveStats(C.Structure):

@@ -298,6 +298,7 @@ struct ChainSched {
 struct TileSched {
   bool built = false, ok = false;
   unsigned ntiles = 0, nsteps = 0, M = 0, max_groups = 0, max_halo = 0;  // M: dependency slots per row
+  double rows_per_step = 0;           // rows / steps: how full the tiles' steps are
   size_t ngroups = 0;
   unsigned ver32 = ~0u, ver64 = ~0u;  // factor_version the records were written from
   int coop[2] = {0, 0};               // resident CTAs of the sweep kernel [f64]
@@ -380,7 +381,7 @@ int chain_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs
 void chain_schedules_reset(dfm2g_ilu_s *p);
 template <typename T>
 int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
-               unsigned long long timeout, bool may_alloc, bool *usable);
+               unsigned long long timeout, bool may_alloc, bool pick, bool *usable);
 void tile_schedules_reset(dfm2g_ilu_s *p);
 void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const unsigned *col, const unsigned *order,
                     bool fwd, unsigned max_rows, unsigned max_width, std::vector<unsigned> &tile_of,

@@ -800,7 +800,7 @@ static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, cons
   }
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * B, stream()));
-  if (p->sweep_mode == DFM2G_SWEEP_CHAINS) {
+  if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_AUTO) {
     const unsigned nlev_c = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev_c, may_alloc,
@@ -866,14 +866,15 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
   }
   // sync-free, tile, chain and blob schedules: `out` is filled with the pending marker
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
-  if (p->sweep_mode == DFM2G_SWEEP_TILES) {
+  if (p->sweep_mode == DFM2G_SWEEP_TILES || p->sweep_mode == DFM2G_SWEEP_AUTO) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(tile_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
-                            &usable));
-    if (usable) return DFM2G_OK;  // else (rows too long for the tiles, or not built): the chains below
+                            p->sweep_mode == DFM2G_SWEEP_AUTO, &usable));
+    if (usable) return DFM2G_OK;  // else (rows too long for the tiles, not built, or not picked): the chains below
   }
-  if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_TILES) {
+  if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_TILES ||
+      p->sweep_mode == DFM2G_SWEEP_AUTO) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
@@ -1055,10 +1056,11 @@ static int ilu_install_pattern(dfm2g_ilu p, unsigned n, unsigned ndim, size_t nn
     p->gs_f.ok = p->gs_b.ok = false;
     p->parts_ok = false;
   }
-  // The chain schedule is the default (3x3, 3.24M DOF on GB300, FP32 / FP64
-  // forward sweep: 0.62 / 1.45 ms against 0.91 / 2.19 ms sync-free; scalar
-  // Poisson on the same mesh: mixed solve 165 ms against 225 ms).
-  p->sweep_mode = DFM2G_SWEEP_CHAINS;
+  // Default: tiles or chains, picked per pattern and precision (3.24M DOF on
+  // GB300, FP32 / FP64 forward sweep: 0.47 / 0.88 ms over tiles against 0.58
+  // / 1.23 ms over chains and 0.91 / 2.19 ms sync-free; scalar Poisson on the
+  // same mesh, chains: mixed solve 165 ms against 225 ms sync-free).
+  p->sweep_mode = DFM2G_SWEEP_AUTO;
   const size_t nvec = (size_t)n * ndim + 1;
   DFM2G_TRY(p->tmp64a.resize(nvec));
   DFM2G_TRY(p->tmp64b.resize(nvec));
@@ -1269,9 +1271,10 @@ int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
       mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS &&
-      mode != DFM2G_SWEEP_TILES)
+      mode != DFM2G_SWEEP_TILES && mode != DFM2G_SWEEP_AUTO)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
-  if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_CHAINS)
+  if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_CHAINS &&
+      mode != DFM2G_SWEEP_AUTO)
     return fail(DFM2G_ERR_UNSUPPORTED, "sweep mode %d needs 3x3 blocks (the pattern has ndim %u)", mode, p->ndim);
   if (mode == DFM2G_SWEEP_PARTS && !p->parts_ok)
     return fail(DFM2G_ERR_UNSUPPORTED, "row-range partition unavailable for this pattern");

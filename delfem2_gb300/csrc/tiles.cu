@@ -104,6 +104,7 @@ constexpr unsigned kTiMinLead = 2;  // consumers wait for step s + 1's halo befo
 #ifndef DFM2G_TILE_EARLY
 #define DFM2G_TILE_EARLY 0  // 1: consumers load step s + 1 before step s's products
 #endif
+constexpr double kTiAutoRows = 20.0;            // DFM2G_SWEEP_AUTO: least rows per step for tiles
 constexpr unsigned kTiGrabLead = 4;             // steps before a tile's end at which the next tile is taken
 constexpr size_t kTiSmemCap = 227u * 1024u;
 static_assert(kTiWarps >= 1 && kTiWarps <= 15, "named barrier of the consumer warps");
@@ -504,7 +505,9 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 #pragma unroll
       for (unsigned b = 0; b < MR; ++b) {
         const unsigned c = P.cd[b];
-        const T x = xs[(size_t)(c & ~kTiLocal) * 3 + a];
+        // codes of other tiles' rows are no index into xs: the zero row is read instead
+        const unsigned li = (c & kTiLocal) ? (c & ~kTiLocal) : kTiZero;
+        const T x = xs[(size_t)li * 3 + a];
         xv[b] = (c & kTiLocal) ? x : P.xh[b];
       }
       const unsigned row = P.row;
@@ -867,6 +870,7 @@ int tile_build(dfm2g_ilu_s *p, bool fwd, TileSched &ts) {
   if ((ngroups + 1) * kTiG >= 0xFFFFFFFFull || halo.size() >= 0xFFFFFFFFull) return DFM2G_OK;
   ts.ntiles = ntiles;
   ts.nsteps = (unsigned)(steps.size() / 2);
+  ts.rows_per_step = ts.nsteps ? (double)n / ts.nsteps : 0.0;
   ts.ngroups = ngroups;
   ts.max_groups = max_groups;
   ts.max_halo = max_halo;
@@ -934,7 +938,7 @@ DevBuf<unsigned char> &tile_in(TileSched &ts, float) { return ts.in32; }
 // not exist yet.
 template <typename T>
 int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
-               unsigned long long timeout, bool may_alloc, bool *usable) {
+               unsigned long long timeout, bool may_alloc, bool pick, bool *usable) {
   TileSched &ts = forward ? p->ts_f : p->ts_b;
   *usable = false;
   if (p->ndim != 3) return DFM2G_OK;
@@ -945,6 +949,12 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   }
   if (!ts.ok) return DFM2G_OK;
   const bool f64 = sizeof(T) == 8;
+  // DFM2G_SWEEP_AUTO: tiles only where they pay (3.24M / 823K DOF voxel
+  // blocks: 33-35 rows per step; cloth sheets 9-11 and ILU(1) of a voxel
+  // block 7, where the chains are 1.1-1.6x faster; FP64 on 26 tiles of a 32^3
+  // block: the chains by 7%)
+  if (pick && (ts.rows_per_step < kTiAutoRows || (f64 && 2u * ts.ntiles < (unsigned)ctx().num_sms)))
+    return DFM2G_OK;
   const unsigned S = (unsigned)sizeof(T);
   const TileGeom g = tile_geom(ts.M, S, forward);
   const SlotGeom sg = slot_geom(ts.max_groups, g.gbytes, S);
@@ -1014,9 +1024,9 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
 }
 
 template int tile_sweep<float>(dfm2g_ilu_s *, bool, const float *, float *, const float *, const float *,
-                               const int *, unsigned long long, bool, bool *);
+                               const int *, unsigned long long, bool, bool, bool *);
 template int tile_sweep<double>(dfm2g_ilu_s *, bool, const double *, double *, const double *, const double *,
-                                const int *, unsigned long long, bool, bool *);
+                                const int *, unsigned long long, bool, bool, bool *);
 
 // Drops the tiles and records (a new pattern); rebuilt on first use.
 void tile_schedules_reset(dfm2g_ilu_s *p) {

@@ -75,13 +75,21 @@ enum dfm2g_sweep {
                                registers and polls only the others; the
                                chain's factor blocks are TMA-streamed into
                                shared memory ahead of the warp               */
-  DFM2G_SWEEP_TILES = 6     /* 3x3: rows in compact tiles (grown breadth-
-                               first in dependency order), one CTA per tile
-                               walking the tile's local levels with shared-
-                               memory hand-offs inside the tile and polls
-                               only across tiles; records TMA-streamed per
-                               level. Patterns whose rows have more than 16
-                               blocks in a triangle use the chain schedule */
+  DFM2G_SWEEP_TILES = 6,    /* 3x3: rows in tiles of up to 49
+                               segments of dependency chains (7 x 7 columns
+                               of grid lines on voxel meshes), one CTA per
+                               tile walking the tile's local levels with
+                               shared-memory hand-offs inside the tile and
+                               copies or polls only across tiles; records
+                               TMA-streamed per level. Patterns whose rows
+                               have more than 16 blocks in a triangle use
+                               the chain schedule                           */
+  DFM2G_SWEEP_AUTO = 7      /* the default: DFM2G_SWEEP_TILES where the tiles'
+                               steps hold 20 rows or more on average (and,
+                               for FP64, there are at least half as many
+                               tiles as SMs: the FP64 steps are bound by the
+                               SM's FP64 rate), DFM2G_SWEEP_CHAINS otherwise
+                               (2-D meshes, fill-in patterns, small grids)   */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>       */
@@ -209,9 +217,10 @@ DFM2G_API int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem)
  * stream and its input buffer). The other schedules (sync-free, levels,
  * groups, parts) need nothing built. */
 DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
-/* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE, DFM2G_SWEEP_LEVELS and DFM2G_SWEEP_CHAINS. */
+/* 1x1 and 2x2 patterns take DFM2G_SWEEP_SYNCFREE, DFM2G_SWEEP_LEVELS, DFM2G_SWEEP_CHAINS and
+ * DFM2G_SWEEP_AUTO (the chains). */
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
-/* Current schedule (a new pattern starts with DFM2G_SWEEP_CHAINS). */
+/* Current schedule (a new pattern starts with DFM2G_SWEEP_AUTO). */
 DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
@@ -236,9 +245,10 @@ DFM2G_API int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const
  * DFM2G_SWEEP_TILES uses, from a sorted ILU pattern (row offsets, columns,
  * dia_ind) and the sweep's level order (dfm2g_ilu_get_levels). tile_of[i] is
  * row i's tile (numbered in dependency order), level[i] its local level inside
- * the tile; tiles hold at most max_rows rows and max_width rows per local
- * level; *max_deps the most blocks of a row's triangle (forward: strictly
- * lower, backward: strictly upper). */
+ * the tile; tiles hold at most max_width strand segments of at most
+ * max_rows / max_width rows each (so at most max_width rows per local level);
+ * the sweep uses max_rows 1617, max_width 49. *max_deps the most blocks of a
+ * row's triangle (forward: strictly lower, backward: strictly upper). */
 DFM2G_API int dfm2g_tile_partition(unsigned n, const unsigned *row_start, const unsigned *col,
                                    const unsigned *dia_ind, const unsigned *order, int backward,
                                    unsigned max_rows, unsigned max_width, unsigned *tile_of,

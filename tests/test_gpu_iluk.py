@@ -47,7 +47,7 @@ def test_iluk_matches_reference_fixture(prob, k, tag):
     assert st.rel_residual < 1e-10 and rel_err(xm, G[f"k{tag}_x"]) < 1e-8
 
 
-@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6])
+@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6, 7])
 def test_iluk_sweeps_match_oracle_in_every_schedule(prob, port, mode):
     import delfem2_gb300 as D
     a, P, b = prob
@@ -67,6 +67,68 @@ def test_iluk_sweeps_match_oracle_in_every_schedule(prob, port, mode):
     g = fo.copy()
     ilu.BackwardSubstitution(g)
     assert rel_err(g, port.ilu_backward(rs, col, dia, vc, fo)) < 1e-10
+
+
+def _outside_rows_per_step(lib, port, rs, col, dia, backward):
+    """Most rows of other tiles that one step of the tile schedule depends on
+    (dfm2g_tile_partition with the sweep's sizes)."""
+    import ctypes as C
+    n = rs.size - 1
+    _, order, _ = port.ilu_levels(rs, col, dia, backward)
+    u32 = lambda x: np.ascontiguousarray(x, np.uint32)
+    rs_, col_, dia_, order = u32(rs), u32(col), u32(dia), u32(order)
+    tile_of, level = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+    nt, m = C.c_uint(0), C.c_uint(0)
+    assert lib.dfm2g_tile_partition(n, rs_.ctypes.data, col_.ctypes.data, dia_.ctypes.data, order.ctypes.data,
+                                    int(backward), 1617, 49, tile_of.ctypes.data, level.ctypes.data, C.byref(nt),
+                                    C.byref(m)) == 0
+    lo, hi = (dia_, rs_[1:]) if backward else (rs_[:-1], dia_)
+    rows = np.repeat(np.arange(n), (hi - lo).astype(np.int64))
+    deps = np.concatenate([col_[a:b] for a, b in zip(lo, hi)])
+    out = tile_of[deps] != tile_of[rows]
+    step = tile_of[rows[out]].astype(np.int64) * (1 << 20) + level[rows[out]]
+    pairs = np.unique(np.stack([step, deps[out].astype(np.int64)], 1), axis=0)
+    return int(np.unique(pairs[:, 0], return_counts=True)[1].max()), int(m.value)
+
+
+def test_iluk_tiles_with_rows_read_in_global_memory(gpu, port):
+    """ILU(1) of a 28^3 voxel block, swept by the tile schedule (13 blocks per
+    triangle row fit its records), where some backward steps depend on more
+    than 128 rows of other tiles: the first 128 are copied ahead, the rest
+    read in global memory. FP64 and FP32 sweeps match the oracle's sweeps of
+    the same factors (1e-10, 1e-4), and the mixed solver reaches 1e-10."""
+    import ctypes as C
+    import torch
+    import delfem2_gb300 as D
+    from delfem2_gb300 import _native as N
+    a = D.voxel_problem_arrays(28, 28, 28, 1.0 / 28, seed=4, e_range=(0.1, 10.0))
+    P = D.StaticElasticProblem(a)
+    b = P.assemble()
+    ilu = D.CPreconditionerILU()
+    ilu.Initialize_ILUk(P.K, 1)
+    ilu.CopyValue(P.K)
+    assert ilu.Decompose()
+    ilu.set_sweep_mode(6)  # the default would take the chains here: 7-8 rows per step
+    rs = ilu.row_start()
+    col, dia = ilu.pattern()
+    vc, vd = ilu.values()
+    most, m = _outside_rows_per_step(gpu, port, rs, col, dia, True)
+    assert m == 13 and most > 128, (m, most)
+    v = np.random.default_rng(8).standard_normal(b.size)
+    fo = port.ilu_forward(rs, col, dia, vc, vd, v)
+    zo = port.ilu_backward(rs, col, dia, vc, fo)
+    f = v.copy()
+    ilu.ForwardSubstitution(f)
+    assert rel_err(f, fo) < 1e-10
+    g = fo.copy()
+    ilu.BackwardSubstitution(g)
+    assert rel_err(g, zo) < 1e-10
+    z32 = torch.tensor(v, dtype=torch.float32, device="cuda")
+    N.call("dfm2g_ilu_solve_precond", ilu._h, N.F32, C.c_void_p(z32.data_ptr()), N.MEM_DEVICE)
+    assert rel_err(z32.double().cpu().numpy(), zo) < 1e-4
+    xm = np.zeros_like(b)
+    st = D.Solve_PCG_Mixed(b, xm, 1e-10, P.K, ilu, method="reliable")
+    assert st.rel_residual < 1e-10
 
 
 def test_iluk_on_the_cloth_pattern(gpu, port):

@@ -102,7 +102,7 @@ def test_factors_are_the_reference_bits(gpu, name, k):
 
 @pytest.mark.parametrize("name", NAMES)
 @pytest.mark.parametrize("k", [0, 1])
-@pytest.mark.parametrize("mode", [0, 1, 5])
+@pytest.mark.parametrize("mode", [0, 1, 5, 7])
 def test_sweeps(gpu, name, k, mode):
     import delfem2_gb300 as D
     G = golden("nd")

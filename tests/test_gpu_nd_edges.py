@@ -31,7 +31,7 @@ def _system(kind, n, nd, seed=3):
 
 @pytest.mark.parametrize("kind,n", [("arrow", 5000), ("chain", 2000)])
 @pytest.mark.parametrize("nd", [1, 2])
-@pytest.mark.parametrize("mode", [0, 1, 5])
+@pytest.mark.parametrize("mode", [0, 1, 5, 7])
 def test_edge_patterns(gpu, port, kind, n, nd, mode):
     import delfem2_gb300 as D
     ind, psup, vc, vd = _system(kind, n, nd)

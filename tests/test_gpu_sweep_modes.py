@@ -47,7 +47,7 @@ def _system(kind, n, seed):
 
 
 @pytest.mark.parametrize("kind,n", [("arrow", 20000), ("chain", 3000), ("random", 6000)])
-@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6])
+@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6, 7])
 def test_sweep_modes_on_edge_patterns(gpu, port, kind, n, mode):
     import delfem2_gb300 as D
     ind, psup, vc, vd = _system(kind, n, 3)
@@ -94,7 +94,8 @@ def test_chain_kernels_shared_by_patterns_with_different_records(gpu, port):
         ilu.SetPattern0(K)
         ilu.CopyValue(K)
         assert ilu.Decompose()
-        assert ilu.sweep_mode() == 5  # the default schedule
+        assert ilu.sweep_mode() == 7  # the default: tiles or chains, picked per pattern
+        ilu.set_sweep_mode(5)
         col, dia = port.ilu_pattern0(ind, psup)
         ivc, ivd = port.ilu_copy_value(ind, col, psup, vc, vd)
         assert port.ilu_decompose(ind, col, dia, ivc, ivd)[0] == 0
