@@ -221,6 +221,52 @@ __device__ __forceinline__ bool grid_sum_last(double partial, double *partials,
   return threadIdx.x == 0;
 }
 
+// Barrier of all CTAs of a cooperative launch: bar[0] counts arrivals, bar[1]
+// is the generation the last arrival advances (both start at 0 and the count
+// returns to 0, so one pair serves any number of barriers of successive
+// launches on a stream). Bounded: false, with DFM2G_ERR_WAIT_TIMEOUT in
+// *err, when the other CTAs do not all arrive within timeout_ns.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned long long timeout_ns) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned *gen = bar + 1;
+    const unsigned g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer_ns();
+      while (*gen == g) {
+        if (globaltimer_ns() - t0 > timeout_ns) {
+          atomicCAS(err, 0, DFM2G_ERR_WAIT_TIMEOUT);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// Sum of partials[0, nparts) in a fixed order, the same in every CTA that
+// calls it (all threads of the CTA receive it).
+__device__ __forceinline__ double sum_partials_all(const double *partials, unsigned nparts, double *sh) {
+  __shared__ double total_s;
+  double s = 0.0;
+  for (unsigned b = threadIdx.x; b < nparts; b += blockDim.x) s += ld_relaxed(partials + b);
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) total_s = s;
+  __syncthreads();
+  return total_s;
+}
+
 }  // namespace dfm2g
 
 // ---- handle layouts -----------------------------------------------------------------

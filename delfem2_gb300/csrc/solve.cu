@@ -226,19 +226,30 @@ __global__ void __launch_bounds__(kThreads) k_true_residual(IterState *st, unsig
   refresh_tail(st, rr, dd, partials, sh, sh2);
 }
 
-// The same product through the TMA-staged component-layout pipeline
-// (spmv_tma_rows_c<double>), for 3x3 patterns with tiles.
+// Both parts of the reliable update in one cooperative launch (k_flush_x,
+// k_true_residual) for 3x3 patterns with SpMV tiles, only when a refresh is
+// due: x64 += x32 / scale and x32 = 0 over the CTA's grid-stride share, a
+// meeting of all CTAs, then r64 = b - K64 x64 through the TMA-staged
+// component-layout product (spmv_tma_rows_c<double>).
 __global__ void __launch_bounds__(TileCfgC<double>::kThreads, 1)
-    k_true_residual_tma(IterState *st, const unsigned *__restrict__ tiles, unsigned ntiles,
-                        const unsigned *__restrict__ row_start, const unsigned *__restrict__ col,
-                        const double *__restrict__ vcrs, const double *__restrict__ vdia,
-                        const double *__restrict__ x64, const double *__restrict__ b, float *__restrict__ r32,
-                        double *partials, int *err, unsigned long long timeout_ns) {
+    k_refresh_tma(IterState *st, const unsigned *__restrict__ tiles, unsigned ntiles,
+                  const unsigned *__restrict__ row_start, const unsigned *__restrict__ col,
+                  const double *__restrict__ vcrs, const double *__restrict__ vdia, double *x64, float *x32,
+                  const double *__restrict__ b, float *__restrict__ r32, size_t n, double *partials, unsigned *bar,
+                  int *err, unsigned long long timeout_ns) {
   extern __shared__ __align__(128) unsigned char tma_smem[];
   __shared__ double sh[32];
   __shared__ double sh2[32];
   if (st->done || !st->update) return;
-  const double sc = st->scale_next, inv_old = 1.0 / st->scale;
+  const double sc = st->scale_next, old = st->scale, inv_old = 1.0 / st->scale;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    x64[i] += (double)x32[i] / old;
+    x32[i] = 0.f;
+  }
+  if (!grid_barrier(bar, err, timeout_ns)) {
+    if (threadIdx.x == 0) st->done = 4;
+    return;
+  }
   double rr = 0.0, dd = 0.0;
   spmv_tma_rows_c<double>(tiles, ntiles, row_start, col, vcrs, vdia, x64, err, timeout_ns, tma_smem,
                           [&](unsigned row, unsigned a, double v) {
@@ -261,17 +272,14 @@ __device__ __forceinline__ T pending_marker() {
     return __uint_as_float(0xffffffffu);
 }
 
-// r -= alpha Ap; x += alpha p; |r|^2 -> history and the stop test. When fill_a
-// and fill_b are given, both are set to the sweeps' pending marker element by
-// element after Ap is read (Ap may alias fill_a). Four elements per thread and
-// pass, all loads issued before the arithmetic.
+// r -= alpha Ap; x += alpha p over the CTA's grid-stride share of the
+// vectors; returns the share of |r|^2. When fill_a and fill_b are given, both
+// are set to the sweeps' pending marker element by element after Ap is read
+// (Ap may alias fill_a). Four elements per thread and pass, all loads issued
+// before the arithmetic.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T *__restrict__ r, T *__restrict__ x,
-                                                     const T *p, const T *Ap, double *partials, double *hist,
-                                                     T *fill_a, T *fill_b) {
-  __shared__ double sh[32];
-  if (st->done) return;
-  const double alpha = st->alpha;
+__device__ __forceinline__ double update_pass(size_t n, T *__restrict__ r, T *__restrict__ x, const T *p,
+                                              const T *Ap, double alpha, T *fill_a, T *fill_b) {
   const size_t S = (size_t)gridDim.x * blockDim.x;
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   double rr = 0.0;
@@ -324,43 +332,92 @@ __global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T 
     const double rn = one(r[i], x[i], p[i], Ap[i], i);
     rr += rn * rn;
   }
-  double total;
-  if (grid_sum_last(rr, partials, &st->ticket[1], sh, &total)) {
-    st->rr = total;
-    const unsigned it = st->it + 1;
-    st->it = it;
-    if (st->mode == 2) {  // reliable updates: the FP64 refresh decides convergence
-      const double rn_scaled = sqrt(total);
-      const double rn = rn_scaled / st->scale;
-      if (st->nhist < st->hist_cap) hist[st->nhist] = rn;
-      st->nhist++;
-      if (!isfinite(total)) {
-        st->done = 4;
-      } else if (rn < st->delta * st->rmax || rn < st->tol * st->bnorm || it >= st->max_iter) {
-        st->update = 1;
-        st->scale_next = rn_scaled > 0.0 ? st->scale / rn_scaled : st->scale;
-      }
-      return;
-    }
-    const double ratio = sqrt(total * st->inv_rr0);
-    const double entry = st->mode == 0 ? sqrt(total) : ratio;
-    if (st->nhist < st->hist_cap) hist[st->nhist] = entry;
+  return rr;
+}
+
+// |r|^2 (total) -> history and the stop test (one thread of the grid).
+__device__ __forceinline__ void update_tail(IterState *st, double total, double *hist) {
+  st->rr = total;
+  const unsigned it = st->it + 1;
+  st->it = it;
+  if (st->mode == 2) {  // reliable updates: the FP64 refresh decides convergence
+    const double rn_scaled = sqrt(total);
+    const double rn = rn_scaled / st->scale;
+    if (st->nhist < st->hist_cap) hist[st->nhist] = rn;
     st->nhist++;
     if (!isfinite(total)) {
       st->done = 4;
-    } else if (ratio < st->tol) {
-      st->done = 1;
-    } else if (it >= st->max_iter) {
-      if (st->mode == 0) {  // Solve_PCG appends a final |r| on exhaustion
-        if (st->nhist < st->hist_cap) hist[st->nhist] = sqrt(total);
-        st->nhist++;
-      }
-      st->done = 2;
-    } else if (st->mode == 1) {  // CG: beta = |r1|^2/|r0|^2
-      st->beta = total / st->rPr;
-      st->rPr = total;
+    } else if (rn < st->delta * st->rmax || rn < st->tol * st->bnorm || it >= st->max_iter) {
+      st->update = 1;
+      st->scale_next = rn_scaled > 0.0 ? st->scale / rn_scaled : st->scale;
     }
+    return;
   }
+  const double ratio = sqrt(total * st->inv_rr0);
+  const double entry = st->mode == 0 ? sqrt(total) : ratio;
+  if (st->nhist < st->hist_cap) hist[st->nhist] = entry;
+  st->nhist++;
+  if (!isfinite(total)) {
+    st->done = 4;
+  } else if (ratio < st->tol) {
+    st->done = 1;
+  } else if (it >= st->max_iter) {
+    if (st->mode == 0) {  // Solve_PCG appends a final |r| on exhaustion
+      if (st->nhist < st->hist_cap) hist[st->nhist] = sqrt(total);
+      st->nhist++;
+    }
+    st->done = 2;
+  } else if (st->mode == 1) {  // CG: beta = |r1|^2/|r0|^2
+    st->beta = total / st->rPr;
+    st->rPr = total;
+  }
+}
+
+// r -= alpha Ap; x += alpha p; |r|^2 -> history and the stop test
+// (update_pass, update_tail).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_update(IterState *st, size_t n, T *__restrict__ r, T *__restrict__ x,
+                                                     const T *p, const T *Ap, double *partials, double *hist,
+                                                     T *fill_a, T *fill_b) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  const double rr = update_pass<T>(n, r, x, p, Ap, st->alpha, fill_a, fill_b);
+  double total;
+  if (grid_sum_last(rr, partials, &st->ticket[1], sh, &total)) update_tail(st, total, hist);
+}
+
+// The SpMV with p.Ap (component layout, k_spmv_pAp_tma_c) and the update
+// (k_update) in one cooperative launch: the CTAs meet once to add the p.Ap
+// partials (each CTA adds them in the same order, so every CTA has the same
+// alpha), then update their grid-stride share of r and x. The |r|^2 partials
+// go to partials[gridDim.x, 2 gridDim.x).
+template <typename T>
+__global__ void __launch_bounds__(TileCfgC<T>::kThreads, 1)
+    k_spmv_update_tma_c(IterState *st, const unsigned *__restrict__ tiles, unsigned ntiles,
+                        const unsigned *__restrict__ row_start, const unsigned *__restrict__ col,
+                        const T *__restrict__ vcrs, const T *__restrict__ vdia, const T *p, T *Ap, T *r, T *x,
+                        size_t n, double *partials, double *hist, T *fill_a, T *fill_b, unsigned *bar, int *err,
+                        unsigned long long timeout_ns) {
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  __shared__ double sh[32];
+  if (st->done) return;
+  double dot = 0.0;
+  spmv_tma_rows_c<T>(tiles, ntiles, row_start, col, vcrs, vdia, p, err, timeout_ns, tma_smem,
+                     [&](unsigned row, unsigned a, T v) {
+                       Ap[(size_t)row * 3 + a] = v;
+                       dot += (double)(v * p[(size_t)row * 3 + a]);
+                     });
+  dot = block_sum(dot, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = dot;
+  if (!grid_barrier(bar, err, timeout_ns)) {
+    if (threadIdx.x == 0) st->done = 4;
+    return;
+  }
+  const double alpha = st->rPr / sum_partials_all(partials, gridDim.x, sh);
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->alpha = alpha;
+  const double rr = update_pass<T>(n, r, x, p, Ap, alpha, fill_a, fill_b);
+  double total;
+  if (grid_sum_last(rr, partials + gridDim.x, &st->ticket[1], sh, &total)) update_tail(st, total, hist);
 }
 
 // rPr1 = (r, Pr); beta = rPr1/rPr. Four elements per thread and pass.
@@ -409,6 +466,70 @@ __global__ void k_p_update(const IterState *st, size_t n, T *__restrict__ p, con
   const size_t S = (size_t)gridDim.x * blockDim.x;
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   for (; i + 3 * S < n; i += 4 * S) {
+    T a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = p[i + u * S];
+      b[u] = z[i + u * S];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[i + u * S] = beta * a[u] + b[u];
+  }
+  for (; i < n; i += S) p[i] = beta * p[i] + z[i];
+}
+
+// (r, z), beta and p = z + beta p in one cooperative launch (k_dot_beta and
+// k_p_update): the CTAs meet once to add the dot's partials, each in the same
+// order, so every CTA computes the same beta. The state the dot updates
+// (rPr, ratio, restart_p) is read before the meeting and written after it.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_dot_pupdate(IterState *st, size_t n, const T *__restrict__ r,
+                                                          const T *__restrict__ z, T *__restrict__ p,
+                                                          double *partials, unsigned *bar, int *err,
+                                                          unsigned long long timeout_ns) {
+  __shared__ double sh[32];
+  if (st->done) return;
+  const double rPr = st->rPr, ratio = st->ratio;
+  const int restart = st->restart_p;
+  const size_t S = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  double s = 0.0;
+  for (; i + 3 * S < n; i += 4 * S) {
+    T a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = r[i + u * S];
+      b[u] = z[i + u * S];
+    }
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s += a[u] * b[u];
+    } else {  // a short FP32 run, accumulated in FP64
+      float acc = 0.f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc += a[u] * b[u];
+      s += (double)acc;
+    }
+  }
+  for (; i < n; i += S) s += (double)r[i] * (double)z[i];
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+  if (!grid_barrier(bar, err, timeout_ns)) {
+    if (threadIdx.x == 0) st->done = 4;
+    return;
+  }
+  const double total = sum_partials_all(partials, gridDim.x, sh);
+  // after a rescale of the FP32 vectors, the old p and (r,Pr) are in the old
+  // scale: p_new = z + rPr1/(rPr*ratio^2) * (ratio*p) = z + rPr1/(rPr*ratio) * p
+  const double beta_d = restart ? 0.0 : total / (rPr * ratio);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->beta = beta_d;
+    st->rPr = total;
+    st->ratio = 1.0;
+    st->restart_p = 0;
+  }
+  const T beta = (T)beta_d;
+  for (i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i + 3 * S < n; i += 4 * S) {
     T a[4], b[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -481,6 +602,7 @@ struct Workspace {
   DevBuf<IterState> st;
   DevBuf<double> partials, scal, hist;
   DevBuf<unsigned> tickets;
+  DevBuf<unsigned> bar;  // grid_barrier words of the cooperative solver kernels
   DevBuf<double> v64[6];
   DevBuf<float> v32[6];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -494,6 +616,8 @@ static int ws_prepare(size_t n, unsigned hist_cap, bool need32) {
   DFM2G_TRY(g_ws.partials.ensure((size_t)ctx().num_sms * 64));
   DFM2G_TRY(g_ws.scal.ensure(8));
   DFM2G_TRY(g_ws.tickets.ensure(4));
+  DFM2G_TRY(g_ws.bar.ensure(2));
+  DFM2G_CUDA(cudaMemsetAsync(g_ws.bar.p, 0, 2 * sizeof(unsigned), stream()));
   DFM2G_TRY(g_ws.hist.ensure(hist_cap + 4));
   for (auto &b : g_ws.v64) DFM2G_TRY(b.ensure(n + 1));
   if (need32)
@@ -522,6 +646,38 @@ static int dot_host(size_t n, const void *a, const void *b, int prec, double *ou
   DFM2G_TRY(dot_dev(n, a, b, prec, g_ws.scal.p + 7));
   DFM2G_CUDA(cudaMemcpyAsync(out, g_ws.scal.p + 7, sizeof(double), cudaMemcpyDeviceToHost, stream()));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  return DFM2G_OK;
+}
+
+// Cooperative launch of `kernel` with the given arguments (each must have the
+// kernel parameter's exact type).
+template <typename... A>
+static int coop_launch(void (*kernel)(A...), unsigned grid, unsigned threads, size_t smem, A... args) {
+  void *argv[] = {(void *)&args...};
+  DFM2G_CUDA(cudaLaunchCooperativeKernel((void *)kernel, dim3(grid), dim3(threads), argv, smem, stream()));
+  return DFM2G_OK;
+}
+
+// Lets a TMA-staged kernel use TileCfgC's shared memory (once per device).
+template <typename K>
+static int allow_tma_smem(K kernel, size_t smem, int &attr_device) {
+  if (attr_device != ctx().device) {
+    DFM2G_CUDA(cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_device = ctx().device;
+  }
+  return DFM2G_OK;
+}
+
+// CTAs of k_dot_pupdate<T>: reduce_blocks(), or as many as are resident at once.
+template <typename T>
+static int dot_pupdate_blocks(unsigned *grid) {
+  static int per_sm_dev = -1, per_sm = 0;
+  if (per_sm_dev != ctx().device) {
+    DFM2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dot_pupdate<T>, kThreads, 0));
+    per_sm_dev = ctx().device;
+  }
+  if (per_sm <= 0) return fail(DFM2G_ERR_CUDA, "k_dot_pupdate cannot be resident");
+  *grid = std::min<unsigned>(reduce_blocks(), (unsigned)per_sm * (unsigned)ctx().num_sms);
   return DFM2G_OK;
 }
 
@@ -581,37 +737,57 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
   const unsigned spmv_blocks = blocks_for((size_t)nblk * 32, kThreads, (unsigned)ctx().num_sms * 8);
   const unsigned vec_blocks = reduce_blocks();
   const int chunk = 16;
+  // 3x3 patterns with SpMV tiles: two cooperative launches besides the SpMV
+  // and the sweeps per iteration (k_spmv_update_tma_c, k_dot_pupdate) and the
+  // refresh (k_refresh_tma) only does work when one is due; otherwise five
+  // (k_spmv_pAp*, k_update, k_flush_x + k_true_residual*, k_dot_beta, k_p_update).
+  const bool fused = m->ndim == 3 && m->tiles_ok;
+  using CT = TileCfgC<T>;
+  using C64 = TileCfgC<double>;
+  const unsigned nt_T = sizeof(T) == 8 ? m->ntiles64 : m->ntiles32;
+  const unsigned *tiles_T = sizeof(T) == 8 ? m->tiles64.p : m->tiles32.p;
+  unsigned dp_grid = 0;
+  if (fused) {
+    static int attr_a = -1, attr_r = -1;
+    DFM2G_TRY(allow_tma_smem(k_spmv_update_tma_c<T>, CT::kSmem, attr_a));
+    DFM2G_TRY(allow_tma_smem(k_refresh_tma, C64::kSmem, attr_r));
+    DFM2G_TRY(dot_pupdate_blocks<T>(&dp_grid));
+  }
   for (;;) {
     for (int k = 0; k < chunk; ++k) {
       T *Ap = Pr;
-      {
+      // the sweeps' outputs get their pending marker in the update (Ap is Pr: read first, element by element)
+      const bool fill = mode != 1 && p->sweep_mode != DFM2G_SWEEP_LEVELS;
+      T *fa = fill ? mid : nullptr, *fb = fill ? Pr : nullptr;
+      if (fused) {
         ProfScope ps(DFM2G_PROF_SPMV, 1);
-        DFM2G_TRY(launch_spmv_pAp<T>(m, st, vcrs, vdia, pv, Ap, g_ws.partials.p, spmv_blocks));
-      }
-      {
-        ProfScope ps(DFM2G_PROF_UPDATE, 1);
-        // the sweeps' outputs get their pending marker here (Ap is Pr: read first, element by element)
-        const bool fill = mode != 1 && p->sweep_mode != DFM2G_SWEEP_LEVELS;
-        k_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, x, pv, Ap, g_ws.partials.p, g_ws.hist.p,
-                                                           fill ? mid : nullptr, fill ? Pr : nullptr);
+        DFM2G_TRY(coop_launch(k_spmv_update_tma_c<T>, std::min(nt_T, (unsigned)ctx().num_sms), CT::kThreads,
+                              CT::kSmem, st, tiles_T, nt_T, (const unsigned *)m->row_start.p,
+                              (const unsigned *)m->col.p, vcrs, vdia, (const T *)pv, Ap, r, x, n, g_ws.partials.p,
+                              g_ws.hist.p, fa, fb, g_ws.bar.p, m->err.p, kWaitTimeoutNs));
+      } else {
+        {
+          ProfScope ps(DFM2G_PROF_SPMV, 1);
+          DFM2G_TRY(launch_spmv_pAp<T>(m, st, vcrs, vdia, pv, Ap, g_ws.partials.p, spmv_blocks));
+        }
+        {
+          ProfScope ps(DFM2G_PROF_UPDATE, 1);
+          k_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, x, pv, Ap, g_ws.partials.p, g_ws.hist.p, fa,
+                                                             fb);
+        }
       }
       if constexpr (sizeof(T) == 4) {
-        if (mode == 2) {
+        if (mode == 2 && fused) {
+          ProfScope ps(DFM2G_PROF_OUTER, 1);
+          DFM2G_TRY(coop_launch(k_refresh_tma, std::min(m->ntiles64, (unsigned)ctx().num_sms), C64::kThreads,
+                                C64::kSmem, st, (const unsigned *)m->tiles64.p, m->ntiles64,
+                                (const unsigned *)m->row_start.p, (const unsigned *)m->col.p,
+                                (const double *)m->vcrs.p, (const double *)m->vdia.p, rf.x64, (float *)x, rf.b64,
+                                (float *)r, n, g_ws.partials.p, g_ws.bar.p, m->err.p, kWaitTimeoutNs));
+        } else if (mode == 2) {
           ProfScope ps(DFM2G_PROF_OUTER, 2);
           k_flush_x<<<vec_blocks, kThreads, 0, stream()>>>(st, n, rf.x64, (float *)x);
-          if (m->ndim == 3 && m->tiles_ok) {
-            using C = TileCfgC<double>;
-            static int attr_device = -1;  // once per device
-            if (attr_device != ctx().device) {
-              DFM2G_CUDA(cudaFuncSetAttribute(k_true_residual_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)C::kSmem));
-              attr_device = ctx().device;
-            }
-            k_true_residual_tma<<<std::min(m->ntiles64, (unsigned)ctx().num_sms), C::kThreads, C::kSmem,
-                                  stream()>>>(st, m->tiles64.p, m->ntiles64, m->row_start.p, m->col.p, m->vcrs.p,
-                                              m->vdia.p, rf.x64, rf.b64, (float *)r, g_ws.partials.p, m->err.p,
-                                              kWaitTimeoutNs);
-          } else if (m->ndim == 3)
+          if (m->ndim == 3)
             k_true_residual<3><<<spmv_blocks, kThreads, 0, stream()>>>(st, nblk, m->row_start.p, m->col.p,
                                                                        m->vcrs.p, m->vdia.p, rf.x64, rf.b64,
                                                                        (float *)r, g_ws.partials.p);
@@ -634,13 +810,19 @@ static int pcg_core(dfm2g_bsr_s *m, dfm2g_ilu_s *p, T *r, T *x, T *w0, T *w1, T 
           ProfScope ps(DFM2G_PROF_BWD, 0);
           DFM2G_TRY(ilu_sweep_guarded(p, prec, false, mid, Pr, &st->done));
         }
-        {
+        if (fused) {
           ProfScope ps(DFM2G_PROF_DOT, 1);
-          k_dot_beta<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, Pr, g_ws.partials.p);
-        }
-        {
-          ProfScope ps(DFM2G_PROF_PUPDATE, 1);
-          k_p_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, pv, Pr);
+          DFM2G_TRY(coop_launch(k_dot_pupdate<T>, dp_grid, (unsigned)kThreads, (size_t)0, st, n, (const T *)r,
+                                (const T *)Pr, pv, g_ws.partials.p, g_ws.bar.p, m->err.p, kWaitTimeoutNs));
+        } else {
+          {
+            ProfScope ps(DFM2G_PROF_DOT, 1);
+            k_dot_beta<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, r, Pr, g_ws.partials.p);
+          }
+          {
+            ProfScope ps(DFM2G_PROF_PUPDATE, 1);
+            k_p_update<T><<<vec_blocks, kThreads, 0, stream()>>>(st, n, pv, Pr);
+          }
         }
       } else {
         ProfScope ps(DFM2G_PROF_PUPDATE, 1);

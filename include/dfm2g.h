@@ -448,13 +448,15 @@ DFM2G_API int dfm2g_vec_set_zero(double *x, size_t n, int mem);
 /* Kernel classes timed when profiling is on (CUDA events around every launch
  * of the solver loops; adds a little overhead, so off by default). */
 enum dfm2g_prof_kind {
-  DFM2G_PROF_SPMV = 0,     /* Ap = K p fused with p.Ap                       */
+  DFM2G_PROF_SPMV = 0,     /* Ap = K p fused with p.Ap (3x3 patterns with
+                              SpMV tiles: and the update, in one launch)       */
   DFM2G_PROF_UPDATE = 1,   /* r -= a Ap, x += a p, |r|^2, and the pending-
                               marker fill of the sweep outputs                 */
   DFM2G_PROF_FILL = 2,     /* (unused: the fill is part of the update)        */
   DFM2G_PROF_FWD = 3,      /* forward sweep                                    */
   DFM2G_PROF_BWD = 4,      /* backward sweep                                   */
-  DFM2G_PROF_DOT = 5,      /* (r, z) and beta                                  */
+  DFM2G_PROF_DOT = 5,      /* (r, z) and beta (3x3 patterns with SpMV tiles:
+                              and p = z + beta p, in one launch)              */
   DFM2G_PROF_PUPDATE = 6,  /* p = z + beta p                                   */
   DFM2G_PROF_OUTER = 7,    /* FP64 residual / refinement kernels               */
   DFM2G_PROF_NKIND = 8
