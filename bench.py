@@ -260,6 +260,7 @@ def cloth_bench(dev, nsteps: int, cpu: bool, c=None):
                        f"iterations per step, checkpoints every {c['ckpt_every']} steps",
            "steps_timed": nsteps, "steps_in_workload": c["nsteps"],
            "ms_per_step": round(fwd_ms / nsteps, 3), "pcg_iterations_per_step": st.iterations / nsteps,
+           "ms_per_step_and_pcg_iteration": round(fwd_ms / max(st.iterations, 1), 3),
            "max_rel_residual": st.rel_residual, "forward_ms": round(fwd_ms, 2), "adjoint_ms": round(adj_ms, 2),
            "adjoint_over_forward": round(adj_ms / fwd_ms, 3), "adjoint_pcg_iterations": sb.iterations,
            "gradient_finite": bool(torch.isfinite(dLdE).all())}
@@ -278,8 +279,9 @@ def cloth_bench(dev, nsteps: int, cpu: bool, c=None):
                                  c["dt"], c["tol"], c["max_iter"])
         cpu_ms = (time.perf_counter() - t) * 1e3
         out["cpu_baseline"] = {"value": round(cpu_ms, 1), "unit": "ms per step", "cores": 1, "kind": "port",
-                               "sample": f"one step of the C restatement (assembly, ILU(0), {nh - 1} PCG "
-                                         f"iterations) on the same sheet"}
+                               "sample": f"the first step (from rest) of the C restatement (assembly, ILU(0), "
+                                         f"{nh - 1} PCG iterations) on the same sheet",
+                               "ms_per_step_and_pcg_iteration": round(cpu_ms / max(nh - 1, 1), 3)}
     return out
 
 
