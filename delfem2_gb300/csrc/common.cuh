@@ -354,7 +354,6 @@ struct TileSched {
   dfm2g::DevBuf<unsigned> rec_of;     // 10 * group + position of each row
   dfm2g::DevBuf<unsigned> gmeta;      // per group: 10 row ids, then codes [10][Mc]
   dfm2g::DevBuf<unsigned char> bytes32, bytes64;
-  dfm2g::DevBuf<unsigned char> in32, in64;  // right-hand side in the records' row order
   dfm2g::DevBuf<unsigned> ctr;        // tile counter and done-ticket of the launch
 };
 

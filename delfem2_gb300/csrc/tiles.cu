@@ -23,16 +23,16 @@
 //    wrote them);
 //  - values of rows of other tiles (the step's halo, listed per step) are
 //    copied from global memory into the step's slot ahead of the step
-//    (cp.async through L2, completing on the slot's halo mbarrier); a value
-//    still holding the pending marker (the sync-free schedules' NaN) is
-//    polled in global memory when the step runs;
-//  - the right-hand side arrives with the step's records: a gather kernel
-//    first writes it in the records' row order (group-major, 32 values per
-//    group of ten rows).
-// A producer warp streams each step's records, right-hand side and halo list
-// into a ring of shared-memory slots (cp.async.bulk, one mbarrier per slot),
-// issues each step's halo copies `lead` steps before the consumers reach
-// it (late enough that the values are usually written), takes the CTA's next tile
+//    (cp.async through L2, completing on the slot's halo mbarrier); a copy
+//    still holding the pending marker (the sync-free schedules' NaN) is read
+//    again in global memory a step ahead, and polled there when the step runs;
+//  - the right-hand side is copied into the step's slot with the halo values
+//    (4- or 8-byte cp.async per row component, in the records' row order:
+//    group-major, 32 values per group of ten rows).
+// A producer warp streams each step's records and halo list into a ring of
+// shared-memory slots (cp.async.bulk, one mbarrier per slot), issues each
+// step's halo and right-hand-side copies `lead` steps before the consumers
+// reach it (late enough that the halo values are usually written), takes the CTA's next tile
 // from a counter a few steps before the current one ends (so tiles go to CTAs
 // in the order CTAs become free) and then prefetches that tile's records into
 // L2.
@@ -203,20 +203,6 @@ __global__ void k_tile_fill(unsigned n, size_t ngroups, const unsigned *__restri
   }
 }
 
-// The right-hand side in the records' row order: in_g[32 g + 3q + a] =
-// in[3 row(g, q) + a] (0 for lanes without a row).
-template <typename T>
-__global__ void k_tile_gather_in(size_t ngroups, const unsigned *__restrict__ gmeta, unsigned words,
-                                 const T *__restrict__ in, T *__restrict__ in_g) {
-  const size_t nth = (size_t)gridDim.x * blockDim.x;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < ngroups * 32u; e += nth) {
-    const size_t g = e >> 5;
-    const unsigned l = (unsigned)(e & 31u), q = l / 3u, a = l - 3u * q;
-    const unsigned row = l < 30u ? gmeta[g * words + q] : ~0u;
-    in_g[e] = row != ~0u ? in[(size_t)row * 3 + a] : T(0);
-  }
-}
-
 __device__ __forceinline__ void bar_consumers() {
   asm volatile("bar.sync 1, %0;" ::"r"(kTiCons) : "memory");
 }
@@ -229,7 +215,7 @@ __device__ __forceinline__ void bar_consumers() {
 template <typename T, bool FWD, unsigned MR>
 __global__ void __launch_bounds__(kTiThreads, 1)
     k_sweep_tiles(unsigned ntiles, const uint4 *__restrict__ tiles, const uint4 *__restrict__ steps,
-                  const unsigned char *__restrict__ bytes, const T *__restrict__ in_g,
+                  const unsigned char *__restrict__ bytes, const T *__restrict__ in,
                   const unsigned *__restrict__ halo, unsigned M, unsigned vo, unsigned gbytes, unsigned nslots,
                   unsigned lead, SlotGeom sg, T *out, unsigned *ctr, int *err, unsigned long long timeout_ns,
                   const int *skip) {
@@ -272,15 +258,22 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         sb = steps[2 * (t0.x + base + lane) + 1];
       }
     };
-    // halo values of step u into its slot; every lane arrives on the slot's
-    // halo barrier once its copies are complete
+    // halo values and right-hand side of step u into its slot; every lane
+    // arrives on the slot's halo barrier once its copies are complete
     auto halo_copy = [&](unsigned u) {
       const unsigned su = u % nslots;
       if (mbar_wait_bounded(&full[su], (u / nslots) & 1u, timeout_ns)) {
-        const uint4 m1 = smeta[2 * su + 1];
-        if (smeta[2 * su].w != kTiEnd) {
+        const uint4 m0 = smeta[2 * su], m1 = smeta[2 * su + 1];
+        if (m0.w != kTiEnd) {
           const unsigned hc = min(m1.y, kTiHalo);
           unsigned char *sp = ring + (size_t)su * sg.bytes;
+          // right-hand side: component a of row q of group g to lane 3q + a of the group's 32 values
+          for (unsigned k = lane; k < m0.z * 30u; k += 32u) {
+            const unsigned g = k / 30u, l = k - 30u * g, q = l / 3u, a = l - 3u * q;
+            const unsigned row = reinterpret_cast<const unsigned *>(sp + (size_t)g * gbytes)[q];
+            if (row != ~0u)
+              cpa_small<sizeof(T)>(sp + sg.in_off + (size_t)(g * 32u + l) * sizeof(T), in + (size_t)row * 3 + a);
+          }
           const unsigned *hl = reinterpret_cast<const unsigned *>(sp + sg.hl_off);
           for (unsigned k = lane; k < 2u * hc; k += 32u) {
             const unsigned h = k >> 1, hr = hl[h];
@@ -362,11 +355,10 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         smeta[2 * slot] = make_uint4(st.y, st.z, st.w, cur);
         smeta[2 * slot + 1] = sh;
         unsigned char *sp = ring + (size_t)slot * sg.bytes;
-        const unsigned nrec = st.w * gbytes, nin = st.w * 32u * (unsigned)sizeof(T);
+        const unsigned nrec = st.w * gbytes;
         const unsigned nhl = round4u(sh.y) * 4u;
-        mbar_arrive_expect_tx(&full[slot], nrec + nin + nhl);
+        mbar_arrive_expect_tx(&full[slot], nrec + nhl);
         tma_load_1d(sp, bytes + (size_t)st.x * gbytes, nrec, &full[slot]);
-        tma_load_1d(sp + sg.in_off, in_g + (size_t)st.x * 32u, nin, &full[slot]);
         if (nhl) tma_load_1d(sp + sg.hl_off, halo + sh.x, nhl, &full[slot]);
       }
       ++cs;
@@ -925,8 +917,6 @@ int tile_allow_smem(void *kernel, size_t smem) {
 
 DevBuf<unsigned char> &tile_bytes(TileSched &ts, double) { return ts.bytes64; }
 DevBuf<unsigned char> &tile_bytes(TileSched &ts, float) { return ts.bytes32; }
-DevBuf<unsigned char> &tile_in(TileSched &ts, double) { return ts.in64; }
-DevBuf<unsigned char> &tile_in(TileSched &ts, float) { return ts.in32; }
 
 }  // namespace
 
@@ -942,7 +932,7 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   TileSched &ts = forward ? p->ts_f : p->ts_b;
   *usable = false;
   if (p->ndim != 3) return DFM2G_OK;
-  if (!may_alloc && (!ts.built || !ts.ok || !tile_bytes(ts, T(0)).p || !tile_in(ts, T(0)).p)) return DFM2G_OK;
+  if (!may_alloc && (!ts.built || !ts.ok || !tile_bytes(ts, T(0)).p)) return DFM2G_OK;
   if (!ts.built) {
     ts.built = true;
     DFM2G_TRY(tile_build(p, forward, ts));
@@ -967,14 +957,12 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   const size_t smem = tile_smem(S, nslots, sg.bytes);
   if (smem > kTiSmemCap) return DFM2G_OK;
   DevBuf<unsigned char> &bytes = tile_bytes(ts, T(0));
-  DevBuf<unsigned char> &in_g = tile_in(ts, T(0));
   unsigned &ver = f64 ? ts.ver64 : ts.ver32;
   if (!bytes.p) {
     DFM2G_TRY(bytes.resize(ts.ngroups * g.gbytes + 16));
     DFM2G_CUDA(cudaMemsetAsync(bytes.p, 0, ts.ngroups * g.gbytes + 16, stream()));
     ver = ~0u;
   }
-  if (!in_g.p) DFM2G_TRY(in_g.resize(ts.ngroups * 32u * S + 16));
   if (ver != p->factor_version) {
     const unsigned blocks = ctx().num_sms * 16;
     if (forward)
@@ -999,26 +987,21 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
     if (per_sm <= 0) return DFM2G_OK;
     cap = per_sm * ctx().num_sms;
   }
-  // the right-hand side in the records' row order
-  k_tile_gather_in<T><<<ctx().num_sms * 8, 256, 0, stream()>>>(ts.ngroups, ts.gmeta.p, kTiG * (g.Mc + 1u), in,
-                                                                reinterpret_cast<T *>(in_g.p));
-  DFM2G_LAUNCH_CHECK();
   const unsigned blocks = std::min<unsigned>((unsigned)cap, ts.ntiles);
   unsigned ntiles = ts.ntiles, M = ts.M, vo = g.vo, gb = g.gbytes;
   const uint4 *tiles = ts.tiles.p;
   const uint4 *steps = ts.steps.p;
   const unsigned char *bp = bytes.p;
-  const T *ing = reinterpret_cast<const T *>(in_g.p);
   const unsigned *hl = ts.halo.p;
   unsigned *ctr = ts.ctr.p;
   int *err = p->err.p;
   SlotGeom sgv = sg;
-  void *args[] = {(void *)&ntiles, (void *)&tiles, (void *)&steps, (void *)&bp,   (void *)&ing,
+  void *args[] = {(void *)&ntiles, (void *)&tiles, (void *)&steps, (void *)&bp,   (void *)&in,
                   (void *)&hl,     (void *)&M,     (void *)&vo,    (void *)&gb,   (void *)&nslots,
                   (void *)&lead,   (void *)&sgv,   (void *)&out,   (void *)&ctr,  (void *)&err,
                   (void *)&timeout, (void *)&skip};
   DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(kTiThreads), args, smem, stream()));
-  note_launches(2);
+  note_launches(1);
   *usable = true;
   return DFM2G_OK;
 }
@@ -1043,8 +1026,6 @@ void tile_schedules_reset(dfm2g_ilu_s *p) {
     ts->halo.release();
     ts->bytes32.release();
     ts->bytes64.release();
-    ts->in32.release();
-    ts->in64.release();
     ts->ctr.release();
   }
 }

@@ -80,6 +80,14 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void *src_gmem, unsigned 
 __device__ __forceinline__ void cpa16_l2(void *dst_smem, const void *src_gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst_smem)), "l"(src_gmem) : "memory");
 }
+// 4- or 8-byte global -> shared copy through L1 (cp.async.ca); both
+// addresses aligned to the size.
+template <int BYTES>
+__device__ __forceinline__ void cpa_small(void *dst_smem, const void *src_gmem) {
+  static_assert(BYTES == 4 || BYTES == 8, "cp.async.ca copies 4, 8 or 16 bytes");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst_smem)), "l"(src_gmem), "n"(BYTES)
+               : "memory");
+}
 __device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cpa_wait() {
