@@ -34,13 +34,22 @@ __device__ __forceinline__ void round16(size_t off, size_t end, size_t &a, unsig
 // double-buffered; the tile's row offsets are staged with its values, block
 // columns and diagonal blocks. FP32: 15 consumer warps (150-row tiles), FP64:
 // 7 (70-row tiles), one CTA per SM.
+#ifndef DFM2G_SPMV_F32_CONSUMERS
+#define DFM2G_SPMV_F32_CONSUMERS 15u  // FP32 tile: consumer warps (ten rows each)
+#endif
+#ifndef DFM2G_SPMV_F32_BLOCKS
+#define DFM2G_SPMV_F32_BLOCKS 2304u  // FP32 tile: blocks at most
+#endif
+#ifndef DFM2G_SPMV_F32_STAGES
+#define DFM2G_SPMV_F32_STAGES 2u  // FP32 ring stages
+#endif
 template <typename T>
 struct TileCfgC {
-  static constexpr unsigned kConsumers = sizeof(T) == 8 ? 7u : 15u;
+  static constexpr unsigned kConsumers = sizeof(T) == 8 ? 7u : DFM2G_SPMV_F32_CONSUMERS;
   static constexpr unsigned kThreads = 32u * (kConsumers + 1u);
   static constexpr unsigned kRows = kConsumers * 10u;
-  static constexpr unsigned kBlocks = sizeof(T) == 8 ? 1152u : 2304u;
-  static constexpr unsigned kStages = 2;
+  static constexpr unsigned kBlocks = sizeof(T) == 8 ? 1152u : DFM2G_SPMV_F32_BLOCKS;
+  static constexpr unsigned kStages = sizeof(T) == 8 ? 2u : DFM2G_SPMV_F32_STAGES;
   static constexpr unsigned kValBytes = kBlocks * 9 * sizeof(T) + 32;
   static constexpr unsigned kColBytes = kBlocks * 4 + 32;
   static constexpr unsigned kDiaBytes = (kRows * 9 * sizeof(T) + 32 + 15) / 16 * 16;
