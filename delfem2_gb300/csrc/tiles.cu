@@ -86,7 +86,11 @@ constexpr unsigned kTiG = 10;                   // rows per group (30 lanes)
 constexpr unsigned kTiWidth = kTiG * kTiWarps;  // rows per step at most
 // segments per tile (so rows per step) the partition takes: 49 = 7 x 7 z lines,
 // a full square of them on the voxel grids, where a 50th would stick out
-constexpr unsigned kTiSegs = kTiWidth - 1;
+#ifndef DFM2G_TILE_SEGS
+#define DFM2G_TILE_SEGS (kTiWidth - 1)
+#endif
+constexpr unsigned kTiSegs = DFM2G_TILE_SEGS;
+static_assert(kTiSegs >= 1 && kTiSegs <= kTiWidth, "segments per tile");
 constexpr unsigned kTiThreads = 32 * (kTiWarps + 1);
 constexpr unsigned kTiCons = 32 * kTiWarps;     // consumer threads
 constexpr unsigned kTiHead = 48;
