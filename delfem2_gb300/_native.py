@@ -144,6 +144,7 @@ SIGNATURES = {
     "dfm2g_launch_count": [C.POINTER(C.c_ulonglong)],
     "dfm2g_alloc_count": [C.POINTER(C.c_ulonglong)],
     "dfm2g_debug_wait_timeout": [_u],
+    "dfm2g_debug_grid_barrier": [_u, _i],
 }
 
 PROF_KINDS = ["spmv", "update", "fill", "fwd", "bwd", "dot", "pupdate", "outer"]

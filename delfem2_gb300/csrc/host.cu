@@ -294,6 +294,17 @@ __global__ void k_wait_never(const double *never, int *status, unsigned long lon
   atomicExch(status, DFM2G_OK);
 }
 
+// Two grid_barrier rounds over the same words (cooperative launch); with
+// `absent` the last CTA returns without arriving, so the others must give up
+// after `timeout_ns` and record the timeout.
+__global__ void k_grid_barrier_probe(unsigned *bar, int *err, int *status, unsigned long long timeout_ns,
+                                     int absent) {
+  if (absent && blockIdx.x == gridDim.x - 1) return;
+  bool ok = grid_barrier(bar, err, timeout_ns);
+  if (ok) ok = grid_barrier(bar, err, timeout_ns);
+  if (threadIdx.x == 0 && !ok) atomicExch(status, DFM2G_ERR_WAIT_TIMEOUT);
+}
+
 int dfm2g_debug_wait_timeout(unsigned timeout_ms) {
   DFM2G_TRY(ensure_context());
   if (timeout_ms == 0 || timeout_ms > 5000) return fail(DFM2G_ERR_ARG, "timeout_ms must be in [1, 5000]");
@@ -310,6 +321,34 @@ int dfm2g_debug_wait_timeout(unsigned timeout_ms) {
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   if (h == DFM2G_ERR_WAIT_TIMEOUT) return fail(DFM2G_ERR_WAIT_TIMEOUT, "debug wait timed out after %u ms", timeout_ms);
   return h;
+}
+
+int dfm2g_debug_grid_barrier(unsigned timeout_ms, int one_block_absent) {
+  DFM2G_TRY(ensure_context());
+  if (timeout_ms == 0 || timeout_ms > 5000) return fail(DFM2G_ERR_ARG, "timeout_ms must be in [1, 5000]");
+  DevBuf<unsigned> bar;
+  DevBuf<int> err, st;
+  DFM2G_TRY(bar.resize(2));
+  DFM2G_TRY(err.resize(1));
+  DFM2G_TRY(st.resize(1));
+  DFM2G_CUDA(cudaMemsetAsync(bar.p, 0, 2 * sizeof(unsigned), stream()));
+  DFM2G_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), stream()));
+  DFM2G_CUDA(cudaMemsetAsync(st.p, 0, sizeof(int), stream()));
+  unsigned long long timeout_ns = 1000000ull * timeout_ms;
+  int absent = one_block_absent ? 1 : 0;
+  unsigned *pb = bar.p;
+  int *pe = err.p, *ps = st.p;
+  void *args[] = {(void *)&pb, (void *)&pe, (void *)&ps, (void *)&timeout_ns, (void *)&absent};
+  DFM2G_CUDA(cudaLaunchCooperativeKernel((void *)k_grid_barrier_probe, dim3(4), dim3(64), args, 0, stream()));
+  note_launches(1);
+  int h = -1, e = -1;
+  DFM2G_CUDA(cudaMemcpyAsync(&h, st.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaMemcpyAsync(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  if (h == DFM2G_ERR_WAIT_TIMEOUT && e == DFM2G_ERR_WAIT_TIMEOUT)
+    return fail(DFM2G_ERR_WAIT_TIMEOUT, "debug grid barrier timed out after %u ms", timeout_ms);
+  if (h != DFM2G_OK || e != DFM2G_OK) return fail(DFM2G_ERR_STATE, "debug grid barrier: status %d, error word %d", h, e);
+  return DFM2G_OK;
 }
 
 }  // extern "C"

@@ -474,6 +474,11 @@ DFM2G_API int dfm2g_alloc_count(unsigned long long *count);
 /* Launches one tiny kernel that waits on a value nothing ever writes, bounded
  * by `timeout_ms`; must return DFM2G_ERR_WAIT_TIMEOUT with the context usable. */
 DFM2G_API int dfm2g_debug_wait_timeout(unsigned timeout_ms);
+/* Two rounds of the solver kernels' bounded grid barrier over 4 cooperative
+ * CTAs: DFM2G_OK when every CTA arrives; with one_block_absent one CTA returns
+ * without arriving and the call must return DFM2G_ERR_WAIT_TIMEOUT after about
+ * `timeout_ms`, with the context usable. */
+DFM2G_API int dfm2g_debug_grid_barrier(unsigned timeout_ms, int one_block_absent);
 
 #ifdef __cplusplus
 }

@@ -283,6 +283,25 @@ def test_nonfinite_rhs_is_reported(case):
     assert ei.value.status == D._native.ERR_NONFINITE
 
 
+def test_grid_barrier_meets_and_times_out(gpu):
+    """The bounded grid barrier of the fused solver kernels: two rounds pass when
+    every CTA arrives; when one CTA never arrives the others give up, the call
+    reports the timeout and the context stays usable (a solve runs after it)."""
+    import delfem2_gb300 as D
+    from delfem2_gb300 import _native as N
+    lib = N.load()
+    assert lib.dfm2g_debug_grid_barrier(50, 0) == N.OK
+    assert lib.dfm2g_debug_grid_barrier(50, 1) == N.ERR_WAIT_TIMEOUT
+    assert "grid barrier timed out" in N.last_error()
+    a = D.voxel_problem_arrays(4, 4, 4, 0.25, young=1.0)
+    P = D.StaticElasticProblem(a)
+    b = P.assemble()
+    assert P.factor()
+    x = np.zeros_like(b)
+    hist = D.Solve_PCG(b.copy(), x, 1e-10, 1000, P.K, P.ilu)
+    assert hist[-1] < 1e-10 * hist[0]
+
+
 def test_bounded_wait_times_out_and_context_survives(gpu):
     from delfem2_gb300 import _native as N
     st = N.load().dfm2g_debug_wait_timeout(50)
