@@ -32,10 +32,10 @@
 // A producer warp streams each step's records and halo list into a ring of
 // shared-memory slots (cp.async.bulk, one mbarrier per slot), issues each
 // step's halo and right-hand-side copies `lead` steps before the consumers
-// reach it (late enough that the halo values are usually written), takes the CTA's next tile
-// from a counter a few steps before the current one ends (so tiles go to CTAs
-// in the order CTAs become free) and then prefetches that tile's records into
-// L2.
+// reach it (late enough that the halo values are usually written), takes the
+// CTA's next tile from a counter a few steps before the current one ends (so
+// tiles go to CTAs in the order CTAs become free) and then prefetches that
+// tile's records into L2.
 //
 // Progress: tiles are handed out in increasing number (the first by CTA
 // index, later ones from the counter), every CTA is resident (cooperative
@@ -78,7 +78,7 @@ namespace {
 #define DFM2G_TILE_ROWS 1617  // rows per tile at most: 49 segments of 33 rows
 #endif
 #ifndef DFM2G_TILE_WARPS
-#define DFM2G_TILE_WARPS 5  // consumer warps per CTA: at most 10 per warp rows per step
+#define DFM2G_TILE_WARPS 5  // consumer warps per CTA (ten rows each per step)
 #endif
 constexpr unsigned kTiRows = DFM2G_TILE_ROWS;
 constexpr unsigned kTiWarps = DFM2G_TILE_WARPS;
@@ -105,9 +105,6 @@ constexpr unsigned kTiHalo = 128;               // halo rows copied per step (32
 #endif
 constexpr unsigned kTiHaloLead = DFM2G_TILE_HALO_LEAD;
 constexpr unsigned kTiMinLead = 2;  // consumers wait for step s + 1's halo before step s's barrier
-#ifndef DFM2G_TILE_EARLY
-#define DFM2G_TILE_EARLY 0  // 1: consumers load step s + 1 before step s's products
-#endif
 constexpr double kTiAutoRows = 20.0;            // DFM2G_SWEEP_AUTO: least rows per step for tiles
 constexpr unsigned kTiGrabLead = 4;             // steps before a tile's end at which the next tile is taken
 constexpr size_t kTiSmemCap = 227u * 1024u;
@@ -483,10 +480,8 @@ __global__ void __launch_bounds__(kTiThreads, 1)
     P.in = reinterpret_cast<const T *>(sp + sg.in_off)[warp * 32u + lane];
   };
 
-  // The next step's loads follow this step's products (issuing them before
-  // the products, which two steps' registers allow at 8 dependency slots,
-  // measured slower: the step's shared-memory reads then queue behind them).
-  constexpr bool kEarly = DFM2G_TILE_EARLY != 0 && MR <= 8;
+  // The next step's loads follow this step's products (issued before them
+  // they measured slower: the step's shared-memory reads queue behind them).
   Pre P, Q;
   preload(P, 0);
   for (unsigned s = 0;; ++s) {
@@ -494,7 +489,6 @@ __global__ void __launch_bounds__(kTiThreads, 1)
     const unsigned slot = P.slot;
     // not past the CTA's last step, where the producer stops
     const bool more = !end && sflag[s & 1u] == 0;
-    if (kEarly && more) preload(Q, s + 1);
     if (P.work) {
       // the tile's own rows: written by earlier steps, visible after their barriers
       T xv[MR];
@@ -574,7 +568,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
         st_relaxed(out + (size_t)row * 3 + a, z);
       }
     }
-    if (!kEarly && more) preload(Q, s + 1);
+    if (more) preload(Q, s + 1);
     bar_consumers();
     if (sflag[s & 1u] != 0 || end) break;
     if (threadIdx.x == 0) mbar_arrive(&empty[slot]);
