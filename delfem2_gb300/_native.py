@@ -36,6 +36,7 @@ SWEEP_PARTS = 4
 SWEEP_CHAINS = 5
 SWEEP_TILES = 6
 SWEEP_AUTO = 7
+SWEEP_CLUSTER = 8
 
 
 class SolveStats(C.Structure):

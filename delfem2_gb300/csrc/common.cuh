@@ -428,6 +428,9 @@ template <typename T>
 int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout, bool may_alloc, bool pick, bool *usable);
 void tile_schedules_reset(dfm2g_ilu_s *p);
+template <typename T>
+int cluster_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
+                  bool *usable);
 void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const unsigned *col, const unsigned *order,
                     bool fwd, unsigned max_rows, unsigned max_width, std::vector<unsigned> &tile_of,
                     std::vector<unsigned> &lev, unsigned &ntiles, unsigned &m);

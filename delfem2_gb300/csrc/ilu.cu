@@ -852,6 +852,11 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     return DFM2G_OK;
   }
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
+  if (p->sweep_mode == DFM2G_SWEEP_CLUSTER) {
+    bool usable = false;
+    DFM2G_TRY(cluster_sweep<T>(p, forward, in, out, vcrs, vdia, skip, &usable));
+    if (usable) return DFM2G_OK;  // else (the vector exceeds shared memory): the automatic choice below
+  }
   if (p->sweep_mode == DFM2G_SWEEP_BLOCK) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
@@ -866,15 +871,15 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
   }
   // sync-free, tile, chain and blob schedules: `out` is filled with the pending marker
   if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
-  if (p->sweep_mode == DFM2G_SWEEP_TILES || p->sweep_mode == DFM2G_SWEEP_AUTO) {
+  const bool auto_pick = p->sweep_mode == DFM2G_SWEEP_AUTO || p->sweep_mode == DFM2G_SWEEP_CLUSTER;
+  if (p->sweep_mode == DFM2G_SWEEP_TILES || auto_pick) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(tile_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
-                            p->sweep_mode == DFM2G_SWEEP_AUTO, &usable));
+                            auto_pick, &usable));
     if (usable) return DFM2G_OK;  // else (rows too long for the tiles, not built, or not picked): the chains below
   }
-  if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_TILES ||
-      p->sweep_mode == DFM2G_SWEEP_AUTO) {
+  if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_TILES || auto_pick) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
@@ -1271,7 +1276,7 @@ int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
       mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS &&
-      mode != DFM2G_SWEEP_TILES && mode != DFM2G_SWEEP_AUTO)
+      mode != DFM2G_SWEEP_TILES && mode != DFM2G_SWEEP_AUTO && mode != DFM2G_SWEEP_CLUSTER)
     return fail(DFM2G_ERR_ARG, "unknown sweep mode");
   if (p->ndim != 3 && mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_CHAINS &&
       mode != DFM2G_SWEEP_AUTO)

@@ -84,6 +84,16 @@ enum dfm2g_sweep {
                                TMA-streamed per level. Patterns whose rows
                                have more than 16 blocks in a triangle use
                                the chain schedule                           */
+  DFM2G_SWEEP_CLUSTER = 8,  /* 3x3 systems whose solution vector fits in
+                               shared memory (9,400 block rows FP64, 18,900
+                               FP32): one thread-block cluster of 8 CTAs
+                               walks the levels, every CTA holding the whole
+                               vector, results broadcast through distributed
+                               shared memory, one cluster barrier per level;
+                               larger systems use the AUTO choice. Slower than
+                               the chains on the systems measured except the
+                               smallest (a cluster barrier and broadcast cost
+                               about 1.3 us per level in FP32, 2.9 in FP64)  */
   DFM2G_SWEEP_AUTO = 7      /* the default: DFM2G_SWEEP_TILES where the tiles'
                                steps hold 20 rows or more on average (and,
                                for FP64, there are at least half as many

@@ -47,7 +47,7 @@ def test_iluk_matches_reference_fixture(prob, k, tag):
     assert st.rel_residual < 1e-10 and rel_err(xm, G[f"k{tag}_x"]) < 1e-8
 
 
-@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6, 7, 8])
 def test_iluk_sweeps_match_oracle_in_every_schedule(prob, port, mode):
     import delfem2_gb300 as D
     a, P, b = prob

@@ -103,7 +103,7 @@ def test_ilu_factors_match_oracle(case):
     assert rel_err(vd, s["ivd"]) < 1e-10
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_sweeps_match_oracle(case, port, mode):
     name, s, P, b = case
     default = P.ilu.sweep_mode()
@@ -149,7 +149,7 @@ def test_matvec_matches_oracle(case, port):
     assert np.isnan(y[5]) and np.isfinite(np.delete(y, 5)).all()
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_solve_pcg_matches_oracle(case, port, mode):
     import delfem2_gb300 as D
     name, s, P, b = case

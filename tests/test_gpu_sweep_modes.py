@@ -47,7 +47,7 @@ def _system(kind, n, seed):
 
 
 @pytest.mark.parametrize("kind,n", [("arrow", 20000), ("chain", 3000), ("random", 6000)])
-@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("mode", [0, 1, 3, 4, 5, 6, 7, 8])
 def test_sweep_modes_on_edge_patterns(gpu, port, kind, n, mode):
     import delfem2_gb300 as D
     ind, psup, vc, vd = _system(kind, n, 3)

@@ -26,7 +26,7 @@ pytestmark = pytest.mark.gpu
 
 SWEEP_TOL_F64 = 1e-10  # as tests/test_gpu_parity.py::test_sweeps_match_oracle
 SWEEP_TOL_F32 = 1e-4   # FP32 sweeps against the FP64 oracle, as there
-MODES = [0, 1, 2, 3, 4, 5, 6, 7]  # sync-free, levels, groups, block, parts, chains, tiles, auto
+MODES = [0, 1, 2, 3, 4, 5, 6, 7, 8]  # sync-free, levels, groups, block, parts, chains, tiles, auto, cluster
 NU, RHO, G = 0.3, 1.0, (0.0, 0.0, -1e-3)
 
 
