@@ -62,7 +62,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     if (not os.path.exists(LIB)) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB, *objs]
+        cmd = [nvcc, *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", LIB, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

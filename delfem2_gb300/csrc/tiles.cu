@@ -65,6 +65,7 @@
 #include <functional>
 #include <mutex>
 #include <queue>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -748,21 +749,26 @@ namespace {
 // loaded in fours), 8 or 16.
 unsigned tile_rounds(unsigned m) { return round4u(m) <= 8 ? 8u : 16u; }
 
-int tile_build(dfm2g_ilu_s *p, bool fwd, TileSched &ts) {
-  ts.ok = false;
-  const unsigned n = p->nblk;
-  if (n >= kTiGlobal) return DFM2G_OK;  // row ids must fit the codes' 30 bits
-  std::vector<unsigned> rs, col, dia, order;
-  DFM2G_CUDA(cudaStreamSynchronize(stream()));
-  DFM2G_TRY(tile_to_host(rs, p->row_start.p, (size_t)n + 1));
-  DFM2G_TRY(tile_to_host(col, p->col.p, p->nnz));
-  DFM2G_TRY(tile_to_host(dia, p->dia_ind.p, n));
-  DFM2G_TRY(tile_to_host(order, fwd ? p->order_f.p : p->order_b.p, n));
+// The host part of a direction's tile schedule (no CUDA calls, so the two
+// directions can be built at once on two host threads): partition, rows of
+// each tile by local level, group records (row ids, codes), per-step halo
+// lists, tile and step descriptors.
+struct TileHost {
+  bool ok = false;
+  unsigned ntiles = 0, nsteps = 0, M = 0, max_groups = 0, max_halo = 0;
+  size_t ngroups = 0;
+  std::vector<uint4> tiles, steps;
+  std::vector<unsigned> rec_of, gmeta, halo;
+};
+
+void tile_host_build(unsigned n, const std::vector<unsigned> &rs, const std::vector<unsigned> &col,
+                     const std::vector<unsigned> &dia, const std::vector<unsigned> &order, bool fwd, TileHost &out) {
+  out.ok = false;
   std::vector<unsigned> tile_of, lev;
   unsigned ntiles = 0, m = 0;
   tile_partition(n, rs.data(), dia.data(), col.data(), order.data(), fwd, kTiRows, kTiSegs, tile_of, lev, ntiles,
                  m);
-  if (m > 16) return DFM2G_OK;  // rows too long for the register rounds
+  if (m > 16) return;  // rows too long for the register rounds
   const unsigned M = std::max(m, 1u);
   // rows of each tile by (local level, level order)
   std::vector<unsigned> tstart(ntiles + 1, 0u), trows(n);
@@ -857,28 +863,77 @@ int tile_build(dfm2g_ilu_s *p, bool fwd, TileSched &ts) {
     tiles[2 * t].w = (unsigned)ngroups - tiles[2 * t].z;
     tiles[2 * t + 1].y = (unsigned)halo.size() - tiles[2 * t + 1].x;
   }
-  if ((ngroups + 1) * kTiG >= 0xFFFFFFFFull || halo.size() >= 0xFFFFFFFFull) return DFM2G_OK;
-  ts.ntiles = ntiles;
-  ts.nsteps = (unsigned)(steps.size() / 2);
+  if ((ngroups + 1) * kTiG >= 0xFFFFFFFFull || halo.size() >= 0xFFFFFFFFull) return;
+  out.ntiles = ntiles;
+  out.nsteps = (unsigned)(steps.size() / 2);
+  out.M = M;
+  out.max_groups = max_groups;
+  out.max_halo = max_halo;
+  out.ngroups = ngroups;
+  out.tiles = std::move(tiles);
+  out.steps = std::move(steps);
+  out.rec_of = std::move(rec_of);
+  out.gmeta = std::move(gmeta);
+  out.halo = std::move(halo);
+  out.ok = true;
+}
+
+int tile_upload(unsigned n, const TileHost &h, TileSched &ts) {
+  ts.ok = false;
+  if (!h.ok) return DFM2G_OK;
+  ts.ntiles = h.ntiles;
+  ts.nsteps = h.nsteps;
   ts.rows_per_step = ts.nsteps ? (double)n / ts.nsteps : 0.0;
-  ts.ngroups = ngroups;
-  ts.max_groups = max_groups;
-  ts.max_halo = max_halo;
-  ts.M = M;
-  DFM2G_TRY(ts.tiles.resize(tiles.size() + 2));
-  DFM2G_TRY(ts.steps.resize(steps.size() + 2));
+  ts.ngroups = h.ngroups;
+  ts.max_groups = h.max_groups;
+  ts.max_halo = h.max_halo;
+  ts.M = h.M;
+  DFM2G_TRY(ts.tiles.resize(h.tiles.size() + 2));
+  DFM2G_TRY(ts.steps.resize(h.steps.size() + 2));
   DFM2G_TRY(ts.rec_of.resize((size_t)n + 1));
-  DFM2G_TRY(ts.gmeta.resize(gmeta.size() + 1));
-  DFM2G_TRY(ts.halo.resize(halo.size() + 4));
+  DFM2G_TRY(ts.gmeta.resize(h.gmeta.size() + 1));
+  DFM2G_TRY(ts.halo.resize(h.halo.size() + 4));
   DFM2G_TRY(ts.ctr.resize(2));
-  DFM2G_CUDA(cudaMemcpy(ts.tiles.p, tiles.data(), sizeof(uint4) * tiles.size(), cudaMemcpyHostToDevice));
-  DFM2G_CUDA(cudaMemcpy(ts.steps.p, steps.data(), sizeof(uint4) * steps.size(), cudaMemcpyHostToDevice));
-  DFM2G_CUDA(cudaMemcpy(ts.rec_of.p, rec_of.data(), sizeof(unsigned) * n, cudaMemcpyHostToDevice));
-  DFM2G_CUDA(cudaMemcpy(ts.gmeta.p, gmeta.data(), sizeof(unsigned) * gmeta.size(), cudaMemcpyHostToDevice));
-  if (!halo.empty())
-    DFM2G_CUDA(cudaMemcpy(ts.halo.p, halo.data(), sizeof(unsigned) * halo.size(), cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.tiles.p, h.tiles.data(), sizeof(uint4) * h.tiles.size(), cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.steps.p, h.steps.data(), sizeof(uint4) * h.steps.size(), cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.rec_of.p, h.rec_of.data(), sizeof(unsigned) * n, cudaMemcpyHostToDevice));
+  DFM2G_CUDA(cudaMemcpy(ts.gmeta.p, h.gmeta.data(), sizeof(unsigned) * h.gmeta.size(), cudaMemcpyHostToDevice));
+  if (!h.halo.empty())
+    DFM2G_CUDA(cudaMemcpy(ts.halo.p, h.halo.data(), sizeof(unsigned) * h.halo.size(), cudaMemcpyHostToDevice));
   DFM2G_CUDA(cudaMemset(ts.ctr.p, 0, 2 * sizeof(unsigned)));
   ts.ok = true;
+  return DFM2G_OK;
+}
+
+// Builds the tile schedules of both directions that are not built yet (the
+// host parts on two threads when both are due).
+int tile_build(dfm2g_ilu_s *p) {
+  const unsigned n = p->nblk;
+  const bool need_f = !p->ts_f.built, need_b = !p->ts_b.built;
+  p->ts_f.built = p->ts_b.built = true;
+  if (!need_f && !need_b) return DFM2G_OK;
+  if (need_f) p->ts_f.ok = false;
+  if (need_b) p->ts_b.ok = false;
+  if (n >= kTiGlobal) return DFM2G_OK;  // row ids must fit the codes' 30 bits
+  std::vector<unsigned> rs, col, dia, order_f, order_b;
+  DFM2G_CUDA(cudaStreamSynchronize(stream()));
+  DFM2G_TRY(tile_to_host(rs, p->row_start.p, (size_t)n + 1));
+  DFM2G_TRY(tile_to_host(col, p->col.p, p->nnz));
+  DFM2G_TRY(tile_to_host(dia, p->dia_ind.p, n));
+  if (need_f) DFM2G_TRY(tile_to_host(order_f, p->order_f.p, n));
+  if (need_b) DFM2G_TRY(tile_to_host(order_b, p->order_b.p, n));
+  TileHost hf, hb;
+  if (need_f && need_b) {
+    std::thread tb([&]() { tile_host_build(n, rs, col, dia, order_b, false, hb); });
+    tile_host_build(n, rs, col, dia, order_f, true, hf);
+    tb.join();
+  } else if (need_f) {
+    tile_host_build(n, rs, col, dia, order_f, true, hf);
+  } else {
+    tile_host_build(n, rs, col, dia, order_b, false, hb);
+  }
+  if (need_f) DFM2G_TRY(tile_upload(n, hf, p->ts_f));
+  if (need_b) DFM2G_TRY(tile_upload(n, hb, p->ts_b));
   return DFM2G_OK;
 }
 
@@ -931,10 +986,7 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   *usable = false;
   if (p->ndim != 3) return DFM2G_OK;
   if (!may_alloc && (!ts.built || !ts.ok || !tile_bytes(ts, T(0)).p)) return DFM2G_OK;
-  if (!ts.built) {
-    ts.built = true;
-    DFM2G_TRY(tile_build(p, forward, ts));
-  }
+  if (!ts.built) DFM2G_TRY(tile_build(p));  // both directions (the other one is swept next)
   if (!ts.ok) return DFM2G_OK;
   const bool f64 = sizeof(T) == 8;
   // DFM2G_SWEEP_AUTO: tiles only where they pay (3.24M / 823K DOF voxel
