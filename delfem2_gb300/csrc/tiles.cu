@@ -681,11 +681,17 @@ void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const u
     for (unsigned u = r; u != none; u = next[u], ++k) seg_of[u] = nseg_total + (unsigned)((uint64_t)k * pieces / len);
     nseg_total += pieces;
   }
-  // offers (layer, rank), smallest first; layer_of[r]: the lowest layer r was offered at in this tile
+  // offers (layer, rank), smallest first; layer_of[r]: the lowest layer r was offered at in this tile.
+  // A row is offered once, when its last unassigned dependency joins the tile (unassigned[r] reaches 0).
   using Offer = std::pair<unsigned, unsigned>;
   std::priority_queue<Offer, std::vector<Offer>, std::greater<Offer>> heap;
   std::vector<unsigned> layer_of(n, none), offered;  // offered: rows whose layer_of is set in this tile
-  std::vector<unsigned> width, seg_tile(nseg_total, none);
+  std::vector<unsigned> width, seg_tile(nseg_total, none), unassigned(n);
+  for (unsigned i = 0; i < n; ++i) {
+    unsigned s0, s1;
+    dep_range(i, s0, s1);
+    unassigned[i] = s1 - s0;
+  }
   unsigned cursor = 0, t = 0;
   for (;;) {
     while (cursor < n && tile_of[order[cursor]] != none) ++cursor;
@@ -708,17 +714,12 @@ void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const u
       if (new_seg && nseg >= max_width) continue;
       unsigned s0, s1;
       dep_range(r, s0, s1);
-      bool ok = true;
-      unsigned lv = 0;
+      unsigned lv = 0;  // every dependency is assigned (the row was offered when the last one joined)
       for (unsigned s = s0; s < s1; ++s) {
         const unsigned d = col[s];
-        if (tile_of[d] == none) {
-          ok = false;
-          break;
-        }
         if (tile_of[d] == t) lv = std::max(lv, lev[d] + 1u);
       }
-      if (!ok || width[lv] >= max_width) continue;  // offered again when another dependency joins
+      if (width[lv] >= max_width) continue;  // left to a later tile
       tile_of[r] = t;
       lev[r] = lv;
       width[lv]++;
@@ -729,13 +730,12 @@ void tile_partition(unsigned n, const unsigned *rs, const unsigned *dia, const u
       }
       for (unsigned k = sptr[r]; k < sptr[r + 1]; ++k) {
         const unsigned u = succ[k];
-        if (tile_of[u] != none) continue;
         // same segment: same layer; another strand: one layer further; the
         // strand's next segment: after every other segment in reach
         const unsigned lay = o.first + (seg_of[u] == seg_of[r] ? 0u : prev[u] == r ? kTiSegFar : 1u);
         if (layer_of[u] == none) offered.push_back(u);
         layer_of[u] = std::min(layer_of[u], lay);
-        heap.push(Offer(layer_of[u], pos[u]));
+        if (--unassigned[u] == 0) heap.push(Offer(layer_of[u], pos[u]));
       }
     }
     ++t;
