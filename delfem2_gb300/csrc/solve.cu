@@ -668,7 +668,10 @@ static int allow_tma_smem(K kernel, size_t smem, int &attr_device) {
   return DFM2G_OK;
 }
 
-// CTAs of k_dot_pupdate<T>: reduce_blocks(), or as many as are resident at once.
+#ifndef DFM2G_DOT_CTAS_PER_SM
+#define DFM2G_DOT_CTAS_PER_SM 4u  // CTAs per SM of k_dot_pupdate
+#endif
+// CTAs of k_dot_pupdate<T>: DFM2G_DOT_CTAS_PER_SM per SM, or as many as are resident at once.
 template <typename T>
 static int dot_pupdate_blocks(unsigned *grid) {
   static int per_sm_dev = -1, per_sm = 0;
@@ -677,7 +680,7 @@ static int dot_pupdate_blocks(unsigned *grid) {
     per_sm_dev = ctx().device;
   }
   if (per_sm <= 0) return fail(DFM2G_ERR_CUDA, "k_dot_pupdate cannot be resident");
-  *grid = std::min<unsigned>(reduce_blocks(), (unsigned)per_sm * (unsigned)ctx().num_sms);
+  *grid = std::min<unsigned>(DFM2G_DOT_CTAS_PER_SM * (unsigned)ctx().num_sms, (unsigned)per_sm * (unsigned)ctx().num_sms);
   return DFM2G_OK;
 }
 
