@@ -96,6 +96,7 @@ SIGNATURES = {
     "dfm2g_ilu_solve_precond_noalloc": [_vp, _i, _vp],
     "dfm2g_ilu_set_sweep_mode": [_vp, _i],
     "dfm2g_ilu_get_sweep_mode": [_vp, _pi],
+    "dfm2g_ilu_last_schedule": [_vp, _i, _i, _pi],
     "dfm2g_ilu_get_pattern": [_vp, _vp, _vp],
     "dfm2g_ilu_info": [_vp, _pu, _psz],
     "dfm2g_ilu_get_row_start": [_vp, _vp],

@@ -390,6 +390,7 @@ struct dfm2g_ilu_s {
   dfm2g::DevBuf<int> nsing;
   int coop_cache[2][2][2] = {};         // resident blocks of the sync-free kernel [f64][fwd][wide]
   unsigned max_lower = 0, max_upper = 0; // longest triangle rows (blocks)
+  int last_sched[2][2] = {{-1, -1}, {-1, -1}};  // schedule of the last sweep [f64][backward]
 };
 
 struct dfm2g_tetmesh_s {

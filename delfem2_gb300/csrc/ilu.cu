@@ -775,6 +775,7 @@ static int coop_blocks(const void *kernel, int *cache) {
 template <typename T, int B>
 static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia,
                          const int *skip, bool prefilled, bool may_alloc) {
+  int &ran = p->last_sched[sizeof(T) == 8 ? 1 : 0][forward ? 0 : 1];
   const unsigned n = p->nblk;
   const uint4 *meta = forward ? p->meta_f.p : p->meta_b.p;
   if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
@@ -796,6 +797,7 @@ static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, cons
     }
     note_launches((unsigned)(ls.size() - 1) + (in != out ? 1u : 0u));
     DFM2G_LAUNCH_CHECK();
+    ran = DFM2G_SWEEP_LEVELS;
     return DFM2G_OK;
   }
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
@@ -805,7 +807,10 @@ static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, cons
     bool usable = false;
     DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev_c, may_alloc,
                              &usable));
-    if (usable) return DFM2G_OK;  // else (records too long for the ring): the sync-free schedule below
+    if (usable) {
+      ran = DFM2G_SWEEP_CHAINS;
+      return DFM2G_OK;
+    }  // else (records too long for the ring): the sync-free schedule below
   }
   void *kernel = forward ? (void *)k_sweep_syncfree_nd<T, true, B> : (void *)k_sweep_syncfree_nd<T, false, B>;
   int *cache = &p->coop_cache[sizeof(T) == 8 ? 1 : 0][forward ? 1 : 0][0];
@@ -820,6 +825,7 @@ static int nd_sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, cons
                   (void *)&out, (void *)&err, (void *)&timeout, (void *)&skip};
   DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(256), args, 0, stream()));
   note_launches(1);
+  ran = DFM2G_SWEEP_SYNCFREE;
   return DFM2G_OK;
 }
 
@@ -830,6 +836,7 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
   if (n == 0) return DFM2G_OK;
   if (p->ndim == 1) return nd_sweep_impl<T, 1>(p, forward, in, out, vcrs, vdia, skip, prefilled, may_alloc);
   if (p->ndim == 2) return nd_sweep_impl<T, 2>(p, forward, in, out, vcrs, vdia, skip, prefilled, may_alloc);
+  int &ran = p->last_sched[sizeof(T) == 8 ? 1 : 0][forward ? 0 : 1];
   if (p->sweep_mode == DFM2G_SWEEP_LEVELS) {
     // levels in order; rows of one level are independent (in == out allowed)
     if (in != out) {
@@ -849,24 +856,32 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     }
     note_launches((unsigned)(ls.size() - 1) + (in != out ? 1u : 0u));
     DFM2G_LAUNCH_CHECK();
+    ran = DFM2G_SWEEP_LEVELS;
     return DFM2G_OK;
   }
   if ((const void *)in == (const void *)out) return fail(DFM2G_ERR_ARG, "sync-free sweep needs in != out");
   if (p->sweep_mode == DFM2G_SWEEP_CLUSTER) {
     bool usable = false;
     DFM2G_TRY(cluster_sweep<T>(p, forward, in, out, vcrs, vdia, skip, &usable));
-    if (usable) return DFM2G_OK;  // else (the vector exceeds shared memory): the automatic choice below
+    if (usable) {
+      ran = DFM2G_SWEEP_CLUSTER;
+      return DFM2G_OK;
+    }  // else (the vector exceeds shared memory): the automatic choice below
   }
   if (p->sweep_mode == DFM2G_SWEEP_BLOCK) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(stream_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
                               &usable));
-    if (usable) return DFM2G_OK;  // else (a row too long for a unit, or not built): the sync-free schedule below
+    if (usable) {
+      ran = DFM2G_SWEEP_BLOCK;
+      return DFM2G_OK;
+    }  // else (a row too long for a unit, or not built): the sync-free schedule below
   }
   if (p->sweep_mode == DFM2G_SWEEP_PARTS && p->parts_ok) {
     if (!prefilled) DFM2G_CUDA(cudaMemsetAsync(out, 0xFF, sizeof(T) * n * 3, stream()));
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
+    ran = DFM2G_SWEEP_PARTS;
     return part_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev);
   }
   // sync-free, tile, chain and blob schedules: `out` is filled with the pending marker
@@ -877,19 +892,27 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
     bool usable = false;
     DFM2G_TRY(tile_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
                             auto_pick, &usable));
-    if (usable) return DFM2G_OK;  // else (rows too long for the tiles, not built, or not picked): the chains below
+    if (usable) {
+      ran = DFM2G_SWEEP_TILES;
+      return DFM2G_OK;
+    }  // else (rows too long for the tiles, not built, or not picked): the chains below
   }
   if (p->sweep_mode == DFM2G_SWEEP_CHAINS || p->sweep_mode == DFM2G_SWEEP_TILES || auto_pick) {
     const unsigned nlev = forward ? p->nlev_f : p->nlev_b;
     bool usable = false;
     DFM2G_TRY(chain_sweep<T>(p, forward, in, out, vcrs, vdia, skip, kWaitTimeoutNs + 20000ull * nlev, may_alloc,
                              &usable));
-    if (usable) return DFM2G_OK;  // else (records too long for the ring): the sync-free schedule below
+    if (usable) {
+      ran = DFM2G_SWEEP_CHAINS;
+      return DFM2G_OK;
+    }  // else (records too long for the ring): the sync-free schedule below
   }
   if constexpr (sizeof(T) == 4) {
     const GroupSched &gs = forward ? p->gs_f : p->gs_b;
-    if (p->sweep_mode == DFM2G_SWEEP_GROUPS && gs.ok && gs.values_ok)
+    if (p->sweep_mode == DFM2G_SWEEP_GROUPS && gs.ok && gs.values_ok) {
+      ran = DFM2G_SWEEP_GROUPS;
       return group_sweep(p, forward, (const float *)in, (float *)out, skip);
+    }
   }
   const unsigned longest = forward ? p->max_lower : p->max_upper;
   const bool wide = longest > 12 && longest <= 24;
@@ -907,6 +930,7 @@ static int sweep_impl(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T
                   (void *)&out, (void *)&err, (void *)&timeout, (void *)&skip};
   DFM2G_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(256), args, 0, stream()));
   note_launches(1);
+  ran = DFM2G_SWEEP_SYNCFREE;
   return DFM2G_OK;
 }
 
@@ -1293,6 +1317,14 @@ int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode) {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!mode) return fail(DFM2G_ERR_ARG, "get_sweep_mode: null out");
   *mode = p->sweep_mode;
+  return DFM2G_OK;
+}
+
+int dfm2g_ilu_last_schedule(dfm2g_ilu p, int prec, int backward, int *mode) {
+  DFM2G_TRY(check_ilu(p, false, false));
+  if (!mode) return fail(DFM2G_ERR_ARG, "last_schedule: null out");
+  if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "last_schedule: bad precision");
+  *mode = p->last_sched[prec == DFM2G_F64 ? 1 : 0][backward ? 1 : 0];
   return DFM2G_OK;
 }
 

@@ -990,9 +990,9 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   if (!ts.ok) return DFM2G_OK;
   const bool f64 = sizeof(T) == 8;
   // DFM2G_SWEEP_AUTO: tiles only where they pay (3.24M / 823K DOF voxel
-  // blocks: 33-35 rows per step; cloth sheets 9-11 and ILU(1) of a voxel
-  // block 7, where the chains are 1.1-1.6x faster; FP64 on 26 tiles of a 32^3
-  // block: the chains by 7%)
+  // blocks: 33-35 rows per step; cloth sheets 9-11 and ILU(1) of voxel
+  // blocks from 48^3 up 7-8, where the chains are 1.1-1.6x faster; FP64 on 26
+  // tiles of a 32^3 block: the chains by 7%)
   if (pick && (ts.rows_per_step < kTiAutoRows || (f64 && 2u * ts.ntiles < (unsigned)ctx().num_sms)))
     return DFM2G_OK;
   const unsigned S = (unsigned)sizeof(T);

@@ -247,6 +247,12 @@ class CPreconditionerILU:
         N.call("dfm2g_ilu_get_sweep_mode", self._h, C.byref(m))
         return m.value
 
+    def last_schedule(self, fp64: bool, backward: bool) -> int:
+        """Schedule the last forward/backward sweep in FP64 or FP32 ran (-1: none yet)."""
+        m = C.c_int(0)
+        N.call("dfm2g_ilu_last_schedule", self._h, N.F64 if fp64 else N.F32, int(backward), C.byref(m))
+        return m.value
+
     def row_start(self):
         """Row offsets of the ILU pattern (the matrix's for ILU(0))."""
         rs = np.zeros(self.nblk + 1, np.uint32)

@@ -232,6 +232,12 @@ DFM2G_API int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec);
 DFM2G_API int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode);
 /* Current schedule (a new pattern starts with DFM2G_SWEEP_AUTO). */
 DFM2G_API int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode);
+/* Schedule the last forward (backward = 0) or backward (backward = 1) sweep of
+ * precision `prec` ran: one of the DFM2G_SWEEP_* schedules other than
+ * DFM2G_SWEEP_AUTO (which picks among them), or -1 before the first sweep.
+ * Shows which schedule the automatic choice, or a fallback of an explicit
+ * mode, took. Host only: reads a value the host recorded at launch. */
+DFM2G_API int dfm2g_ilu_last_schedule(dfm2g_ilu p, int prec, int backward, int *mode);
 /* Inspection (host outputs): sorted pattern (col: nnz, dia_ind: nblk), factor
  * values, level sets (level: nblk, order: nblk, level_start: nlevels+1 with
  * room for nblk+1). */

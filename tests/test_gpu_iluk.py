@@ -108,7 +108,7 @@ def test_iluk_tiles_with_rows_read_in_global_memory(gpu, port):
     ilu.Initialize_ILUk(P.K, 1)
     ilu.CopyValue(P.K)
     assert ilu.Decompose()
-    ilu.set_sweep_mode(6)  # the default would take the chains here: 7-8 rows per step
+    ilu.set_sweep_mode(6)  # the default takes the chains backward here (19.6 rows per step)
     rs = ilu.row_start()
     col, dia = ilu.pattern()
     vc, vd = ilu.values()
