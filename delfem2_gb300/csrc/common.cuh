@@ -338,22 +338,23 @@ struct ChainSched {
   dfm2g::DevBuf<unsigned> ctr;      // chain counter and done-ticket of the launch
 };
 
-// Tiles of one sweep direction (tiles.cu): tile and step descriptors, the
-// record of each row, group headers and codes, per-step halo lists, and the
-// records per value type (rewritten after each decomposition).
+// Tiles of one sweep direction and value type (tiles.cu; FP32 and FP64 tiles
+// differ in size): tile and step descriptors, the record of each row, group
+// headers and codes, per-step halo lists, and the records (rewritten after
+// each decomposition).
 struct TileSched {
   bool built = false, ok = false;
   unsigned ntiles = 0, nsteps = 0, M = 0, max_groups = 0, max_halo = 0;  // M: dependency slots per row
   double rows_per_step = 0;           // rows / steps: how full the tiles' steps are
   size_t ngroups = 0;
-  unsigned ver32 = ~0u, ver64 = ~0u;  // factor_version the records were written from
-  int coop[2] = {0, 0};               // resident CTAs of the sweep kernel [f64]
+  unsigned ver = ~0u;                 // factor_version the records were written from
+  int coop = 0;                       // resident CTAs of the sweep kernel
   dfm2g::DevBuf<uint4> tiles;         // 2 per tile: {first step, steps, first group, groups}, {halo words}
   dfm2g::DevBuf<uint4> steps;         // 2 per step: {first group, rows, local base, groups}, {halo list}
   dfm2g::DevBuf<unsigned> halo;       // per step: the rows of other tiles it reads
   dfm2g::DevBuf<unsigned> rec_of;     // 10 * group + position of each row
   dfm2g::DevBuf<unsigned> gmeta;      // per group: 10 row ids, then codes [10][Mc]
-  dfm2g::DevBuf<unsigned char> bytes32, bytes64;
+  dfm2g::DevBuf<unsigned char> bytes; // the records
   dfm2g::DevBuf<unsigned> ctr;        // tile counter and done-ticket of the launch
 };
 
@@ -374,7 +375,7 @@ struct dfm2g_ilu_s {
   PartSched parts_f, parts_b;           // row-range partitions (forward, backward)
   StreamSched ss32_f, ss32_b, ss64_f, ss64_b;  // level streams of the single-CTA sweep
   ChainSched cs_f, cs_b;                // chain schedules (forward, backward)
-  TileSched ts_f, ts_b;                 // tile schedules (forward, backward)
+  TileSched tiles[2][2];                // tile schedules [f64][backward]
   dfm2g::DevBuf<double> in_lv64;        // right-hand side gathered in level order
   dfm2g::DevBuf<float> in_lv32;
   unsigned factor_version = 0;          // incremented by each decomposition

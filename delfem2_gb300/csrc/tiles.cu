@@ -8,10 +8,11 @@
 // Inside a tile the rows are grouped by their local level (1 + the highest
 // local level of the rows of the same tile they depend on): the tile's steps,
 // at most one row per segment each. On a structured mesh in its natural order
-// the tiles are columns of the grid (7 x 7 z lines, 33 rows deep, on the voxel
-// meshes, whose dependencies all point to lower neighbours): about 45 steps
-// of up to 49 rows per tile, and a dependency path crosses a tile boundary
-// once per tile instead of once per row or pencil of rows.
+// the tiles are columns of the grid (7 x 7 z lines on the voxel meshes, whose
+// dependencies all point to lower neighbours: whole lines of up to 65 rows for
+// FP32 sweeps, 33-row segments for FP64, whose tiles hold at most 1,617 rows):
+// steps of up to 49 rows, and a dependency path crosses a tile boundary once
+// per tile instead of once per row or pencil of rows.
 //
 // One CTA sweeps one tile at a time, step by step: ten rows per consumer
 // warp and step, three lanes per row (lane 3q + c of row q): lane c reads
@@ -51,7 +52,7 @@
 // D^-1 in the forward sweep) values per lane):
 //   [0, 48)   u32 row id of each of the ten rows (~0u: none), padding
 //   [48, ..)  u32 code[G][Mc]: 0x80000000 | local index (a row of the same
-//             tile, or kTiZero for an unused slot); 0x40000000 | row (a row
+//             tile, or tile_rows for an unused slot); 0x40000000 | row (a row
 //             of another tile read in global memory: beyond the step's first
 //             kTiHalo, or so close to the end of the vector that its 32-byte
 //             copy would pass it); else a halo entry: bits 0-7 its index in
@@ -75,13 +76,18 @@ namespace dfm2g {
 
 namespace {
 
-#ifndef DFM2G_TILE_ROWS
-#define DFM2G_TILE_ROWS 1617  // rows per tile at most: 49 segments of 33 rows
+// rows per tile at most: FP32 49 segments of 65 rows (7 x 7 whole z lines on
+// the voxel grids up to 64 cells high), FP64 49 of 33 (its shared-memory copy
+// of the tile's results is twice as wide and would leave too few ring slots)
+#ifndef DFM2G_TILE_ROWS_F32
+#define DFM2G_TILE_ROWS_F32 3185
+#endif
+#ifndef DFM2G_TILE_ROWS_F64
+#define DFM2G_TILE_ROWS_F64 1617
 #endif
 #ifndef DFM2G_TILE_WARPS
 #define DFM2G_TILE_WARPS 5  // consumer warps per CTA (ten rows each per step)
 #endif
-constexpr unsigned kTiRows = DFM2G_TILE_ROWS;
 constexpr unsigned kTiWarps = DFM2G_TILE_WARPS;
 constexpr unsigned kTiG = 10;                   // rows per group (30 lanes)
 constexpr unsigned kTiWidth = kTiG * kTiWarps;  // rows per step at most
@@ -97,7 +103,6 @@ constexpr unsigned kTiCons = 32 * kTiWarps;     // consumer threads
 constexpr unsigned kTiHead = 48;
 constexpr unsigned kTiLocal = 0x80000000u;
 constexpr unsigned kTiGlobal = 0x40000000u;     // code: a row read in global memory (low 30 bits)
-constexpr unsigned kTiZero = kTiRows;           // local index of the all-zero row
 constexpr unsigned kTiEnd = 0xFFFFFFFFu;
 constexpr unsigned kTiMaxSlots = 12;
 constexpr unsigned kTiHalo = 128;               // halo rows copied per step (32 B each; index in 8 bits)
@@ -107,6 +112,7 @@ constexpr unsigned kTiHalo = 128;               // halo rows copied per step (32
 constexpr unsigned kTiHaloLead = DFM2G_TILE_HALO_LEAD;
 constexpr unsigned kTiMinLead = 2;  // consumers wait for step s + 1's halo before step s's barrier
 constexpr double kTiAutoRows = 20.0;            // DFM2G_SWEEP_AUTO: least rows per step for tiles
+constexpr unsigned kTiAutoDeps = 8;             // DFM2G_SWEEP_AUTO: most dependency blocks per row for tiles
 constexpr unsigned kTiGrabLead = 4;             // steps before a tile's end at which the next tile is taken
 constexpr size_t kTiSmemCap = 227u * 1024u;
 static_assert(kTiWarps >= 1 && kTiWarps <= 15, "named barrier of the consumer warps");
@@ -114,6 +120,11 @@ static_assert(kTiHalo <= 256, "halo index in 8 bits");
 static_assert(kTiHaloLead >= kTiMinLead, "halo lead");
 
 __host__ __device__ inline unsigned pad16u(unsigned x) { return (x + 15u) & ~15u; }
+// rows per tile at most for values of S bytes; also the local index of the
+// all-zero row that unused dependency slots point to
+__host__ __device__ constexpr unsigned tile_rows(unsigned S) {
+  return S == 8u ? DFM2G_TILE_ROWS_F64 : DFM2G_TILE_ROWS_F32;
+}
 __host__ __device__ inline unsigned round4u(unsigned x) { return (x + 3u) & ~3u; }
 
 struct TileGeom {
@@ -151,11 +162,11 @@ inline SlotGeom slot_geom(unsigned max_groups, unsigned gbytes, unsigned S) {
 }
 
 // Shared memory of the sweep kernel: barriers [0, 288), slot descriptors
-// [512, 896), stop flags [960, 968), the tile's results (kTiRows + 1 rows),
+// [512, 896), stop flags [960, 968), the tile's results (tile_rows + 1 rows),
 // the slot ring.
 __host__ __device__ inline size_t tile_xs_off() { return 1024; }
 __host__ __device__ inline size_t tile_ring_off(unsigned S) {
-  return tile_xs_off() + pad16u((kTiRows + 1u) * 3u * S);
+  return tile_xs_off() + pad16u((tile_rows(S) + 1u) * 3u * S);
 }
 inline size_t tile_smem(unsigned S, unsigned slots, unsigned slot_bytes) {
   return tile_ring_off(S) + (size_t)slots * slot_bytes;
@@ -223,6 +234,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
                   const int *skip) {
   extern __shared__ __align__(128) unsigned char ti_smem[];
   if (skip && *skip) return;
+  constexpr unsigned kZero = tile_rows((unsigned)sizeof(T));  // local index of the all-zero row
   uint64_t *full = reinterpret_cast<uint64_t *>(ti_smem);
   uint64_t *empty = full + kTiMaxSlots;
   uint64_t *hbar = empty + kTiMaxSlots;
@@ -241,7 +253,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
     sflag[0] = sflag[1] = 0;
     mbar_fence_init();
   }
-  if (threadIdx.x < 3) xs[(size_t)kTiZero * 3 + threadIdx.x] = T(0);
+  if (threadIdx.x < 3) xs[(size_t)kZero * 3 + threadIdx.x] = T(0);
   __syncthreads();
 
   if (warp == kTiWarps) {
@@ -451,8 +463,8 @@ __global__ void __launch_bounds__(kTiThreads, 1)
 #pragma unroll
     for (unsigned k = 0; k < MR / 4; ++k) {
       const uint4 c = (4u * k < Mc) ? cw[k]
-                                    : make_uint4(kTiLocal | kTiZero, kTiLocal | kTiZero, kTiLocal | kTiZero,
-                                                 kTiLocal | kTiZero);
+                                    : make_uint4(kTiLocal | kZero, kTiLocal | kZero, kTiLocal | kZero,
+                                                 kTiLocal | kZero);
       P.cd[4 * k + 0] = c.x;
       P.cd[4 * k + 1] = c.y;
       P.cd[4 * k + 2] = c.z;
@@ -470,7 +482,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       const unsigned c = P.cd[b];
       const bool loc = (c & kTiLocal) != 0u, glob = !loc && (c & kTiGlobal) != 0u;
       const unsigned off = sizeof(T) == 4 ? ((c >> 8) & 3u) * 4u : ((c >> 10) & 1u) * 8u;
-      const T *xp = (loc || glob) ? xs + (size_t)kTiZero * 3 : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off);
+      const T *xp = (loc || glob) ? xs + (size_t)kZero * 3 : reinterpret_cast<const T *>(hd + (c & 0xFFu) * 32u + off);
       T x = xp[a];
       if (!loc && (glob || is_pending(x))) {
         const unsigned r = glob ? (c & ~kTiGlobal) : hl[c & 0xFFu];
@@ -497,7 +509,7 @@ __global__ void __launch_bounds__(kTiThreads, 1)
       for (unsigned b = 0; b < MR; ++b) {
         const unsigned c = P.cd[b];
         // codes of other tiles' rows are no index into xs: the zero row is read instead
-        const unsigned li = (c & kTiLocal) ? (c & ~kTiLocal) : kTiZero;
+        const unsigned li = (c & kTiLocal) ? (c & ~kTiLocal) : kZero;
         const T x = xs[(size_t)li * 3 + a];
         xv[b] = (c & kTiLocal) ? x : P.xh[b];
       }
@@ -761,12 +773,15 @@ struct TileHost {
   std::vector<unsigned> rec_of, gmeta, halo;
 };
 
+// Tiles of at most max_rows rows (unused dependency slots point to local row
+// max_rows, the all-zero row).
 void tile_host_build(unsigned n, const std::vector<unsigned> &rs, const std::vector<unsigned> &col,
-                     const std::vector<unsigned> &dia, const std::vector<unsigned> &order, bool fwd, TileHost &out) {
+                     const std::vector<unsigned> &dia, const std::vector<unsigned> &order, bool fwd,
+                     unsigned max_rows, TileHost &out) {
   out.ok = false;
   std::vector<unsigned> tile_of, lev;
   unsigned ntiles = 0, m = 0;
-  tile_partition(n, rs.data(), dia.data(), col.data(), order.data(), fwd, kTiRows, kTiSegs, tile_of, lev, ntiles,
+  tile_partition(n, rs.data(), dia.data(), col.data(), order.data(), fwd, max_rows, kTiSegs, tile_of, lev, ntiles,
                  m);
   if (m > 16) return;  // rows too long for the register rounds
   const unsigned M = std::max(m, 1u);
@@ -828,7 +843,7 @@ void tile_host_build(unsigned n, const std::vector<unsigned> &rs, const std::vec
       for (size_t g = ngroups; g < ngroups + ng; ++g)
         for (unsigned q = 0; q < kTiG; ++q) {
           gmeta[g * words + q] = ~0u;
-          for (unsigned bb = 0; bb < Mc; ++bb) gmeta[g * words + kTiG + q * Mc + bb] = kTiLocal | kTiZero;
+          for (unsigned bb = 0; bb < Mc; ++bb) gmeta[g * words + kTiG + q * Mc + bb] = kTiLocal | max_rows;
         }
       for (unsigned u = 0; u < w; ++u) {
         const unsigned i = b[k + u];
@@ -905,35 +920,43 @@ int tile_upload(unsigned n, const TileHost &h, TileSched &ts) {
   return DFM2G_OK;
 }
 
-// Builds the tile schedules of both directions that are not built yet (the
-// host parts on two threads when both are due).
+// Builds the tile schedules that are not built yet, of both value types and
+// both directions (the FP64 ones on first use of the FP32 ones and the other
+// way round, so that a first solve in the other precision finds them): the
+// host partitions on one thread each.
 int tile_build(dfm2g_ilu_s *p) {
   const unsigned n = p->nblk;
-  const bool need_f = !p->ts_f.built, need_b = !p->ts_b.built;
-  p->ts_f.built = p->ts_b.built = true;
-  if (!need_f && !need_b) return DFM2G_OK;
-  if (need_f) p->ts_f.ok = false;
-  if (need_b) p->ts_b.ok = false;
+  bool need[2][2], any = false, need_dir[2] = {false, false};
+  for (int f = 0; f < 2; ++f)
+    for (int d = 0; d < 2; ++d) {
+      TileSched &ts = p->tiles[f][d];
+      need[f][d] = !ts.built;
+      ts.built = true;
+      if (need[f][d]) ts.ok = false;
+      any |= need[f][d];
+      need_dir[d] |= need[f][d];
+    }
+  if (!any) return DFM2G_OK;
   if (n >= kTiGlobal) return DFM2G_OK;  // row ids must fit the codes' 30 bits
-  std::vector<unsigned> rs, col, dia, order_f, order_b;
+  std::vector<unsigned> rs, col, dia, order[2];
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   DFM2G_TRY(tile_to_host(rs, p->row_start.p, (size_t)n + 1));
   DFM2G_TRY(tile_to_host(col, p->col.p, p->nnz));
   DFM2G_TRY(tile_to_host(dia, p->dia_ind.p, n));
-  if (need_f) DFM2G_TRY(tile_to_host(order_f, p->order_f.p, n));
-  if (need_b) DFM2G_TRY(tile_to_host(order_b, p->order_b.p, n));
-  TileHost hf, hb;
-  if (need_f && need_b) {
-    std::thread tb([&]() { tile_host_build(n, rs, col, dia, order_b, false, hb); });
-    tile_host_build(n, rs, col, dia, order_f, true, hf);
-    tb.join();
-  } else if (need_f) {
-    tile_host_build(n, rs, col, dia, order_f, true, hf);
-  } else {
-    tile_host_build(n, rs, col, dia, order_b, false, hb);
-  }
-  if (need_f) DFM2G_TRY(tile_upload(n, hf, p->ts_f));
-  if (need_b) DFM2G_TRY(tile_upload(n, hb, p->ts_b));
+  if (need_dir[0]) DFM2G_TRY(tile_to_host(order[0], p->order_f.p, n));
+  if (need_dir[1]) DFM2G_TRY(tile_to_host(order[1], p->order_b.p, n));
+  TileHost h[2][2];
+  std::vector<std::thread> workers;
+  for (int f = 0; f < 2; ++f)
+    for (int d = 0; d < 2; ++d)
+      if (need[f][d])
+        workers.emplace_back([&, f, d]() {
+          tile_host_build(n, rs, col, dia, order[d], d == 0, tile_rows(f ? 8u : 4u), h[f][d]);
+        });
+  for (std::thread &w : workers) w.join();
+  for (int f = 0; f < 2; ++f)
+    for (int d = 0; d < 2; ++d)
+      if (need[f][d]) DFM2G_TRY(tile_upload(n, h[f][d], p->tiles[f][d]));
   return DFM2G_OK;
 }
 
@@ -968,9 +991,6 @@ int tile_allow_smem(void *kernel, size_t smem) {
   return DFM2G_OK;
 }
 
-DevBuf<unsigned char> &tile_bytes(TileSched &ts, double) { return ts.bytes64; }
-DevBuf<unsigned char> &tile_bytes(TileSched &ts, float) { return ts.bytes32; }
-
 }  // namespace
 
 // Builds the tiles of one direction (first use), rewrites the records of the
@@ -982,17 +1002,20 @@ DevBuf<unsigned char> &tile_bytes(TileSched &ts, float) { return ts.bytes32; }
 template <typename T>
 int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs, const T *vdia, const int *skip,
                unsigned long long timeout, bool may_alloc, bool pick, bool *usable) {
-  TileSched &ts = forward ? p->ts_f : p->ts_b;
+  const bool f64 = sizeof(T) == 8;
+  TileSched &ts = p->tiles[f64 ? 1 : 0][forward ? 0 : 1];
   *usable = false;
   if (p->ndim != 3) return DFM2G_OK;
-  if (!may_alloc && (!ts.built || !ts.ok || !tile_bytes(ts, T(0)).p)) return DFM2G_OK;
-  if (!ts.built) DFM2G_TRY(tile_build(p));  // both directions (the other one is swept next)
+  // DFM2G_SWEEP_AUTO takes no tiles for rows of more than kTiAutoDeps blocks
+  // (ILU(k > 0) of voxel blocks: the chains are 1.5x faster even where its
+  // FP32 tiles hold 25-30 rows per step), so their tiles are not built
+  if (pick && (forward ? p->max_lower : p->max_upper) > kTiAutoDeps) return DFM2G_OK;
+  if (!may_alloc && (!ts.built || !ts.ok || !ts.bytes.p)) return DFM2G_OK;
+  if (!ts.built) DFM2G_TRY(tile_build(p));  // both directions and value types
   if (!ts.ok) return DFM2G_OK;
-  const bool f64 = sizeof(T) == 8;
-  // DFM2G_SWEEP_AUTO: tiles only where they pay (3.24M / 823K DOF voxel
-  // blocks: 33-35 rows per step; cloth sheets 9-11 and ILU(1) of voxel
-  // blocks from 48^3 up 7-8, where the chains are 1.1-1.6x faster; FP64 on 26
-  // tiles of a 32^3 block: the chains by 7%)
+  // DFM2G_SWEEP_AUTO: tiles only where their steps are full (ILU(0) of voxel
+  // blocks: 33-40 rows per step; cloth sheets 9-15, where the chains are
+  // 1.1-1.3x faster; FP64 on 26 tiles of a 32^3 block: the chains by 7%)
   if (pick && (ts.rows_per_step < kTiAutoRows || (f64 && 2u * ts.ntiles < (unsigned)ctx().num_sms)))
     return DFM2G_OK;
   const unsigned S = (unsigned)sizeof(T);
@@ -1006,8 +1029,8 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   unsigned lead = std::min(kTiHaloLead, nslots - 2u);
   const size_t smem = tile_smem(S, nslots, sg.bytes);
   if (smem > kTiSmemCap) return DFM2G_OK;
-  DevBuf<unsigned char> &bytes = tile_bytes(ts, T(0));
-  unsigned &ver = f64 ? ts.ver64 : ts.ver32;
+  DevBuf<unsigned char> &bytes = ts.bytes;
+  unsigned &ver = ts.ver;
   if (!bytes.p) {
     DFM2G_TRY(bytes.resize(ts.ngroups * g.gbytes + 16));
     DFM2G_CUDA(cudaMemsetAsync(bytes.p, 0, ts.ngroups * g.gbytes + 16, stream()));
@@ -1030,7 +1053,7 @@ int tile_sweep(dfm2g_ilu_s *p, bool forward, const T *in, T *out, const T *vcrs,
   const unsigned MR = tile_rounds(ts.M);
   void *kernel = forward ? tile_kernel<T, true>(MR) : tile_kernel<T, false>(MR);
   DFM2G_TRY(tile_allow_smem(kernel, smem));
-  int &cap = ts.coop[f64 ? 1 : 0];
+  int &cap = ts.coop;
   if (cap <= 0) {
     int per_sm = 0;
     DFM2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTiThreads, smem));
@@ -1063,19 +1086,19 @@ template int tile_sweep<double>(dfm2g_ilu_s *, bool, const double *, double *, c
 
 // Drops the tiles and records (a new pattern); rebuilt on first use.
 void tile_schedules_reset(dfm2g_ilu_s *p) {
-  for (TileSched *ts : {&p->ts_f, &p->ts_b}) {
+  for (TileSched *ts : {&p->tiles[0][0], &p->tiles[0][1], &p->tiles[1][0], &p->tiles[1][1]}) {
     ts->built = ts->ok = false;
     ts->ntiles = ts->nsteps = ts->M = ts->max_groups = ts->max_halo = 0;
+    ts->rows_per_step = 0;
     ts->ngroups = 0;
-    ts->ver32 = ts->ver64 = ~0u;
-    ts->coop[0] = ts->coop[1] = 0;
+    ts->ver = ~0u;
+    ts->coop = 0;
     ts->tiles.release();
     ts->steps.release();
     ts->rec_of.release();
     ts->gmeta.release();
     ts->halo.release();
-    ts->bytes32.release();
-    ts->bytes64.release();
+    ts->bytes.release();
     ts->ctr.release();
   }
 }

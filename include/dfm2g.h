@@ -95,11 +95,13 @@ enum dfm2g_sweep {
                                smallest (a cluster barrier and broadcast cost
                                about 1.3 us per level in FP32, 2.9 in FP64)  */
   DFM2G_SWEEP_AUTO = 7      /* the default: DFM2G_SWEEP_TILES where the tiles'
-                               steps hold 20 rows or more on average (and,
-                               for FP64, there are at least half as many
-                               tiles as SMs: the FP64 steps are bound by the
-                               SM's FP64 rate), DFM2G_SWEEP_CHAINS otherwise
-                               (2-D meshes, fill-in patterns, small grids)   */
+                               steps hold 20 rows or more on average, rows
+                               have at most 8 dependency blocks per
+                               triangle and, for FP64, there are at least
+                               half as many tiles as SMs (the FP64 steps are
+                               bound by the SM's FP64 rate);
+                               DFM2G_SWEEP_CHAINS otherwise (2-D meshes,
+                               fill-in patterns, small grids)                */
 };
 
 typedef struct dfm2g_bsr_s *dfm2g_bsr;       /* CMatrixSparse<double>       */
@@ -263,7 +265,8 @@ DFM2G_API int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const
  * row i's tile (numbered in dependency order), level[i] its local level inside
  * the tile; tiles hold at most max_width strand segments of at most
  * max_rows / max_width rows each (so at most max_width rows per local level);
- * the sweep uses max_rows 1617, max_width 49. *max_deps the most blocks of a
+ * the sweep uses max_rows 3185 (FP32) or 1617 (FP64), max_width 49.
+ * *max_deps the most blocks of a
  * row's triangle (forward: strictly lower, backward: strictly upper). */
 DFM2G_API int dfm2g_tile_partition(unsigned n, const unsigned *row_start, const unsigned *col,
                                    const unsigned *dia_ind, const unsigned *order, int backward,

@@ -1,16 +1,17 @@
 """Which schedule the automatic sweep choice (DFM2G_SWEEP_AUTO, the default)
 runs, read back with dfm2g_ilu_last_schedule, against its rule: the tile
-schedule where the tile partition averages at least 20 rows per step and, in
-FP64, has at least half as many tiles as the GPU has SMs; the chain schedule
-otherwise, and always for 1x1 and 2x2 blocks.
+schedule where the tile partition averages at least 20 rows per step, rows
+have at most 8 dependency blocks and, in FP64, the partition has at least
+half as many tiles as the GPU has SMs; the chain schedule otherwise, and
+always for 1x1 and 2x2 blocks.
 
 The partition's rows per step and tile count come from dfm2g_tile_partition
-with the sweep's sizes (1617 rows, 49 rows per step) on the oracle's level
-order. Cases: voxel blocks of 32^3 cells (tiles in FP32; 26 tiles, so the
-chains in FP64) and 48^3 (tiles in both), the cloth sheet's quad pattern
-(about 10 rows per step: chains), ILU(1) of a 48^3 voxel block (7.6 rows per
-step: chains) and of a 28^3 block (about 20 rows per step, either side of the
-bar by direction), a scalar chain pattern (chains). An explicit schedule is the
+with the sweep's sizes (49 rows per step; tiles of 3185 rows in FP32, 1617 in
+FP64) on the oracle's level order. Cases: voxel blocks of 32^3 cells (tiles in
+FP32; 26 tiles, so the chains in FP64) and 48^3 (tiles in both), the cloth
+sheet's quad pattern (9-11 rows per step: chains), ILU(1) of a 48^3 voxel
+block (13 dependency blocks per row: chains, although its FP32 tiles of whole
+z lines reach 25-27 rows per step), a scalar chain pattern (chains). An explicit schedule is the
 one that runs, and the cluster schedule on a vector larger than shared
 memory falls back to the automatic choice."""
 import ctypes as C
@@ -30,6 +31,7 @@ def _rule(lib, port, ilu, fp64):
     rs = np.ascontiguousarray(ilu.row_start(), np.uint32)
     col, dia = (np.ascontiguousarray(a, np.uint32) for a in ilu.pattern())
     n = rs.size - 1
+    rows = 1617 if fp64 else 3185
     out = []
     for backward in (False, True):
         _, order, _ = port.ilu_levels(rs, col, dia, backward)
@@ -37,10 +39,10 @@ def _rule(lib, port, ilu, fp64):
         tile_of, level = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
         nt, m = C.c_uint(0), C.c_uint(0)
         assert lib.dfm2g_tile_partition(n, rs.ctypes.data, col.ctypes.data, dia.ctypes.data, order.ctypes.data,
-                                        int(backward), 1617, 49, tile_of.ctypes.data, level.ctypes.data,
+                                        int(backward), rows, 49, tile_of.ctypes.data, level.ctypes.data,
                                         C.byref(nt), C.byref(m)) == 0
         nsteps = sum(int(level[tile_of == t].max()) + 1 for t in range(nt.value))
-        tiles = n / nsteps >= 20.0 and (not fp64 or 2 * nt.value >= sms)
+        tiles = n / nsteps >= 20.0 and m.value <= 8 and (not fp64 or 2 * nt.value >= sms)
         out.append(TILES if tiles else CHAINS)
     return out
 
@@ -109,16 +111,9 @@ def test_auto_takes_the_chains_on_cloth(gpu, port):
 
 def test_auto_takes_the_chains_on_iluk(gpu, port):
     ilu, n3 = _voxel_ilu(48, k=1)
-    assert _rule(gpu, port, ilu, False) == [CHAINS, CHAINS]
-    assert _sweep_both(ilu, False, n3) == [CHAINS, CHAINS]
-
-
-def test_auto_picks_each_direction_by_its_own_partition(gpu, port):
-    """ILU(1) of a 28^3 block: 20.4 rows per step forward, 19.6 backward."""
-    ilu, n3 = _voxel_ilu(28, k=1)
-    want = _rule(gpu, port, ilu, False)
-    assert want == [TILES, CHAINS]
-    assert _sweep_both(ilu, False, n3) == want
+    for fp64 in (False, True):
+        assert _rule(gpu, port, ilu, fp64) == [CHAINS, CHAINS]
+        assert _sweep_both(ilu, fp64, n3) == [CHAINS, CHAINS], fp64
 
 
 def test_auto_on_scalar_blocks(gpu):

@@ -71,7 +71,8 @@ def test_iluk_sweeps_match_oracle_in_every_schedule(prob, port, mode):
 
 def _outside_rows_per_step(lib, port, rs, col, dia, backward):
     """Most rows of other tiles that one step of the tile schedule depends on
-    (dfm2g_tile_partition with the sweep's sizes)."""
+    (dfm2g_tile_partition with the FP64 sweep's sizes; on a 28^3 block the
+    FP32 tiles are the same, its 29-row z lines being one segment either way)."""
     import ctypes as C
     n = rs.size - 1
     _, order, _ = port.ilu_levels(rs, col, dia, backward)

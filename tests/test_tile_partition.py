@@ -9,7 +9,8 @@ the same tile (0 if none); tiles hold at most max_rows rows and max_width
 rows per local level; tiles are numbered in the level order of their seeds.
 On the natural ordering of a voxel mesh (nodes numbered z fastest, every
 dependency on a lower neighbour) the tiles are columns of the node grid
-(7 x 7 z lines, one segment deep) where the grid allows."""
+(7 x 7 z lines, one segment deep) where the grid allows, for the FP64 and
+the FP32 tile sizes."""
 import ctypes as C
 
 import numpy as np
@@ -60,19 +61,21 @@ def _check(ind, col, dia, order, tile_of, level, nt, m, backward, max_rows, max_
     assert first == sorted(first)
 
 
+@pytest.mark.parametrize("rows,depths,full", [(1617, (20, 21), 4), (3185, (41,), 2)])
 @pytest.mark.parametrize("backward", [False, True])
-def test_voxel_mesh_tiles_are_columns(built_lib, port, backward):
-    """With the sweep kernel's sizes (1617 rows, 49 segments of 33 rows) the
-    strands are the grid's z lines (41 nodes: two segments, 21 + 20 rows) and
-    the tiles are full boxes of them: 7 x 7 columns where the grid holds them,
-    wider flat boxes at its edges."""
+def test_voxel_mesh_tiles_are_columns(built_lib, port, backward, rows, depths, full):
+    """With the sweep kernel's sizes (FP64: 1617 rows, 49 segments of 33 rows;
+    FP32: 3185 rows, 49 segments of 65) the strands are the grid's z lines (41
+    nodes: two segments of 21 + 20 rows, or one whole line) and the tiles are
+    full boxes of them: 7 x 7 columns where the grid holds them, wider flat
+    boxes at its edges."""
     import delfem2_gb300 as D
     nx, ny, nz = 16, 9, 40  # nodes 17 x 10 x 41
     a = D.voxel_problem_arrays(nx, ny, nz, 1.0 / nx, young=1.0)
     ind, psup = a["psup_ind"], a["psup"]
     col, dia = port.ilu_pattern0(ind, psup)
-    tile_of, level, nt, m, order = _partition(built_lib, port, ind, col, dia, backward, 1617, 49)
-    _check(ind, col, dia, order, tile_of, level, nt, m, backward, 1617, 49)
+    tile_of, level, nt, m, order = _partition(built_lib, port, ind, col, dia, backward, rows, 49)
+    _check(ind, col, dia, order, tile_of, level, nt, m, backward, rows, 49)
     assert m == 7
     # node (x, y, z) is row (x * (ny + 1) + y) * (nz + 1) + z
     x, y, z = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
@@ -82,12 +85,13 @@ def test_voxel_mesh_tiles_are_columns(built_lib, port, backward):
         r = tile_of == t
         ext = [int(v[r].max() - v[r].min() + 1) for v in (x, y, z)]
         assert int(r.sum()) == ext[0] * ext[1] * ext[2], (t, ext)  # a full box
-        assert ext[2] in (20, 21) and ext[0] * ext[1] <= 49, (t, ext)  # whole segments, at most 49
+        assert ext[2] in depths and ext[0] * ext[1] <= 49, (t, ext)  # whole segments, at most 49
         assert int(level[r].max()) + 1 == ext[0] + ext[1] + ext[2] - 2  # a plane of the box per step
         columns += ext[:2] == [7, 7]
-    assert columns >= 4
+    assert columns == full  # 2 x 1 full columns of z lines in the 17 x 10 grid, per segment along z
     first = tile_of == 0
-    corner = (x >= nx + 1 - 7, y >= ny + 1 - 7, z >= nz + 1 - 21) if backward else (x < 7, y < 7, z < 21)
+    d = max(depths)
+    corner = (x >= nx + 1 - 7, y >= ny + 1 - 7, z >= nz + 1 - d) if backward else (x < 7, y < 7, z < d)
     assert np.array_equal(first, corner[0] & corner[1] & corner[2])  # the seed's column
 
 
