@@ -617,8 +617,9 @@ int tile_to_host(std::vector<V> &h, const V *d, size_t n) {
 // are offered at the row's layer when they are in its segment, one layer
 // further when they are in another strand, and after every other offer within
 // reach when they start the next segment of its strand, so a tile takes the
-// seed's segment, then the segments next to it at the same depth, and so on: on the voxel grids, columns of 7 x 7 z lines 33 rows
-// deep. A row joins once every row it depends on is assigned (to an earlier
+// seed's segment, then the segments next to it at the same depth, and so on:
+// on the voxel grids, columns of 7 x 7 z-line segments. A row joins once every
+// row it depends on is assigned (to an earlier
 // tile or this one), as long as the tile has fewer than max_rows rows, its
 // segment is in the tile or the tile has fewer than max_width segments, and
 // its local level has fewer than max_width rows. The tiles are numbered along
