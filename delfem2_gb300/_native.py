@@ -23,6 +23,7 @@ ERR_PATTERN = 7
 ERR_UNSUPPORTED = 8
 ERR_STATE = 9
 ERR_NONFINITE = 10
+ERR_HOST = 11
 
 MEM_HOST = 0
 MEM_DEVICE = 1
@@ -147,6 +148,7 @@ SIGNATURES = {
     "dfm2g_alloc_count": [C.POINTER(C.c_ulonglong)],
     "dfm2g_debug_wait_timeout": [_u],
     "dfm2g_debug_grid_barrier": [_u, _i],
+    "dfm2g_debug_host_failure": [_i],
 }
 
 PROF_KINDS = ["spmv", "update", "fill", "fwd", "bwd", "dot", "pupdate", "outer"]

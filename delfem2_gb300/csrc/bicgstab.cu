@@ -134,7 +134,7 @@ using namespace dfm2g;
 extern "C" {
 
 int dfm2g_solve_pbicgstab(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol, unsigned max_iter,
-                          double *hist, unsigned hist_cap, unsigned *n_hist, int mem, dfm2g_solve_stats *stats) {
+                          double *hist, unsigned hist_cap, unsigned *n_hist, int mem, dfm2g_solve_stats *stats) try {
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "solve_pbicgstab: matrix has no pattern");
   if (!p || !p->has_factor || p->nblk != m->nblk)
     return fail(DFM2G_ERR_STATE, "solve_pbicgstab: preconditioner not decomposed for this matrix");
@@ -248,6 +248,8 @@ int dfm2g_solve_pbicgstab(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double
   if (h.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_pbicgstab: non-finite residual");
   if (h.done == 2) return fail(DFM2G_ERR_NOT_CONVERGED, "solve_pbicgstab: %u iterations without reaching tol", h.it);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

@@ -397,7 +397,7 @@ static int check_bsr(dfm2g_bsr m, bool need_pattern = true) {
 
 extern "C" {
 
-int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim) {
+int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim) try {
   if (!out) return fail(DFM2G_ERR_ARG, "bsr_create: null out");
   if (ndim < 1 || ndim > 3) return fail(DFM2G_ERR_UNSUPPORTED, "block size ndim=%u (1, 2 or 3 supported)", ndim);
   DFM2G_TRY(ensure_context());
@@ -406,18 +406,22 @@ int dfm2g_bsr_create(dfm2g_bsr *out, unsigned nblk, unsigned ndim) {
   m->ndim = ndim;
   *out = m;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_destroy(dfm2g_bsr m) {
+int dfm2g_bsr_destroy(dfm2g_bsr m) try {
   if (m) {
     cudaStreamSynchronize(stream());
     delete m;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_start, const unsigned *col,
-                          size_t ncol) {
+                          size_t ncol) try {
   DFM2G_TRY(check_bsr(m, false));
   if (!row_start || n_row_start != (size_t)m->nblk + 1)
     return fail(DFM2G_ERR_ARG, "set_pattern: row_start must have nblk+1 = %u entries", m->nblk + 1);
@@ -458,32 +462,40 @@ int dfm2g_bsr_set_pattern(dfm2g_bsr m, const unsigned *row_start, size_t n_row_s
   if (m->ndim == 3) DFM2G_TRY(bsr_tiles_build(m));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_info(dfm2g_bsr m, unsigned *nblk, size_t *nnz) {
+int dfm2g_bsr_info(dfm2g_bsr m, unsigned *nblk, size_t *nnz) try {
   DFM2G_TRY(check_bsr(m, false));
   if (nblk) *nblk = m->nblk;
   if (nnz) *nnz = m->nnz;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_ndim(dfm2g_bsr m, unsigned *ndim) {
+int dfm2g_bsr_ndim(dfm2g_bsr m, unsigned *ndim) try {
   DFM2G_TRY(check_bsr(m, false));
   if (!ndim) return fail(DFM2G_ERR_ARG, "bsr_ndim: null out");
   *ndim = m->ndim;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_set_zero(dfm2g_bsr m) {
+int dfm2g_bsr_set_zero(dfm2g_bsr m) try {
   DFM2G_TRY(check_bsr(m));
   const size_t bb = (size_t)m->ndim * m->ndim;
   DFM2G_CUDA(cudaMemsetAsync(m->vcrs.p, 0, sizeof(double) * m->nnz * bb, stream()));
   DFM2G_CUDA(cudaMemsetAsync(m->vdia.p, 0, sizeof(double) * m->nblk * bb, stream()));
   m->f32_valid = false;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, int mem) {
+int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, int mem) try {
   DFM2G_TRY(check_bsr(m));
   const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   const size_t bb = (size_t)m->ndim * m->ndim;
@@ -492,9 +504,11 @@ int dfm2g_bsr_set_values(dfm2g_bsr m, const double *vcrs, const double *vdia, in
   if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   m->f32_valid = false;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem) {
+int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem) try {
   DFM2G_TRY(check_bsr(m));
   const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   const size_t bb = (size_t)m->ndim * m->ndim;
@@ -502,9 +516,11 @@ int dfm2g_bsr_get_values(dfm2g_bsr m, double *vcrs, double *vdia, int mem) {
   if (vdia && m->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, m->vdia.p, sizeof(double) * bb * m->nblk, k, stream()));
   if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem) {
+int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem) try {
   DFM2G_TRY(check_bsr(m));
   if (!bc) return fail(DFM2G_ERR_ARG, "set_fixed_bc: null bc");
   VecArg<int> a;
@@ -519,23 +535,29 @@ int dfm2g_bsr_set_fixed_bc(dfm2g_bsr m, const int *bc, int mem) {
   if (mem == DFM2G_MEM_HOST) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   m->f32_valid = false;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_add_dia(dfm2g_bsr m, double eps) {
+int dfm2g_bsr_add_dia(dfm2g_bsr m, double eps) try {
   DFM2G_TRY(check_bsr(m));
   k_add_dia<<<blocks_for(m->nblk, 256, ctx().num_sms * 8), 256, 0, stream()>>>(m->nblk, m->ndim, m->vdia.p, eps);
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_update_f32(dfm2g_bsr m) {
+int dfm2g_bsr_update_f32(dfm2g_bsr m) try {
   DFM2G_TRY(check_bsr(m));
   m->f32_valid = false;
   return bsr_ensure_f32(m);
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x, double beta, int mem) {
+int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x, double beta, int mem) try {
   DFM2G_TRY(check_bsr(m));
   if (!y || !x) return fail(DFM2G_ERR_ARG, "matvec: null vector");
   const size_t n = (size_t)m->nblk * m->ndim;
@@ -556,9 +578,11 @@ int dfm2g_bsr_matvec(dfm2g_bsr m, int prec, void *y, double alpha, const void *x
     return ay.copy_back();
   }
   return fail(DFM2G_ERR_ARG, "matvec: prec must be DFM2G_F64 or DFM2G_F32");
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_vec_zero_bc(double *b, const int *bc, size_t ndof, int mem) {
+int dfm2g_vec_zero_bc(double *b, const int *bc, size_t ndof, int mem) try {
   if (!b || !bc) return fail(DFM2G_ERR_ARG, "vec_zero_bc: null argument");
   DFM2G_TRY(ensure_context());
   VecArg<double> ab;
@@ -568,10 +592,12 @@ int dfm2g_vec_zero_bc(double *b, const int *bc, size_t ndof, int mem) {
   k_zero_bc<<<blocks_for(ndof, 256, ctx().num_sms * 8), 256, 0, stream()>>>(ndof, ab.dev(), af.dev());
   DFM2G_LAUNCH_CHECK();
   return ab.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned *elem, const double *emat,
-                    int mem) {
+                    int mem) try {
   DFM2G_TRY(check_bsr(m));
   if (nelem == 0) return DFM2G_OK;
   if (!elem || !emat || nnoel == 0) return fail(DFM2G_ERR_ARG, "merge: null argument");
@@ -617,6 +643,8 @@ int dfm2g_bsr_merge(dfm2g_bsr m, unsigned nelem, unsigned nnoel, const unsigned 
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   m->f32_valid = false;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

@@ -725,7 +725,7 @@ extern "C" {
 // order. No device work.
 int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const unsigned *col, const unsigned *dia_ind,
                           const unsigned *order, int backward, unsigned *chain_of, unsigned *nchain,
-                          unsigned *max_cross) {
+                          unsigned *max_cross) try {
   if (n && (!row_start || !col || !dia_ind || !order || !chain_of))
     return fail(DFM2G_ERR_ARG, "chain_partition: null array");
   std::vector<unsigned> co, first, len;
@@ -736,6 +736,8 @@ int dfm2g_chain_partition(unsigned n, const unsigned *row_start, const unsigned 
   if (nchain) *nchain = (unsigned)first.size();
   if (max_cross) *max_cross = m;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

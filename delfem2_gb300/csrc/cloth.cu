@@ -629,7 +629,7 @@ using namespace dfm2g;
 extern "C" {
 
 int dfm2g_cloth_create(dfm2g_cloth *out, dfm2g_bsr m, const double *xyz0, size_t np, const unsigned *tri,
-                       size_t ntri, const unsigned *quad, size_t nquad) {
+                       size_t ntri, const unsigned *quad, size_t nquad) try {
   if (!out) return fail(DFM2G_ERR_ARG, "cloth_create: null out");
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "cloth_create: matrix has no pattern");
   DFM2G_TRY(require_3x3(m, "cloth_create"));
@@ -686,25 +686,31 @@ int dfm2g_cloth_create(dfm2g_cloth *out, dfm2g_bsr m, const double *xyz0, size_t
   }
   *out = c;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_cloth_destroy(dfm2g_cloth c) {
+int dfm2g_cloth_destroy(dfm2g_cloth c) try {
   if (c) {
     cudaStreamSynchronize(stream());
     delete c;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_cloth_info(dfm2g_cloth c, unsigned *ncolor_tri, unsigned *ncolor_quad) {
+int dfm2g_cloth_info(dfm2g_cloth c, unsigned *ncolor_tri, unsigned *ncolor_quad) try {
   if (!c) return fail(DFM2G_ERR_ARG, "null cloth");
   if (ncolor_tri) *ncolor_tri = c->tri_color_start.empty() ? 0 : (unsigned)c->tri_color_start.size() - 1;
   if (ncolor_quad) *ncolor_quad = c->quad_color_start.empty() ? 0 : (unsigned)c->quad_color_start.size() - 1;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_cloth_merge(dfm2g_cloth c, dfm2g_bsr m, const double *xyz, const double *young_tri, double nu,
-                      double stiff_bend, double *dW, double *W, int mem) {
+                      double stiff_bend, double *dW, double *W, int mem) try {
   DFM2G_TRY(check_cloth(c, m));
   if (!xyz || !dW || (c->ntri && !young_tri)) return fail(DFM2G_ERR_ARG, "cloth_merge: null argument");
   VecArg<double> ax, ay, ad;
@@ -727,6 +733,8 @@ int dfm2g_cloth_merge(dfm2g_cloth c, dfm2g_bsr m, const double *xyz, const doubl
     DFM2G_CUDA(cudaStreamSynchronize(stream()));
   }
   return ad.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 static int step_args(dfm2g_cloth c, const int *bc, const double *young, double nu, double stiff, const double *g,
@@ -751,7 +759,7 @@ static int step_args(dfm2g_cloth c, const int *bc, const double *young, double n
 
 int dfm2g_cloth_step(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xyz, double *uvw, const int *bc,
                      const double *young_tri, double nu, double stiff_bend, const double *g, double mass, double dt,
-                     double tol, unsigned max_iter, int solver, dfm2g_solve_stats *stats, int mem) {
+                     double tol, unsigned max_iter, int solver, dfm2g_solve_stats *stats, int mem) try {
   DFM2G_TRY(check_cloth(c, m));
   if (!p) return fail(DFM2G_ERR_ARG, "cloth_step: null preconditioner");
   if (!xyz || !uvw || !bc || (c->ntri && !young_tri)) return fail(DFM2G_ERR_ARG, "cloth_step: null argument");
@@ -768,11 +776,13 @@ int dfm2g_cloth_step(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xyz, doubl
   DFM2G_TRY(cloth_step_dev(c, m, p, ax.dev(), av.dev(), a, stats));
   DFM2G_TRY(ax.copy_back());
   return av.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_cloth_adjoint_terms(dfm2g_cloth c, const double *xyz, const double *young_tri, double nu,
                               double stiff_bend, const double *mu, const double *dx, double *xbar, double *Ebar,
-                              int mem) {
+                              int mem) try {
   if (!c) return fail(DFM2G_ERR_ARG, "null cloth");
   if (!xyz || !mu || !dx || !xbar || !Ebar || (c->ntri && !young_tri))
     return fail(DFM2G_ERR_ARG, "cloth_adjoint_terms: null argument");
@@ -787,12 +797,14 @@ int dfm2g_cloth_adjoint_terms(dfm2g_cloth c, const double *xyz, const double *yo
   DFM2G_TRY(adjoint_terms(c, ax.dev(), ay.dev(), nu, stiff_bend, am.dev(), ad.dev(), axb.dev(), aeb.dev()));
   DFM2G_TRY(axb.copy_back());
   return aeb.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_cloth_rollout(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xyz, double *uvw, const int *bc,
                         const double *young_tri, double nu, double stiff_bend, const double *g, double mass,
                         double dt, double tol, unsigned max_iter, int solver, unsigned nsteps, unsigned ckpt_every,
-                        dfm2g_solve_stats *stats, int mem) {
+                        dfm2g_solve_stats *stats, int mem) try {
   DFM2G_TRY(check_cloth(c, m));
   if (!p) return fail(DFM2G_ERR_ARG, "cloth_rollout: null preconditioner");
   if (!xyz || !uvw || !bc || (c->ntri && !young_tri)) return fail(DFM2G_ERR_ARG, "cloth_rollout: null argument");
@@ -836,10 +848,12 @@ int dfm2g_cloth_rollout(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xyz, do
   }
   DFM2G_TRY(ax.copy_back());
   return av.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_cloth_rollout_adjoint(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double *xbar, double *vbar, double *dLdE,
-                                dfm2g_solve_stats *stats, int mem) {
+                                dfm2g_solve_stats *stats, int mem) try {
   DFM2G_TRY(check_cloth(c, m));
   if (!p) return fail(DFM2G_ERR_ARG, "cloth_rollout_adjoint: null preconditioner");
   if (!xbar || !vbar || (c->ntri && !dLdE)) return fail(DFM2G_ERR_ARG, "cloth_rollout_adjoint: null argument");
@@ -893,6 +907,8 @@ int dfm2g_cloth_rollout_adjoint(dfm2g_cloth c, dfm2g_bsr m, dfm2g_ilu p, double 
   DFM2G_TRY(axb.copy_back());
   DFM2G_TRY(avb.copy_back());
   return ae.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

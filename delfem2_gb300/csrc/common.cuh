@@ -16,6 +16,9 @@ namespace dfm2g {
 // ---- errors ----------------------------------------------------------------
 void set_error(const char *fmt, ...);
 int fail(int status, const char *fmt, ...);
+// From a catch block of an entry point: records what was thrown and returns
+// DFM2G_ERR_HOST (no exception crosses the C ABI).
+int host_failure() noexcept;
 
 #define DFM2G_CUDA(call)                                                              \
   do {                                                                                \

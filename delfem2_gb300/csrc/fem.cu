@@ -330,7 +330,7 @@ using namespace dfm2g;
 extern "C" {
 
 int dfm2g_tetmesh_create(dfm2g_tetmesh *out, dfm2g_bsr m, const double *xyz, size_t np, const unsigned *tet,
-                         size_t ntet) {
+                         size_t ntet) try {
   if (!out) return fail(DFM2G_ERR_ARG, "tetmesh_create: null out");
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "tetmesh_create: matrix has no pattern");
   if (m->ndim == 2) return fail(DFM2G_ERR_UNSUPPORTED, "tetmesh_create: 2x2 blocks (tets take 1x1 or 3x3)");
@@ -365,25 +365,31 @@ int dfm2g_tetmesh_create(dfm2g_tetmesh *out, dfm2g_bsr m, const double *xyz, siz
   }
   *out = t;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_tetmesh_destroy(dfm2g_tetmesh t) {
+int dfm2g_tetmesh_destroy(dfm2g_tetmesh t) try {
   if (t) {
     cudaStreamSynchronize(stream());
     delete t;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_tetmesh_info(dfm2g_tetmesh t, unsigned *ncolor, size_t *ntet) {
+int dfm2g_tetmesh_info(dfm2g_tetmesh t, unsigned *ncolor, size_t *ntet) try {
   if (!t) return fail(DFM2G_ERR_ARG, "null tetmesh");
   if (ncolor) *ncolor = t->color_start.empty() ? 0 : (unsigned)t->color_start.size() - 1;
   if (ntet) *ntet = t->ntet;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const double *young, double nu, double rho,
-                                  const double *g, const double *disp, double *b, int mem) {
+                                  const double *g, const double *disp, double *b, int mem) try {
   if (!t || !m) return fail(DFM2G_ERR_ARG, "assemble: null handle");
   if (m != t->bsr || m->pattern_version != t->pattern_version)
     return fail(DFM2G_ERR_STATE, "assemble: matrix pattern differs from the one the mesh was mapped to");
@@ -402,10 +408,12 @@ int dfm2g_tetmesh_assemble_linear(dfm2g_tetmesh t, dfm2g_bsr m, const double *yo
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return ab.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_tetmesh_assemble_poisson(dfm2g_tetmesh t, dfm2g_bsr m, double alpha, double source, const double *val,
-                                   double *b, int mem) {
+                                   double *b, int mem) try {
   if (!t || !m) return fail(DFM2G_ERR_ARG, "assemble_poisson: null handle");
   if (m != t->bsr || m->pattern_version != t->pattern_version)
     return fail(DFM2G_ERR_STATE, "assemble_poisson: matrix pattern differs from the one the mesh was mapped to");
@@ -424,6 +432,8 @@ int dfm2g_tetmesh_assemble_poisson(dfm2g_tetmesh t, dfm2g_bsr m, double alpha, d
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return ab.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 static int tet_dynamic(dfm2g_tetmesh t, dfm2g_bsr m, int mode, double myu, double lambda, double rho,
@@ -464,21 +474,25 @@ static int tet_dynamic(dfm2g_tetmesh t, dfm2g_bsr m, int mode, double myu, doubl
 
 int dfm2g_tetmesh_assemble_beuler(dfm2g_tetmesh t, dfm2g_bsr m, double myu, double lambda, double rho,
                                   const double *g, double dt, const double *disp, const double *velo,
-                                  const double *rot, double *b, int mem) {
+                                  const double *rot, double *b, int mem) try {
   return tet_dynamic(t, m, rot ? kWarp : kBEuler, myu, lambda, rho, g, dt, 0.0, disp, velo, rot, b, mem,
                      "tetmesh_assemble_beuler");
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_tetmesh_assemble_newmark(dfm2g_tetmesh t, dfm2g_bsr m, double myu, double lambda, double rho,
                                    const double *g, double dt, double gamma, double beta, const double *disp,
-                                   const double *velo, const double *acc, double *b, int mem) {
+                                   const double *velo, const double *acc, double *b, int mem) try {
   (void)gamma;  // unused by the reference's first-iteration element matrix as well
   return tet_dynamic(t, m, kNewmark, myu, lambda, rho, g, dt, beta, disp, velo, acc, b, mem,
                      "tetmesh_assemble_newmark");
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu, const double *u, const double *lam,
-                       double *dLdE, int mem) {
+                       double *dLdE, int mem) try {
   if (!t) return fail(DFM2G_ERR_ARG, "dLdE: null handle");
   (void)young;
   if (!u || !lam || !dLdE) return fail(DFM2G_ERR_ARG, "dLdE: null argument");
@@ -491,6 +505,8 @@ int dfm2g_tetmesh_dLdE(dfm2g_tetmesh t, const double *young, double nu, const do
                                                                                   au.dev(), al.dev(), ao.dev());
   DFM2G_LAUNCH_CHECK();
   return ao.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

@@ -147,7 +147,7 @@ static int check_mesh2(dfm2g_trimesh2 t, dfm2g_bsr m, unsigned ndim, const char 
 extern "C" {
 
 int dfm2g_trimesh2_create(dfm2g_trimesh2 *out, dfm2g_bsr m, const double *xy, size_t np, const unsigned *tri,
-                          size_t ntri) {
+                          size_t ntri) try {
   if (!out) return fail(DFM2G_ERR_ARG, "trimesh2_create: null out");
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "trimesh2_create: matrix has no pattern");
   if (m->ndim == 3) return fail(DFM2G_ERR_UNSUPPORTED, "trimesh2_create: 3x3 blocks (2-D triangles take 1x1 or 2x2)");
@@ -181,18 +181,22 @@ int dfm2g_trimesh2_create(dfm2g_trimesh2 *out, dfm2g_bsr m, const double *xy, si
   }
   *out = t;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_trimesh2_destroy(dfm2g_trimesh2 t) {
+int dfm2g_trimesh2_destroy(dfm2g_trimesh2 t) try {
   if (t) {
     cudaStreamSynchronize(stream());
     delete t;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_trimesh2_assemble_poisson(dfm2g_trimesh2 t, dfm2g_bsr m, double alpha, double source, const double *val,
-                                    double *b, int mem) {
+                                    double *b, int mem) try {
   DFM2G_TRY(check_mesh2(t, m, 1, "trimesh2_assemble_poisson"));
   if (!b) return fail(DFM2G_ERR_ARG, "trimesh2_assemble_poisson: null b");
   VecArg<double> av, ab;
@@ -208,10 +212,12 @@ int dfm2g_trimesh2_assemble_poisson(dfm2g_trimesh2 t, dfm2g_bsr m, double alpha,
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return ab.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_trimesh2_assemble_solid_linear(dfm2g_trimesh2 t, dfm2g_bsr m, double myu, double lambda, double rho,
-                                         double gx, double gy, const double *disp, double *b, int mem) {
+                                         double gx, double gy, const double *disp, double *b, int mem) try {
   DFM2G_TRY(check_mesh2(t, m, 2, "trimesh2_assemble_solid_linear"));
   if (!b) return fail(DFM2G_ERR_ARG, "trimesh2_assemble_solid_linear: null b");
   VecArg<double> ad, ab;
@@ -227,6 +233,8 @@ int dfm2g_trimesh2_assemble_solid_linear(dfm2g_trimesh2 t, dfm2g_bsr m, double m
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return ab.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

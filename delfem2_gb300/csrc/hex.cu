@@ -156,7 +156,7 @@ using namespace dfm2g;
 extern "C" {
 
 int dfm2g_hexmesh_create(dfm2g_hexmesh *out, dfm2g_bsr m, const double *xyz, size_t np, const unsigned *hex,
-                         size_t nhex) {
+                         size_t nhex) try {
   if (!out) return fail(DFM2G_ERR_ARG, "hexmesh_create: null out");
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "hexmesh_create: matrix has no pattern");
   DFM2G_TRY(require_3x3(m, "hexmesh_create"));
@@ -195,18 +195,22 @@ int dfm2g_hexmesh_create(dfm2g_hexmesh *out, dfm2g_bsr m, const double *xyz, siz
   }
   *out = t;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_hexmesh_destroy(dfm2g_hexmesh t) {
+int dfm2g_hexmesh_destroy(dfm2g_hexmesh t) try {
   if (t) {
     cudaStreamSynchronize(stream());
     delete t;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_hexmesh_assemble_linear(dfm2g_hexmesh t, dfm2g_bsr m, double myu, double lambda, double rho,
-                                  const double *g, const double *disp, double *b, int mem) {
+                                  const double *g, const double *disp, double *b, int mem) try {
   if (!t || !m) return fail(DFM2G_ERR_ARG, "hexmesh_assemble_linear: null handle");
   if (m != t->bsr || m->pattern_version != t->pattern_version)
     return fail(DFM2G_ERR_STATE, "hexmesh_assemble_linear: matrix pattern differs from the one the mesh was mapped to");
@@ -225,6 +229,8 @@ int dfm2g_hexmesh_assemble_linear(dfm2g_hexmesh t, dfm2g_bsr m, double myu, doub
   DFM2G_LAUNCH_CHECK();
   m->f32_valid = false;
   return ab.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

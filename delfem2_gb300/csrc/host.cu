@@ -4,7 +4,9 @@
 #include <cstdarg>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <numeric>
+#include <stdexcept>
 
 #include "common.cuh"
 
@@ -29,6 +31,24 @@ int fail(int status, const char *fmt, ...) {
   va_end(ap);
   g_last_error = buf;
   return status;
+}
+
+int host_failure() noexcept {
+  char buf[256];
+  try {
+    throw;
+  } catch (const std::bad_alloc &) {
+    snprintf(buf, sizeof buf, "host-side failure: out of host memory");
+  } catch (const std::exception &e) {
+    snprintf(buf, sizeof buf, "host-side failure: %s", e.what());
+  } catch (...) {
+    snprintf(buf, sizeof buf, "host-side failure: unknown exception");
+  }
+  try {
+    g_last_error = buf;
+  } catch (...) {  // no memory left for the message either
+  }
+  return DFM2G_ERR_HOST;
 }
 
 static Context g_ctx;
@@ -121,40 +141,50 @@ extern "C" {
 
 int dfm2g_version(void) { return 100; }
 
-int dfm2g_profile_enable(int on) {
+int dfm2g_profile_enable(int on) try {
   DFM2G_TRY(ensure_context());
   drain_prof();
   g_prof_on = on != 0;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_profile_reset(void) {
+int dfm2g_profile_reset(void) try {
   drain_prof();
   for (int k = 0; k < DFM2G_PROF_NKIND; ++k) {
     g_prof_count[k] = 0;
     g_prof_ms[k] = 0.0;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_profile_read(int kind, unsigned *launches, double *total_ms) {
+int dfm2g_profile_read(int kind, unsigned *launches, double *total_ms) try {
   if (kind < 0 || kind >= DFM2G_PROF_NKIND) return fail(DFM2G_ERR_ARG, "unknown profile kind %d", kind);
   drain_prof();
   if (launches) *launches = g_prof_count[kind];
   if (total_ms) *total_ms = g_prof_ms[kind];
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_launch_count(unsigned long long *count) {
+int dfm2g_launch_count(unsigned long long *count) try {
   if (!count) return fail(DFM2G_ERR_ARG, "null count");
   *count = g_launches.load();
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_alloc_count(unsigned long long *count) {
+int dfm2g_alloc_count(unsigned long long *count) try {
   if (!count) return fail(DFM2G_ERR_ARG, "null count");
   *count = g_allocs.load();
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 const char *dfm2g_status_string(int s) {
@@ -170,30 +200,35 @@ const char *dfm2g_status_string(int s) {
     case DFM2G_ERR_UNSUPPORTED: return "unsupported block size or mode";
     case DFM2G_ERR_STATE: return "call order violated";
     case DFM2G_ERR_NONFINITE: return "non-finite value in a solve";
+    case DFM2G_ERR_HOST: return "host-side failure (host memory or thread)";
     default: return "unknown status";
   }
 }
 
 const char *dfm2g_last_error(void) { return g_last_error.c_str(); }
 
-int dfm2g_set_stream(void *s) {
+int dfm2g_set_stream(void *s) try {
   DFM2G_TRY(ensure_context());
   // NULL is CUDA's legacy default stream (torch's default stream), not the
   // library's own non-blocking stream: work must order with the caller's.
   g_ctx.stream = static_cast<cudaStream_t>(s);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_synchronize(void) {
+int dfm2g_synchronize(void) try {
   DFM2G_TRY(ensure_context());
   DFM2G_CUDA(cudaStreamSynchronize(g_ctx.stream));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 // Lattice node (ix,iy,iz) -> ix*(ny+1)*(nz+1) + iy*(nz+1) + iz; six tets per
 // voxel around the corner-0 / corner-6 diagonal (gridvoxel.cpp:194-271).
 int dfm2g_mesh_tet_voxel_grid(unsigned nx, unsigned ny, unsigned nz, double scale, double *xyz,
-                              unsigned *tet) {
+                              unsigned *tet) try {
   if (!xyz || !tet) return fail(DFM2G_ERR_ARG, "mesh: null output");
   const size_t my = ny + 1, mz = nz + 1;
   size_t p = 0;
@@ -219,6 +254,8 @@ int dfm2g_mesh_tet_voxel_grid(unsigned nx, unsigned ny, unsigned nz, double scal
           for (int k = 0; k < 4; ++k) tet[t * 4 + k] = c[six[s][k]];
       }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 // Elements-around-point then a marker sweep (self marked first, so excluded).
@@ -267,18 +304,22 @@ static int psup_impl(const unsigned *elem, size_t nelem, unsigned nnoel, size_t 
 }
 
 int dfm2g_psup_count(const unsigned *elem, size_t nelem, unsigned nnoel, size_t np,
-                     unsigned *psup_ind, size_t *npsup) {
+                     unsigned *psup_ind, size_t *npsup) try {
   if (!elem || !psup_ind || !npsup || nnoel == 0) return fail(DFM2G_ERR_ARG, "psup_count: null argument");
   DFM2G_TRY(psup_impl(elem, nelem, nnoel, np, psup_ind, nullptr));
   *npsup = psup_ind[np];
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_psup_fill(const unsigned *elem, size_t nelem, unsigned nnoel, size_t np,
-                    const unsigned *psup_ind, unsigned *psup) {
+                    const unsigned *psup_ind, unsigned *psup) try {
   if (!elem || !psup_ind || nnoel == 0) return fail(DFM2G_ERR_ARG, "psup_fill: null argument");
   if (psup_ind[np] > 0 && !psup) return fail(DFM2G_ERR_ARG, "psup_fill: null psup");
   return psup_impl(elem, nelem, nnoel, np, const_cast<unsigned *>(psup_ind), psup);
+} catch (...) {
+  return host_failure();
 }
 
 // A kernel that waits for a value nobody writes: the wait must give up after
@@ -305,7 +346,7 @@ __global__ void k_grid_barrier_probe(unsigned *bar, int *err, int *status, unsig
   if (threadIdx.x == 0 && !ok) atomicExch(status, DFM2G_ERR_WAIT_TIMEOUT);
 }
 
-int dfm2g_debug_wait_timeout(unsigned timeout_ms) {
+int dfm2g_debug_wait_timeout(unsigned timeout_ms) try {
   DFM2G_TRY(ensure_context());
   if (timeout_ms == 0 || timeout_ms > 5000) return fail(DFM2G_ERR_ARG, "timeout_ms must be in [1, 5000]");
   DevBuf<double> never;
@@ -321,9 +362,11 @@ int dfm2g_debug_wait_timeout(unsigned timeout_ms) {
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   if (h == DFM2G_ERR_WAIT_TIMEOUT) return fail(DFM2G_ERR_WAIT_TIMEOUT, "debug wait timed out after %u ms", timeout_ms);
   return h;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_debug_grid_barrier(unsigned timeout_ms, int one_block_absent) {
+int dfm2g_debug_grid_barrier(unsigned timeout_ms, int one_block_absent) try {
   DFM2G_TRY(ensure_context());
   if (timeout_ms == 0 || timeout_ms > 5000) return fail(DFM2G_ERR_ARG, "timeout_ms must be in [1, 5000]");
   DevBuf<unsigned> bar;
@@ -349,6 +392,16 @@ int dfm2g_debug_grid_barrier(unsigned timeout_ms, int one_block_absent) {
     return fail(DFM2G_ERR_WAIT_TIMEOUT, "debug grid barrier timed out after %u ms", timeout_ms);
   if (h != DFM2G_OK || e != DFM2G_OK) return fail(DFM2G_ERR_STATE, "debug grid barrier: status %d, error word %d", h, e);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
+}
+
+int dfm2g_debug_host_failure(int kind) try {
+  if (kind == 0) throw std::bad_alloc();
+  if (kind == 1) throw std::runtime_error("debug exception");
+  throw kind;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

@@ -1109,7 +1109,7 @@ static int check_ilu(dfm2g_ilu p, bool pattern, bool factor) {
 
 extern "C" {
 
-int dfm2g_ilu_create(dfm2g_ilu *out) {
+int dfm2g_ilu_create(dfm2g_ilu *out) try {
   if (!out) return fail(DFM2G_ERR_ARG, "ilu_create: null out");
   DFM2G_TRY(ensure_context());
   auto *p = new dfm2g_ilu_s();
@@ -1118,32 +1118,40 @@ int dfm2g_ilu_create(dfm2g_ilu *out) {
   DFM2G_CUDA(cudaMemsetAsync(p->err.p, 0, sizeof(int), stream()));
   *out = p;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_destroy(dfm2g_ilu p) {
+int dfm2g_ilu_destroy(dfm2g_ilu p) try {
   if (p) {
     cudaStreamSynchronize(stream());
     delete p;
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) {
+int dfm2g_ilu_set_pattern0(dfm2g_ilu p, dfm2g_bsr m) try {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "set_pattern0: matrix has no pattern");
   return ilu_install_pattern(p, m->nblk, m->ndim, m->nnz, m->row_start.p, m->col.p, cudaMemcpyDeviceToDevice);
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level) {
+int dfm2g_ilu_set_pattern_k(dfm2g_ilu p, dfm2g_bsr m, int fill_level) try {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!m || !m->has_pattern) return fail(DFM2G_ERR_STATE, "set_pattern_k: matrix has no pattern");
   if (fill_level == 0) return dfm2g_ilu_set_pattern0(p, m);
   std::vector<unsigned> rs, col;
   DFM2G_TRY(ilu_symbolic_k(m->nblk, m->h_row_start, m->h_col, fill_level, rs, col));
   return ilu_install_pattern(p, m->nblk, m->ndim, col.size(), rs.data(), col.data(), cudaMemcpyHostToDevice);
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m) {
+int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m) try {
   DFM2G_TRY(check_ilu(p, true, false));
   if (!m || !m->has_pattern || m->nblk != p->nblk) return fail(DFM2G_ERR_ARG, "copy_value: matrix size mismatch");
   if (m->ndim != p->ndim)
@@ -1169,9 +1177,11 @@ int dfm2g_ilu_copy_value(dfm2g_ilu p, dfm2g_bsr m) {
   p->has_factor = false;
   p->f32_valid = false;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular) {
+int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular) try {
   DFM2G_TRY(check_ilu(p, true, false));
   DFM2G_CUDA(cudaMemsetAsync(p->nsing.p, 0, sizeof(int), stream()));
   const std::vector<unsigned> &ls = p->h_lstart_f;
@@ -1198,6 +1208,8 @@ int dfm2g_ilu_decompose(dfm2g_ilu p, int *n_singular) {
   p->factor_version++;
   if (ns > 10) return fail(DFM2G_ERR_SINGULAR_PIVOT, "ILU: %d pivots with |det| <= 1e-30", ns);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 static int precond_host(dfm2g_ilu p, int prec, void *vec, int mem, int which /*1 fwd, 2 bwd, 3 both*/) {
@@ -1266,7 +1278,7 @@ static int noalloc_scratch(void **out) {
   return DFM2G_OK;
 }
 
-int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec) {
+int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec) try {
   DFM2G_TRY(check_ilu(p, true, true));
   if (!vec) return fail(DFM2G_ERR_ARG, "solve_precond_noalloc: null vector");
   if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "prec must be F64 or F32");
@@ -1290,13 +1302,27 @@ int dfm2g_ilu_solve_precond_noalloc(dfm2g_ilu p, int prec, void *vec) {
   DFM2G_TRY(ilu_sweep_noalloc(p, prec, true, vec, scratch));
   DFM2G_TRY(ilu_sweep_noalloc(p, prec, false, scratch, vec));
   return read_err(p);
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_forward(dfm2g_ilu p, int prec, void *vec, int mem) { return precond_host(p, prec, vec, mem, 1); }
-int dfm2g_ilu_backward(dfm2g_ilu p, int prec, void *vec, int mem) { return precond_host(p, prec, vec, mem, 2); }
-int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) { return precond_host(p, prec, vec, mem, 3); }
+int dfm2g_ilu_forward(dfm2g_ilu p, int prec, void *vec, int mem) try {
+  return precond_host(p, prec, vec, mem, 1);
+} catch (...) {
+  return host_failure();
+}
+int dfm2g_ilu_backward(dfm2g_ilu p, int prec, void *vec, int mem) try {
+  return precond_host(p, prec, vec, mem, 2);
+} catch (...) {
+  return host_failure();
+}
+int dfm2g_ilu_solve_precond(dfm2g_ilu p, int prec, void *vec, int mem) try {
+  return precond_host(p, prec, vec, mem, 3);
+} catch (...) {
+  return host_failure();
+}
 
-int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
+int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) try {
   DFM2G_TRY(check_ilu(p, false, false));
   if (mode != DFM2G_SWEEP_SYNCFREE && mode != DFM2G_SWEEP_LEVELS && mode != DFM2G_SWEEP_GROUPS &&
       mode != DFM2G_SWEEP_BLOCK && mode != DFM2G_SWEEP_PARTS && mode != DFM2G_SWEEP_CHAINS &&
@@ -1311,49 +1337,61 @@ int dfm2g_ilu_set_sweep_mode(dfm2g_ilu p, int mode) {
     return fail(DFM2G_ERR_UNSUPPORTED, "blob schedule unavailable for this pattern");
   p->sweep_mode = mode;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode) {
+int dfm2g_ilu_get_sweep_mode(dfm2g_ilu p, int *mode) try {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!mode) return fail(DFM2G_ERR_ARG, "get_sweep_mode: null out");
   *mode = p->sweep_mode;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_last_schedule(dfm2g_ilu p, int prec, int backward, int *mode) {
+int dfm2g_ilu_last_schedule(dfm2g_ilu p, int prec, int backward, int *mode) try {
   DFM2G_TRY(check_ilu(p, false, false));
   if (!mode) return fail(DFM2G_ERR_ARG, "last_schedule: null out");
   if (prec != DFM2G_F64 && prec != DFM2G_F32) return fail(DFM2G_ERR_ARG, "last_schedule: bad precision");
   *mode = p->last_sched[prec == DFM2G_F64 ? 1 : 0][backward ? 1 : 0];
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_info(dfm2g_ilu p, unsigned *nblk, size_t *nnz) {
+int dfm2g_ilu_info(dfm2g_ilu p, unsigned *nblk, size_t *nnz) try {
   DFM2G_TRY(check_ilu(p, true, false));
   if (nblk) *nblk = p->nblk;
   if (nnz) *nnz = p->nnz;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_get_row_start(dfm2g_ilu p, unsigned *row_start) {
+int dfm2g_ilu_get_row_start(dfm2g_ilu p, unsigned *row_start) try {
   DFM2G_TRY(check_ilu(p, true, false));
   if (!row_start) return fail(DFM2G_ERR_ARG, "get_row_start: null out");
   DFM2G_CUDA(cudaMemcpyAsync(row_start, p->row_start.p, sizeof(unsigned) * (p->nblk + 1), cudaMemcpyDeviceToHost,
                              stream()));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_ind) {
+int dfm2g_ilu_get_pattern(dfm2g_ilu p, unsigned *col, unsigned *dia_ind) try {
   DFM2G_TRY(check_ilu(p, true, false));
   if (col && p->nnz) DFM2G_CUDA(cudaMemcpyAsync(col, p->col.p, sizeof(unsigned) * p->nnz, cudaMemcpyDeviceToHost, stream()));
   if (dia_ind && p->nblk)
     DFM2G_CUDA(cudaMemcpyAsync(dia_ind, p->dia_ind.p, sizeof(unsigned) * p->nblk, cudaMemcpyDeviceToHost, stream()));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem) {
+int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem) try {
   DFM2G_TRY(check_ilu(p, true, false));
   const cudaMemcpyKind k = mem == DFM2G_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   const size_t bb = (size_t)p->ndim * p->ndim;
@@ -1361,10 +1399,12 @@ int dfm2g_ilu_get_values(dfm2g_ilu p, double *vcrs, double *vdia, int mem) {
   if (vdia && p->nblk) DFM2G_CUDA(cudaMemcpyAsync(vdia, p->vdia.p, sizeof(double) * bb * p->nblk, k, stream()));
   DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, unsigned *order, unsigned *level_start,
-                         unsigned *nlevels) {
+                         unsigned *nlevels) try {
   DFM2G_TRY(check_ilu(p, true, false));
   const unsigned n = p->nblk;
   const unsigned nlev = backward ? p->nlev_b : p->nlev_f;
@@ -1381,6 +1421,8 @@ int dfm2g_ilu_get_levels(dfm2g_ilu p, int backward, unsigned *level, unsigned *o
   }
   if (nlevels) *nlevels = nlev;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

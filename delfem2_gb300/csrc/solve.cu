@@ -886,7 +886,7 @@ using namespace dfm2g;
 extern "C" {
 
 int dfm2g_solve_pcg(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol, unsigned max_iter, double *hist,
-                    unsigned hist_cap, unsigned *n_hist, int mem, dfm2g_solve_stats *stats) {
+                    unsigned hist_cap, unsigned *n_hist, int mem, dfm2g_solve_stats *stats) try {
   DFM2G_TRY(check_pair(m, p));
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg: null preconditioner");
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_pcg: null vector");
@@ -922,10 +922,12 @@ int dfm2g_solve_pcg(dfm2g_bsr m, dfm2g_ilu p, double *r, double *x, double tol, 
   if (hs.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_pcg: non-finite residual");
   if (hs.done == 2) return fail(DFM2G_ERR_NOT_CONVERGED, "solve_pcg: %u iterations without reaching tol", max_iter);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_iter, double *hist, unsigned hist_cap,
-                   unsigned *n_hist, int mem, dfm2g_solve_stats *stats) {
+                   unsigned *n_hist, int mem, dfm2g_solve_stats *stats) try {
   DFM2G_TRY(check_pair(m, nullptr));
   if (!r || !x) return fail(DFM2G_ERR_ARG, "solve_cg: null vector");
   const size_t n = (size_t)m->nblk * m->ndim;
@@ -964,10 +966,12 @@ int dfm2g_solve_cg(dfm2g_bsr m, double *r, double *x, double tol, unsigned max_i
   if (hs.done == 4) return fail(DFM2G_ERR_NONFINITE, "solve_cg: non-finite residual");
   if (hs.done == 2) return fail(DFM2G_ERR_NOT_CONVERGED, "solve_cg: %u iterations without reaching tol", max_iter);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, double tol, double delta,
-                                   unsigned max_iter, int mem, dfm2g_solve_stats *stats) {
+                                   unsigned max_iter, int mem, dfm2g_solve_stats *stats) try {
   DFM2G_TRY(check_pair(m, p));
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null preconditioner");
   if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed_reliable: null vector");
@@ -1017,10 +1021,12 @@ int dfm2g_solve_pcg_mixed_reliable(dfm2g_bsr m, dfm2g_ilu p, const double *b, do
     return fail(DFM2G_ERR_NOT_CONVERGED, "solve_pcg_mixed_reliable: stopped at relative residual %.3e",
                 hs.rtrue / bnorm);
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, double tol, double inner_tol,
-                          unsigned max_iter, unsigned max_outer, int mem, dfm2g_solve_stats *stats) {
+                          unsigned max_iter, unsigned max_outer, int mem, dfm2g_solve_stats *stats) try {
   DFM2G_TRY(check_pair(m, p));
   if (!p) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null preconditioner");
   if (!b || !x) return fail(DFM2G_ERR_ARG, "solve_pcg_mixed: null vector");
@@ -1092,6 +1098,8 @@ int dfm2g_solve_pcg_mixed(dfm2g_bsr m, dfm2g_ilu p, const double *b, double *x, 
     stats->rel_residual = rel;
   }
   return status;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"
@@ -1119,7 +1127,7 @@ int vec_ws() {
 
 extern "C" {
 
-int dfm2g_dev_alloc(void **p, size_t bytes) {
+int dfm2g_dev_alloc(void **p, size_t bytes) try {
   if (!p) return fail(DFM2G_ERR_ARG, "dev_alloc: null out");
   DFM2G_TRY(ensure_context());
   *p = nullptr;
@@ -1127,17 +1135,21 @@ int dfm2g_dev_alloc(void **p, size_t bytes) {
   note_alloc();
   DFM2G_CUDA(cudaMalloc(p, bytes));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_dev_free(void *p) {
+int dfm2g_dev_free(void *p) try {
   if (p) {
     cudaStreamSynchronize(stream());
     DFM2G_CUDA(cudaFree(p));
   }
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_dev_copy(void *dst, const void *src, size_t bytes, int kind) {
+int dfm2g_dev_copy(void *dst, const void *src, size_t bytes, int kind) try {
   if ((!dst || !src) && bytes) return fail(DFM2G_ERR_ARG, "dev_copy: null pointer");
   DFM2G_TRY(ensure_context());
   cudaMemcpyKind k;
@@ -1150,18 +1162,22 @@ int dfm2g_dev_copy(void *dst, const void *src, size_t bytes, int kind) {
   if (bytes) DFM2G_CUDA(cudaMemcpyAsync(dst, src, bytes, k, stream()));
   if (kind != DFM2G_COPY_D2D) DFM2G_CUDA(cudaStreamSynchronize(stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_vec_dot(const double *x, const double *y, size_t n, double *out, int mem) {
+int dfm2g_vec_dot(const double *x, const double *y, size_t n, double *out, int mem) try {
   if (!x || !y || !out) return fail(DFM2G_ERR_ARG, "vec_dot: null argument");
   DFM2G_TRY(vec_ws());
   VecArg<double> ax, ay;
   DFM2G_TRY(ax.in(x, n, mem, true));
   DFM2G_TRY(ay.in(y, n, mem, true));
   return dot_host(n, ax.dev(), ay.dev(), DFM2G_F64, out);
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_vec_axpy(double *y, double alpha, const double *x, size_t n, int mem) {
+int dfm2g_vec_axpy(double *y, double alpha, const double *x, size_t n, int mem) try {
   if (!x || !y) return fail(DFM2G_ERR_ARG, "vec_axpy: null argument");
   DFM2G_TRY(ensure_context());
   VecArg<double> ax, ay;
@@ -1171,9 +1187,11 @@ int dfm2g_vec_axpy(double *y, double alpha, const double *x, size_t n, int mem) 
   note_launches(1);
   DFM2G_LAUNCH_CHECK();
   return ay.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_vec_scale_add(double *y, double beta, const double *x, size_t n, int mem) {
+int dfm2g_vec_scale_add(double *y, double beta, const double *x, size_t n, int mem) try {
   if (!x || !y) return fail(DFM2G_ERR_ARG, "vec_scale_add: null argument");
   DFM2G_TRY(ensure_context());
   VecArg<double> ax, ay;
@@ -1183,9 +1201,11 @@ int dfm2g_vec_scale_add(double *y, double beta, const double *x, size_t n, int m
   note_launches(1);
   DFM2G_LAUNCH_CHECK();
   return ay.copy_back();
+} catch (...) {
+  return host_failure();
 }
 
-int dfm2g_vec_set_zero(double *x, size_t n, int mem) {
+int dfm2g_vec_set_zero(double *x, size_t n, int mem) try {
   if (!x) return fail(DFM2G_ERR_ARG, "vec_set_zero: null argument");
   if (mem == DFM2G_MEM_HOST) {
     std::memset(x, 0, sizeof(double) * n);
@@ -1195,6 +1215,8 @@ int dfm2g_vec_set_zero(double *x, size_t n, int mem) {
   DFM2G_TRY(ensure_context());
   if (n) DFM2G_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, stream()));
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

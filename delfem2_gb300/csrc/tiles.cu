@@ -1113,7 +1113,7 @@ extern "C" {
 // Host-only: the tile partition the tile schedule uses. No device work.
 int dfm2g_tile_partition(unsigned n, const unsigned *row_start, const unsigned *col, const unsigned *dia_ind,
                          const unsigned *order, int backward, unsigned max_rows, unsigned max_width,
-                         unsigned *tile_of, unsigned *level, unsigned *ntiles, unsigned *max_deps) {
+                         unsigned *tile_of, unsigned *level, unsigned *ntiles, unsigned *max_deps) try {
   if (n && (!row_start || !col || !dia_ind || !order || !tile_of || !level))
     return fail(DFM2G_ERR_ARG, "tile_partition: null array");
   if (max_rows == 0 || max_width == 0) return fail(DFM2G_ERR_ARG, "tile_partition: zero tile size");
@@ -1127,6 +1127,8 @@ int dfm2g_tile_partition(unsigned n, const unsigned *row_start, const unsigned *
   if (ntiles) *ntiles = nt;
   if (max_deps) *max_deps = m;
   return DFM2G_OK;
+} catch (...) {
+  return host_failure();
 }
 
 }  // extern "C"

@@ -6,7 +6,10 @@
  *
  * Conventions
  *  - Every entry point returns an int status (DFM2G_OK == 0). A failing call
- *    leaves a message for dfm2g_last_error() (per host thread).
+ *    leaves a message for dfm2g_last_error() (per host thread). No C++
+ *    exception leaves the library: a host-side failure inside a call (out of
+ *    host memory, a host thread that could not start) returns
+ *    DFM2G_ERR_HOST.
  *  - Index arrays are uint32 ("unsigned int" in the reference). Following
  *    CMatrixSparse, `row_start` is what the reference calls col_ind_ (row
  *    offsets, nblk+1 entries) and `col` is its row_ptr_ (column id of each
@@ -47,7 +50,8 @@ enum dfm2g_status {
   DFM2G_ERR_PATTERN = 7,         /* invalid sparsity pattern               */
   DFM2G_ERR_UNSUPPORTED = 8,     /* block size or mode not supported       */
   DFM2G_ERR_STATE = 9,           /* call order violated (e.g. no pattern)  */
-  DFM2G_ERR_NONFINITE = 10       /* NaN/Inf met in a solve                 */
+  DFM2G_ERR_NONFINITE = 10,      /* NaN/Inf met in a solve                 */
+  DFM2G_ERR_HOST = 11            /* host-side failure (host memory, thread) */
 };
 
 enum dfm2g_mem { DFM2G_MEM_HOST = 0, DFM2G_MEM_DEVICE = 1 };
@@ -498,6 +502,10 @@ DFM2G_API int dfm2g_debug_wait_timeout(unsigned timeout_ms);
  * without arriving and the call must return DFM2G_ERR_WAIT_TIMEOUT after about
  * `timeout_ms`, with the context usable. */
 DFM2G_API int dfm2g_debug_grid_barrier(unsigned timeout_ms, int one_block_absent);
+/* Host only: raises a C++ exception inside the call (kind 0: out of host
+ * memory, 1: a standard exception, 2: anything else); must return
+ * DFM2G_ERR_HOST with a message for dfm2g_last_error(). */
+DFM2G_API int dfm2g_debug_host_failure(int kind);
 
 #ifdef __cplusplus
 }

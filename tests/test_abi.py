@@ -32,9 +32,19 @@ def test_library_exports_every_declared_symbol(built_lib):
 def test_status_strings(built_lib):
     from delfem2_gb300 import _native as N
     assert built_lib.dfm2g_version() >= 100
-    for s in range(0, 11):
+    for s in range(0, 12):
         assert built_lib.dfm2g_status_string(s)
     assert b"singular" in built_lib.dfm2g_status_string(N.ERR_SINGULAR_PIVOT)
+    assert b"host" in built_lib.dfm2g_status_string(N.ERR_HOST)
+
+
+@pytest.mark.parametrize("kind,msg", [(0, b"out of host memory"), (1, b"debug exception"), (2, b"unknown")])
+def test_no_exception_crosses_the_c_abi(built_lib, kind, msg):
+    """A C++ exception inside an entry point becomes DFM2G_ERR_HOST with a
+    message (every entry point is a function-try-block); no device work."""
+    from delfem2_gb300 import _native as N
+    assert built_lib.dfm2g_debug_host_failure(kind) == N.ERR_HOST
+    assert msg in built_lib.dfm2g_last_error()
 
 
 @pytest.mark.parametrize("dims", [(1, 1, 1), (3, 2, 4), (16, 16, 16)])
