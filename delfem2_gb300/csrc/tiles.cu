@@ -63,6 +63,7 @@
 //             then column c of each block, L_b[0..2][c] for b < M
 // A step's groups are consecutive in the stream, so one copy moves a step.
 #include <algorithm>
+#include <atomic>
 #include <functional>
 #include <mutex>
 #include <queue>
@@ -947,14 +948,28 @@ int tile_build(dfm2g_ilu_s *p) {
   if (need_dir[0]) DFM2G_TRY(tile_to_host(order[0], p->order_f.p, n));
   if (need_dir[1]) DFM2G_TRY(tile_to_host(order[1], p->order_b.p, n));
   TileHost h[2][2];
+  // an exception inside a worker (out of host memory) is caught there: it
+  // leaves that schedule unusable and the call reports DFM2G_ERR_HOST
+  std::atomic<bool> failed{false};
   std::vector<std::thread> workers;
-  for (int f = 0; f < 2; ++f)
-    for (int d = 0; d < 2; ++d)
-      if (need[f][d])
-        workers.emplace_back([&, f, d]() {
-          tile_host_build(n, rs, col, dia, order[d], d == 0, tile_rows(f ? 8u : 4u), h[f][d]);
-        });
+  try {
+    for (int f = 0; f < 2; ++f)
+      for (int d = 0; d < 2; ++d)
+        if (need[f][d])
+          workers.emplace_back([&, f, d]() {
+            try {
+              tile_host_build(n, rs, col, dia, order[d], d == 0, tile_rows(f ? 8u : 4u), h[f][d]);
+            } catch (...) {
+              h[f][d].ok = false;
+              failed = true;
+            }
+          });
+  } catch (...) {  // a thread that could not start: join the others before leaving
+    for (std::thread &w : workers) w.join();
+    throw;
+  }
   for (std::thread &w : workers) w.join();
+  if (failed) return fail(DFM2G_ERR_HOST, "tile schedule: out of host memory while partitioning");
   for (int f = 0; f < 2; ++f)
     for (int d = 0; d < 2; ++d)
       if (need[f][d]) DFM2G_TRY(tile_upload(n, h[f][d], p->tiles[f][d]));
