@@ -132,6 +132,25 @@ def test_fill_in_patterns(built_lib, port, k):
         assert m > 7
 
 
+@pytest.mark.parametrize("rows", [1617, 3185])
+def test_sweep_sizes_on_cloth_and_fill_in_patterns(built_lib, port, rows):
+    """The sweep's tile sizes (49 segments of at most 33 or 65 rows) on the
+    cloth sheet's quad pattern and on ILU(1) of a voxel block whose z lines
+    (41 rows) are cut in two at 33 rows and kept whole at 65: the partition's
+    invariants hold in both directions."""
+    import delfem2_gb300 as D
+    from delfem2_gb300.cloth import SetClothShape_Square
+    _, _, _, quad = SetClothShape_Square(20, 1.0)
+    ind, psup = port.psup(quad, 4, 21 * 21)
+    col, dia = port.ilu_pattern0(ind, psup)
+    a = D.voxel_problem_arrays(3, 3, 40, 1.0 / 3, young=1.0)
+    rs1, col1, dia1 = port.ilu_pattern_k(a["psup_ind"], a["psup"], 1)
+    for rs_, col_, dia_ in ((np.asarray(ind), col, dia), (rs1, col1, dia1)):
+        for backward in (False, True):
+            tile_of, level, nt, m, order = _partition(built_lib, port, rs_, col_, dia_, backward, rows, 49)
+            _check(rs_, col_, dia_, order, tile_of, level, nt, m, backward, rows, 49)
+
+
 def test_empty_pattern_and_arguments(built_lib):
     z = np.zeros(1, np.uint32)
     nt, m = C.c_uint(7), C.c_uint(7)
