@@ -19,7 +19,10 @@
  *    flag says (DFM2G_MEM_HOST / DFM2G_MEM_DEVICE). Device pointers must be on
  *    the library's current device; host pointers are copied in/out.
  *  - All work is queued on the library stream (dfm2g_set_stream); calls that
- *    return host data synchronise it.
+ *    return host data synchronise it. The library keeps one device context
+ *    and one stream: call it from one host thread at a time (the error
+ *    message is per thread; handles and cached kernel settings are shared
+ *    and not locked).
  *  - Block sizes 1x1, 2x2 and 3x3 (ndim 1, 2, 3). The 3x3 path is the tuned
  *    one (TMA-staged SpMV, every sweep schedule); 1x1 and 2x2 matrices run
  *    warp-per-row kernels with the sync-free and level sweep schedules.
