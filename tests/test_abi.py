@@ -1,5 +1,6 @@
 """C-ABI library: loads without a GPU, exports every entry point include/dfm2g.h
 declares, and its host-only helpers (mesh, pattern) are bit-exact vs the oracle."""
+import ctypes as C
 import os
 import re
 
@@ -76,3 +77,7 @@ def test_bad_arguments_fail_before_any_device_work(built_lib):
     with pytest.raises(TypeError):
         from delfem2_gb300.ls import _vec
         _vec(np.zeros(3, np.float32), np.float64, True)
+    from delfem2_gb300 import _native as N
+    m = C.c_int(5)
+    assert built_lib.dfm2g_ilu_last_schedule(None, N.F32, 0, C.byref(m)) == N.ERR_ARG and m.value == 5
+    assert b"null ILU handle" in built_lib.dfm2g_last_error()
